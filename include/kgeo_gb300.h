@@ -1,0 +1,103 @@
+/*
+ * kgeo_gb300 C ABI: the analytic Kerr null-geodesic tracer on one GB300 (sm_103a).
+ *
+ * Every entry point is stream-ordered and takes device pointers (CUDA global
+ * memory) sized as documented; nothing is copied to or from the host except
+ * where a function says so. Arrays of samples are (n_samples, npix) row-major,
+ * the layout of the reference's numpy output. Any output pointer may be NULL,
+ * in which case that output is not written. Return values are kgeo_status codes;
+ * conditions only known on the device (see KGEO_FLAG_*) are reported in the
+ * caller-visible flags word after the stream has run.
+ *
+ * The reference (achael/kgeo) is a Python library with no FFI; each declaration
+ * below names the Python call it replaces (file:line in the reference).
+ */
+#ifndef KGEO_GB300_H
+#define KGEO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KGEO_ABI_VERSION 1
+
+/* Return codes. The argument errors correspond one-to-one to the reference's
+ * exceptions (kgeo/kerr_raytracing_ana.py:59-71, kgeo/equatorial_lensing.py:100-101). */
+typedef enum {
+  KGEO_OK = 0,
+  KGEO_ERR_SPIN = 1,        /* "|a| should be a float in range [0,1)" */
+  KGEO_ERR_R_O = 2,         /* "r_o should be a float > 100" */
+  KGEO_ERR_TH_O = 3,        /* "th_o should be a float in range (0,pi/2) or (pi/2,pi)" */
+  KGEO_ERR_LENGTHS = 4,     /* "alpha, beta are different lengths!" / bad npix */
+  KGEO_ERR_NGEO = 5,        /* negative sample count */
+  KGEO_ERR_MBAR = 6,        /* "mbar should be an integer >=0!" */
+  KGEO_ERR_WORKSPACE = 7,   /* workspace too small */
+  KGEO_ERR_NULL = 8,        /* a required pointer is NULL */
+  KGEO_ERR_CUDA = 9,        /* a CUDA runtime call failed */
+  KGEO_ERR_MODEL = 10       /* unknown / out-of-range emissivity or velocity model parameter */
+} kgeo_status;
+
+/* Bits of the device flags word written by the tracing entry points. */
+#define KGEO_FLAG_ANY_ETA_POS 1u
+#define KGEO_FLAG_ANY_ETA_NONPOS 2u
+#define KGEO_FLAG_ANY_STEP_ZERO 4u
+/* |a| < 1e-4 and some pixel has eta == 0: the reference raises
+ * "below MINSPIN but there are eta<0 points in th_integrate!" (kgeo/kerr_raytracing_ana.py:301-302) */
+#define KGEO_FLAG_MINSPIN_VORTICAL 8u
+
+/* Observer: spin a (|a| < 1), radius r_o (>= 100, may be +inf), inclination th_o in (0, pi) minus pi/2. */
+typedef struct {
+  double a;
+  double r_o;
+  double th_o;
+} kgeo_observer;
+
+/* Outputs of a trace. Sample arrays are (n_samples, npix); per-pixel arrays are (npix). */
+typedef struct {
+  double* t;          /* Boyer-Lindquist t */
+  double* r;          /* r */
+  double* th;         /* theta */
+  double* ph;         /* phi */
+  double* sig;        /* affine parameter sigma (Geodesics.affine_times) */
+  double* mino;       /* Mino time tau of each sample (Geodesics.mino_times) */
+  double* tau_tot;    /* total Mino time per pixel (before maxtaufrac) */
+  int32_t* rclass;    /* radial class 1..4 (kgeo/kerr_raytracing_utils.py:365-378) */
+  int32_t* thclass;   /* angular class 1..3 (kgeo/kerr_raytracing_utils.py:265-272) */
+  uint32_t* flags;    /* one device word, KGEO_FLAG_* bits (cleared by the call) */
+} kgeo_geodesics;
+
+/* Bytes of device scratch that kgeo_raytrace / kgeo_coords_at_tau need for npix pixels. */
+size_t kgeo_workspace_size(int64_t npix);
+
+/* raytrace_ana(a, observer_coords, image_coords, ngeo, maxtaufrac)
+ * (kgeo/kerr_raytracing_ana.py:46-122): ngeo samples per pixel, evenly spaced in Mino
+ * time from 0 to maxtaufrac * tau_tot (numpy.linspace arithmetic).
+ * alpha, beta: (npix) device arrays. workspace: device scratch of at least
+ * kgeo_workspace_size(npix) bytes, or NULL to let the call allocate (and free) it
+ * stream-ordered. stream: a cudaStream_t (NULL = default stream). */
+int kgeo_raytrace(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                  int32_t ngeo, double maxtaufrac, kgeo_geodesics* out, void* workspace,
+                  size_t workspace_bytes, void* stream);
+
+/* coords_at_tau(a, observer_coords, image_coords, tau, do_phi_and_t)
+ * (kgeo/kerr_raytracing_ana.py:126-193): coordinates at caller-given Mino times
+ * tau (ntau, npix). With do_phi_and_t == 0 only r and theta are meaningful
+ * (t, ph, sig are written as the reference leaves them: zero-based partial sums). */
+int kgeo_coords_at_tau(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                       const double* tau, int32_t ntau, int32_t do_phi_and_t, kgeo_geodesics* out,
+                       void* workspace, size_t workspace_bytes, void* stream);
+
+/* Human-readable text of a kgeo_status code (the reference's exception message where one exists). */
+const char* kgeo_status_string(int status);
+
+/* ABI version (KGEO_ABI_VERSION of the library that was built). */
+int kgeo_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KGEO_GB300_H */

@@ -1,0 +1,83 @@
+"""ctypes binding of libkgeo_gb300.so (the C ABI declared in include/kgeo_gb300.h).
+
+There is no CPU fallback: every call needs the CUDA library and a CUDA device, and
+fails loudly without them.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+c_double = ctypes.c_double
+c_int = ctypes.c_int
+c_int32 = ctypes.c_int32
+c_int64 = ctypes.c_int64
+c_size_t = ctypes.c_size_t
+c_void_p = ctypes.c_void_p
+
+
+class Observer(ctypes.Structure):
+    _fields_ = [('a', c_double), ('r_o', c_double), ('th_o', c_double)]
+
+
+class GeodesicsOut(ctypes.Structure):
+    _fields_ = [('t', c_void_p), ('r', c_void_p), ('th', c_void_p), ('ph', c_void_p), ('sig', c_void_p),
+                ('mino', c_void_p), ('tau_tot', c_void_p), ('rclass', c_void_p), ('thclass', c_void_p),
+                ('flags', c_void_p)]
+
+
+# name -> (restype, argtypes); kept in step with include/kgeo_gb300.h
+SIGNATURES = {
+    'kgeo_workspace_size': (c_size_t, [c_int64]),
+    'kgeo_raytrace': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_int32, c_double,
+                              ctypes.POINTER(GeodesicsOut), c_void_p, c_size_t, c_void_p]),
+    'kgeo_coords_at_tau': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_void_p, c_int32,
+                                   c_int32, ctypes.POINTER(GeodesicsOut), c_void_p, c_size_t, c_void_p]),
+    'kgeo_status_string': (ctypes.c_char_p, [c_int]),
+    'kgeo_abi_version': (c_int, []),
+}
+
+FLAG_ANY_ETA_POS = 1
+FLAG_ANY_ETA_NONPOS = 2
+FLAG_ANY_STEP_ZERO = 4
+FLAG_MINSPIN_VORTICAL = 8
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load():
+    """Load libkgeo_gb300.so (building it first if the sources are newer)."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if not os.path.exists(path):
+            raise RuntimeError('kgeo_gb300: CUDA library %s is not built; run python kgeo_gb300/build.py '
+                               '(or __graft_entry__.build())' % path)
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def status_string(code):
+    return load().kgeo_status_string(code).decode()
+
+
+class KgeoError(Exception):
+    """A non-zero kgeo_status from the C ABI."""
+
+    def __init__(self, code):
+        self.code = code
+        super().__init__(status_string(code))
+
+
+def check(code):
+    if code != 0:
+        raise KgeoError(code)

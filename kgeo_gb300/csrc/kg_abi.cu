@@ -1,0 +1,156 @@
+// C ABI of the kgeo GB300 tracer (declarations and contracts: include/kgeo_gb300.h).
+#include <cmath>
+#include <cstring>
+
+#include "../../include/kgeo_gb300.h"
+#include "kg_launch.h"
+
+using namespace kg;
+
+namespace {
+
+// Observer checks with the reference's rules (kgeo/kerr_raytracing_ana.py:59-65).
+int check_observer(const kgeo_observer* o) {
+  if (!o) return KGEO_ERR_NULL;
+  if (!(std::fabs(o->a) >= 0 && std::fabs(o->a) < 1)) return KGEO_ERR_SPIN;
+  if (!(o->r_o >= 100)) return KGEO_ERR_R_O;
+  if (!(o->th_o > 0 && o->th_o < PI && o->th_o != 0.5 * PI)) return KGEO_ERR_TH_O;
+  return KGEO_OK;
+}
+
+// Per-image constants with the host libm, as numpy computes them for a Python float.
+Observer make_observer(const kgeo_observer* o) {
+  Observer ob;
+  ob.a = o->a;
+  ob.a2 = o->a * o->a;
+  ob.r_o = o->r_o;
+  ob.th_o = o->th_o;
+  ob.sin_th = std::sin(o->th_o);
+  ob.cos_th = std::cos(o->th_o);
+  ob.cos2 = ob.cos_th * ob.cos_th;
+  double root = std::sqrt(1 - ob.a2);
+  ob.rplus = 1 + root;
+  ob.rminus = 1 - root;
+  ob.minspin = std::fabs(o->a) < MINSPIN;
+  ob.r_o_inf = std::isinf(o->r_o) ? 1 : 0;
+  return ob;
+}
+
+struct Scratch {
+  void* ptr = nullptr;
+  bool owned = false;
+  cudaStream_t s = nullptr;
+  ~Scratch() {
+    if (owned && ptr) cudaFreeAsync(ptr, s);
+  }
+};
+
+int get_scratch(Scratch& sc, void* workspace, size_t bytes, int64_t npix, cudaStream_t s) {
+  size_t need = workspace_bytes(npix);
+  sc.s = s;
+  if (workspace) {
+    if (bytes < need) return KGEO_ERR_WORKSPACE;
+    sc.ptr = workspace;
+    return KGEO_OK;
+  }
+  if (cudaMallocAsync(&sc.ptr, need, s) != cudaSuccess) return KGEO_ERR_CUDA;
+  sc.owned = true;
+  return KGEO_OK;
+}
+
+int trace_common(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                 int64_t nsamp, const double* tau, int do_phi_t, double maxtaufrac, kgeo_geodesics* out,
+                 void* workspace, size_t workspace_bytes_, void* stream) {
+  int st = check_observer(obs);
+  if (st) return st;
+  if (npix < 0) return KGEO_ERR_LENGTHS;
+  if (nsamp < 0) return KGEO_ERR_NGEO;
+  if (!out) return KGEO_ERR_NULL;
+  if (npix > 0 && (!alpha || !beta)) return KGEO_ERR_NULL;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Scratch sc;
+  st = get_scratch(sc, workspace, workspace_bytes_, npix, s);
+  if (st) return st;
+  Workspace w = carve_workspace(sc.ptr, npix);
+  if (cudaMemsetAsync(w.flags, 0, sizeof(uint32_t), s) != cudaSuccess) return KGEO_ERR_CUDA;
+  if (npix == 0) {
+    if (out->flags && cudaMemsetAsync(out->flags, 0, sizeof(uint32_t), s) != cudaSuccess) return KGEO_ERR_CUDA;
+    return KGEO_OK;
+  }
+  SetupArgs sa;
+  sa.obs = make_observer(obs);
+  sa.alpha = alpha;
+  sa.beta = beta;
+  sa.npix = npix;
+  sa.ngeo = tau ? 0 : nsamp;
+  sa.maxtaufrac = maxtaufrac;
+  sa.rec = w.rec;
+  sa.code = w.code;
+  sa.rclass = out->rclass;
+  sa.thclass = out->thclass;
+  sa.tau_tot = out->tau_tot;
+  sa.flags = w.flags;
+  if (launch_ray_setup(sa, s) != cudaSuccess) return KGEO_ERR_CUDA;
+  SampleArgs pa;
+  pa.obs = sa.obs;
+  pa.rec = w.rec;
+  pa.code = w.code;
+  pa.npix = npix;
+  pa.nsamp = nsamp;
+  pa.tau = tau;
+  pa.do_phi_t = do_phi_t;
+  pa.flags = w.flags;
+  pa.t = out->t;
+  pa.r = out->r;
+  pa.th = out->th;
+  pa.ph = out->ph;
+  pa.sig = out->sig;
+  pa.mino = out->mino;
+  if (launch_samples(pa, s) != cudaSuccess) return KGEO_ERR_CUDA;
+  if (out->flags &&
+      cudaMemcpyAsync(out->flags, w.flags, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return KGEO_ERR_CUDA;
+  return KGEO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t kgeo_workspace_size(int64_t npix) { return workspace_bytes(npix); }
+
+int kgeo_raytrace(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                  int32_t ngeo, double maxtaufrac, kgeo_geodesics* out, void* workspace,
+                  size_t workspace_bytes_, void* stream) {
+  return trace_common(obs, alpha, beta, npix, ngeo, nullptr, 1, maxtaufrac, out, workspace, workspace_bytes_,
+                      stream);
+}
+
+int kgeo_coords_at_tau(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                       const double* tau, int32_t ntau, int32_t do_phi_and_t, kgeo_geodesics* out,
+                       void* workspace, size_t workspace_bytes_, void* stream) {
+  if (ntau > 0 && npix > 0 && !tau) return KGEO_ERR_NULL;
+  return trace_common(obs, alpha, beta, npix, ntau, tau, do_phi_and_t ? 1 : 0, 1.0, out, workspace,
+                      workspace_bytes_, stream);
+}
+
+const char* kgeo_status_string(int status) {
+  switch (status) {
+    case KGEO_OK: return "ok";
+    case KGEO_ERR_SPIN: return "|a| should be a float in range [0,1)";
+    case KGEO_ERR_R_O: return "r_o should be a float > 100";
+    case KGEO_ERR_TH_O: return "th_o should be a float in range (0,pi/2) or (pi/2,pi)";
+    case KGEO_ERR_LENGTHS: return "alpha, beta are different lengths!";
+    case KGEO_ERR_NGEO: return "ngeo must be >= 0";
+    case KGEO_ERR_MBAR: return "mbar should be an integer >=0!";
+    case KGEO_ERR_WORKSPACE: return "workspace too small";
+    case KGEO_ERR_NULL: return "a required pointer is NULL";
+    case KGEO_ERR_CUDA: return "CUDA runtime error";
+    case KGEO_ERR_MODEL: return "emissivity / velocity model parameter out of range";
+    default: return "unknown status";
+  }
+}
+
+int kgeo_abi_version(void) { return KGEO_ABI_VERSION; }
+
+}  // extern "C"

@@ -1,0 +1,805 @@
+// Per-ray setup and per-sample evaluation of the analytic Kerr null geodesic
+// (Gralla & Lupsasca 2019a/b), FP64.
+//
+// ray_setup() follows kgeo's per-pixel chain: conserved quantities
+// (kgeo/kerr_raytracing_ana.py:76-82), u_+/u_- with their clamps
+// (kgeo/kerr_raytracing_utils.py:276-328), the radial quartic roots and rclass
+// (:330-380), the total Mino time (:382-548) and every ray-constant term of the theta
+// (kgeo/kerr_raytracing_ana.py:216-363) and r (:404-624) antiderivatives. It is
+// compiled without FMA contraction so that its roundings follow numpy's one-op-at-a-time
+// evaluation, which keeps the exact-zero classification tests faithful.
+//
+// sample_*() evaluate r, theta, G_phi, G_t, I_phi, I_t, I_sigma at one Mino time from
+// that record. The elliptic work is reorganised for the GPU: the Jacobi argument is
+// reduced by its half period (am(u + 2K) = am(u) + pi) and sn, cn, dn come from one
+// Landen evaluation; F, E and every Pi at the same amplitude share one Carlson
+// duplication loop (rj_multi), and the periodic parts are ray constants.
+#pragma once
+
+#include "kg_common.cuh"
+#include "kg_cplx.cuh"
+#include "kg_elliptic.cuh"
+
+namespace kg {
+
+// Per-image constants, evaluated once on the host with the host libm (as numpy does).
+struct Observer {
+  double a, a2;           // spin, a**2
+  double r_o;             // observer radius (may be +inf)
+  double th_o;            // inclination
+  double sin_th, cos_th;  // np.sin(th_o), np.cos(th_o)
+  double cos2;            // np.cos(th_o)**2
+  double rplus, rminus;   // 1 +- sqrt(1 - a**2)
+  int minspin;            // |a| < MINSPIN
+  int r_o_inf;            // r_o == inf
+};
+
+// Status bits shared by all rays of a launch (atomicOr).
+enum : unsigned {
+  FLAG_ANY_ETA_POS = 1u,     // some pixel has eta > 0 (ordinary branch runs, eta == 0 joins it)
+  FLAG_ANY_ETA_NONPOS = 2u,  // some pixel has eta <= 0
+  FLAG_ANY_STEP_ZERO = 4u,   // some pixel has a zero Mino step (numpy linspace's denormal path)
+  FLAG_MINSPIN_VORTICAL = 8u // |a| < MINSPIN with eta <= 0: the reference raises
+};
+
+// Radial integration case (kgeo/kerr_raytracing_ana.py:404, 473, 554).
+enum : int { RCASE_NONE = 0, RCASE_2 = 2, RCASE_3 = 3, RCASE_4 = 4 };
+// Theta branch (kgeo/kerr_raytracing_ana.py:216, 298).
+enum : int { TH_ZERO = 0, TH_ORD = 1, TH_VORT = 2 };
+
+// Field indices of the per-ray record (structure of arrays: rec[field * npix + ray]).
+enum RecField : int {
+  F_LAM = 0, F_S, F_TAUMAX, F_TAUTOT,
+  // theta
+  T_SCALE, T_GTH, T_M, T_S1M, T_K2, T_N, T_KK, T_PIC, T_EC, T_KC, T_PREF, T_GPH, T_GT,
+  T_UP, T_UM, T_PREFC, T_H,
+  // radial, common
+  R_XS, R_IRO, R_M, R_K2, R_KC, R_EC, R_N0, R_N1, R_N2, R_PIC0, R_PIC1, R_PIC2,
+  // radial, case-specific
+  R_C0, R_C1, R_C2, R_C3, R_C4, R_C5, R_C6, R_C7, R_C8, R_C9, R_C10, R_C11, R_C12, R_C13,
+  R_C14, R_C15, R_C16, R_C17, R_C18, R_C19,
+  NUM_FIELDS
+};
+
+// Strided view of one ray's record inside the structure-of-arrays buffer.
+struct RecView {
+  const double* base;  // &rec[ray]
+  int64_t stride;      // npix
+  KG_HD double operator[](int k) const {
+#if defined(__CUDA_ARCH__)
+    return __ldg(base + (int64_t)k * stride);
+#else
+    return base[(int64_t)k * stride];
+#endif
+  }
+};
+
+struct RayRec {
+  double f[NUM_FIELDS];
+  int code;  // rcase | thbranch << 4 | (kk == 0) << 8 | minspin << 9
+};
+
+KG_HD int code_rcase(int code) { return code & 15; }
+KG_HD int code_th(int code) { return (code >> 4) & 15; }
+KG_HD bool code_kk0(int code) { return (code >> 8) & 1; }
+KG_HD bool code_minspin(int code) { return (code >> 9) & 1; }
+
+// ---------------------------------------------------------------------------
+// building blocks at a generic amplitude (ray constants)
+// ---------------------------------------------------------------------------
+
+// S1, S2 of GL19a B92/B93 (kgeo/kerr_raytracing_ana.py:638-663) at amplitude phi.
+KG_HD void s1s2_at(double al, double phi, double j, bool want_s2, double* S1, double* S2) {
+  double al2 = al * al;
+  double al2p1 = 1 + al2;
+  double al2j = 1 - j + al2;
+  double sphi = sin(phi);
+  double s2phi = sqrt(1. - j * (sphi * sphi));
+  double p2 = sqrt(al2p1 / al2j);
+  double f2 = 0.5 * p2 * log(fabs(((1 - p2) * (1 + p2 * s2phi)) / ((1 + p2) * (1 - p2 * s2phi))));
+  double F = ellip_f(phi, j);
+  *S1 = (F + al2 * ellip_pi_ref(al2p1, phi, j) - al * f2) / al2p1;
+  if (want_s2) {
+    double E = ellip_e_inc(phi, j);
+    double tanphi = tan(phi);
+    double S2a = (1 - j) * F + al2 * E + al2 * s2phi * (al - tanphi) / (1 + al * tanphi) - al2 * al;
+    S2a = -S2a / (al2p1 * al2j);
+    double S2b = *S1 * (1. / al2p1 + (1 - j) / al2j);
+    *S2 = S2a + S2b;
+  }
+}
+
+// R1, R2 of GL19a B62/B65 (kgeo/kerr_raytracing_ana.py:666-683) at amplitude phi.
+KG_HD void r1r2_at(double al, double phi, double j, bool want_r2, double* R1, double* R2) {
+  double al2 = al * al;
+  double sphi = sin(phi);
+  double s2phi = sqrt(1 - j * (sphi * sphi));
+  double p1 = sqrt((al2 - 1) / (j + (1 - j) * al2));
+  double f1 = 0.5 * p1 * log(fabs((p1 * s2phi + sphi) / (p1 * s2phi - sphi)));
+  double nn = al2 / (al2 - 1);
+  *R1 = (ellip_pi_ref(nn, phi, j) - al * f1) / (1 - al2);
+  if (want_r2) {
+    double F = ellip_f(phi, j);
+    double E = ellip_e_inc(phi, j);
+    double r2 = (F - (al2 / (j + (1 - j) * al2)) * (E - al * sphi * s2phi / (1 + al * cos(phi)))) / (al2 - 1);
+    *R2 = r2 + (2 * j - nn) * *R1 / (j + (1 - j) * al2);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per-ray setup
+// ---------------------------------------------------------------------------
+
+struct Roots {
+  cplx r1, r2, r3, r4;
+  int rclass;
+};
+
+// kgeo/kerr_raytracing_utils.py:330-380
+KG_HD Roots radial_roots(const Observer& o, double lam, double eta) {
+  double A = o.a2 - eta - lam * lam;
+  double lma = lam - o.a;
+  double B = 2 * (eta + lma * lma);
+  double C = -(o.a2) * eta;
+  double P = -(A * A) / 12. - C;
+  double Q = (-A / 3.) * ((A * A) / 36. - C) - (B * B) / 8.;
+  cplx disc = cx_real(4 * cube_rn(P) + 27 * (Q * Q));
+  cplx sd = csqrt(disc / cx_real(108.));
+  cplx wp3 = cx_real(-0.5 * Q) + sd;
+  cplx wm3 = cx_real(-0.5 * Q) - sd;
+  cplx xi0 = cbrt_max_real(wp3) + cbrt_max_real(wm3) - cx_real(A / 3.);
+  cplx z = csqrt(cx_real(0.5) * xi0);
+  cplx zz = z * z;
+  cplx bz = cx_real(0.25 * B) / z;
+  cplx base = cx_real(-0.5 * A) - zz;
+  cplx s_lo = csqrt(base + bz);
+  cplx s_hi = csqrt(base - bz);
+  Roots R;
+  R.r1 = -z - s_lo;
+  R.r2 = -z + s_lo;
+  R.r3 = z - s_hi;
+  R.r4 = z + s_hi;
+  int rc = 0;
+  if (R.r2.im != 0) rc = 4;
+  if (R.r2.im == 0 && R.r4.im != 0) rc = 3;
+  if (R.r2.im == 0 && R.r4.im == 0 && R.r4.re < o.rplus) rc = 2;
+  if (R.r2.im == 0 && R.r4.im == 0 && R.r4.re > o.rplus) rc = 1;
+  R.rclass = rc;
+  return R;
+}
+
+// Everything that depends only on the ray. Writes the record, returns the flags it raises.
+// `anyflags` are the launch-wide flags (only FLAG_ANY_ETA_POS is read, and only by
+// eta == 0 rays; pass FLAG_ANY_ETA_POS when unknown and fix up later).
+KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double maxtaufrac,
+                         RayRec* rec, int* rclass_out, int* thclass_out) {
+  unsigned flags = 0;
+  double* f = rec->f;
+  for (int i = 0; i < NUM_FIELDS; ++i) f[i] = 0.0;
+  const double a = o.a, a2 = o.a2;
+
+  // conserved quantities, kgeo/kerr_raytracing_ana.py:151-158
+  double lam = -alpha * o.sin_th;
+  double eta = (alpha * alpha - a2) * o.cos2 + beta * beta;
+  if (o.minspin && eta < 0) eta = EP;
+  if (eta > 0) flags |= FLAG_ANY_ETA_POS;
+  if (eta <= 0) flags |= FLAG_ANY_ETA_NONPOS;
+  if (o.minspin && eta <= 0) flags |= FLAG_MINSPIN_VORTICAL;
+  double s = beta >= 0 ? 1.0 : -1.0;  // my_sign, kgeo/kerr_raytracing_utils.py:857-864
+  f[F_LAM] = lam;
+  f[F_S] = s;
+
+  // u_+, u_- with clamps, kgeo/kerr_raytracing_utils.py:290-326 (aliased below MINSPIN)
+  double up, um;
+  if (o.minspin) {
+    up = eta / (eta + lam * lam);
+    if ((o.cos2 - up) > 0) up = o.cos2;
+    if (up * up > 1) up = 1;
+    if (up == 0 && eta < 0) up = EP;
+    if (up == 0 && eta >= 0) up = -EP;
+    if (eta < 0 && (o.cos2 - up) < 0) up = o.cos2;
+    um = up;
+  } else {
+    double half = 0.5 * (1 - (eta + lam * lam) / (a * a));
+    double root = sqrt(half * half + eta / (a * a));
+    up = half + root;
+    um = half - root;
+    if ((o.cos2 - up) > 0) up = o.cos2;
+    if (up * up > 1) up = 1;
+    if (um == 0 && eta < 0) um = EP;
+    if (um == 0 && eta >= 0) um = -EP;
+    if (eta < 0 && (o.cos2 - um) < 0) um = o.cos2;
+  }
+  *thclass_out = eta > 0 ? 1 : (eta < 0 ? 2 : 3);
+
+  // radial roots and rclass
+  Roots R = radial_roots(o, lam, eta);
+  *rclass_out = R.rclass;
+
+  // ---- total Mino time, kgeo/kerr_raytracing_utils.py:382-548
+  const double rplus = o.rplus, rminus = o.rminus, r_o = o.r_o;
+  double tau_tot = 0.0;
+  bool m4 = R.r1.im != 0;
+  bool m3 = (R.r3.im != 0) && !m4;
+  bool mII = (R.r3.im == 0.) && (R.r3.re < rplus || (R.r3.re == rplus && R.r3.im < 0)) && !m3;
+  bool mI = (R.r3.im == 0.) && (R.r3.re > rplus || (R.r3.re == rplus && R.r3.im > 0)) && !mII;
+  if (m4) {
+    double a1 = R.r4.im, b1 = R.r4.re, a2i = R.r2.im, b2 = R.r2.re;
+    double CC = sqrt((a1 - a2i) * (a1 - a2i) + (b1 - b2) * (b1 - b2));
+    double DD = sqrt((a1 + a2i) * (a1 + a2i) + (b1 - b2) * (b1 - b2));
+    double k4 = (4 * CC * DD) / ((CC + DD) * (CC + DD));
+    double g0 = sqrt((4 * (a2i * a2i) - (CC - DD) * (CC - DD)) / ((CC + DD) * (CC + DD) - 4 * (a2i * a2i)));
+    double x4rp = (rplus + b1) / a2i;
+    double x4ro = o.r_o_inf ? kg_inf() : (r_o + b1) / a2i;
+    double pref = 2. / (CC + DD);
+    double I4rp = pref * ellip_f(atan(x4rp) + atan(g0), k4);
+    double I4ro = pref * ellip_f(atan(x4ro) + atan(g0), k4);
+    tau_tot = I4ro - I4rp;
+  }
+  if (m3) {
+    double a1 = R.r4.im, b1 = R.r4.re, rr1 = R.r1.re, rr2 = R.r2.re;
+    double rr21 = rr2 - rr1;
+    double rrp1 = rplus - rr1, rrp2 = rplus - rr2;
+    double AA = sqrt(a1 * a1 + (b1 - rr2) * (b1 - rr2));
+    double BB = sqrt(a1 * a1 + (b1 - rr1) * (b1 - rr1));
+    double k3 = ((AA + BB) * (AA + BB) - rr21 * rr21) / (4 * AA * BB);
+    double x3rp = (AA * rrp1 - BB * rrp2) / (AA * rrp1 + BB * rrp2);
+    double x3ro;
+    if (o.r_o_inf) x3ro = (AA - BB) / (AA + BB);
+    else x3ro = (AA * (r_o - rr1) - BB * (r_o - rr2)) / (AA * (r_o - rr1) + BB * (r_o - rr2));
+    double pref = 1. / sqrt(AA * BB);
+    double I3rp = pref * ellip_f(acos(x3rp), k3);
+    double I3ro = pref * ellip_f(acos(x3ro), k3);
+    tau_tot = I3ro - I3rp;
+  }
+  if (mII || mI) {
+    double rr1 = R.r1.re, rr2 = R.r2.re, rr3 = R.r3.re, rr4 = R.r4.re;
+    double rr31 = rr3 - rr1, rr32 = rr3 - rr2, rr41 = rr4 - rr1, rr42 = rr4 - rr2;
+    double k2 = (rr32 * rr41) / (rr31 * rr42);
+    double x2ro = o.r_o_inf ? sqrt(rr31 / rr41) : sqrt((rr31 * (r_o - rr4)) / (rr41 * (r_o - rr3)));
+    double pref = 2. / sqrt(rr31 * rr42);
+    if (mII) {
+      double x2rp = sqrt((rr31 * (rplus - rr4)) / (rr41 * (rplus - rr3)));
+      double I2rp = pref * ellip_f(asin(x2rp), k2);
+      double I2ro = pref * ellip_f(asin(x2ro), k2);
+      tau_tot = I2ro - I2rp;
+    } else {
+      double I2ro = pref * ellip_f(asin(x2ro), k2);
+      tau_tot = 2 * I2ro;
+    }
+  }
+  f[F_TAUTOT] = tau_tot;
+  double taumax = maxtaufrac * tau_tot;
+  f[F_TAUMAX] = taumax;
+
+  // ---- theta constants, kgeo/kerr_raytracing_ana.py:216-363
+  int th = TH_ZERO;
+  bool kk0 = false;
+  if (eta >= 0.) {
+    // ordinary (taken by eta == 0 rays only when some eta > 0; the kernel decides)
+    th = TH_ORD;
+    double kk, a2um;
+    if (o.minspin) {
+      kk = 0.0;
+      a2um = -(eta + lam * lam);
+      kk0 = true;
+    } else {
+      kk = up / um;
+      a2um = a * a * um;
+      kk0 = (kk == 0);
+    }
+    double pref = 1 / sqrt(-a2um);
+    double arg = asin(o.cos_th / sqrt(up));
+    double F = ellip_f(arg, kk);
+    double Gth_o = -pref * F;
+    double Gph_o = -pref * ellip_pi_ref(up, arg, kk);
+    double Gt_o;
+    if (kk == 0) Gt_o = 2 * up * pref * 0.125 * (-2 * arg + sin(2 * arg));
+    else Gt_o = 2 * up * pref * (ellip_e_inc(arg, kk) - F) / (2 * kk);
+    double m = kk / (kk - 1);
+    f[T_SCALE] = sqrt(-a2um);
+    f[T_GTH] = Gth_o;
+    f[T_M] = m;
+    f[T_S1M] = sqrt(1 - m);
+    f[T_K2] = 2.0 * ellip_k(m);
+    f[T_N] = up;
+    f[T_KK] = kk;
+    f[T_PIC] = ellip_pi_ref(up, HALFPI, kk);
+    f[T_EC] = ellip_e(kk);
+    f[T_KC] = ellip_k(kk);
+    f[T_PREF] = pref;
+    f[T_GPH] = Gph_o;
+    f[T_GT] = Gt_o;
+    f[T_UP] = up;
+    f[T_UM] = um;
+  }
+  if (eta < 0.) {
+    th = TH_VORT;
+    double ratio = up / um;
+    double a2um = a * a * um;
+    double h = (o.th_o <= PI / 2) ? 1. : -1.;
+    double prefA = 1 / sqrt(a2um);
+    double prefB = prefA / (1. - um);
+    double prefC = sqrt(um / (a * a));
+    double nu_o = asin(sqrt((o.cos2 - um) / (up - um)));
+    double kk = 1 - ratio;
+    double upm = (up - um) / (1. - um);
+    double Gth_o = -h * prefA * ellip_f(nu_o, kk);
+    double Gph_o = -h * prefB * ellip_pi_ref(upm, nu_o, kk);
+    double Gt_o = -h * prefC * ellip_e_inc(nu_o, kk);
+    double m = kk / (kk - 1);
+    f[T_SCALE] = sqrt(a2um);
+    f[T_GTH] = Gth_o;
+    f[T_M] = m;
+    f[T_S1M] = sqrt(1 - m);
+    f[T_K2] = 2.0 * ellip_k(m);
+    f[T_N] = upm;
+    f[T_KK] = kk;
+    f[T_PIC] = ellip_pi_ref(upm, HALFPI, kk);
+    f[T_EC] = ellip_e(kk);
+    f[T_KC] = ellip_k(kk);
+    f[T_PREF] = prefB;
+    f[T_GPH] = Gph_o;
+    f[T_GT] = Gt_o;
+    f[T_UP] = up;
+    f[T_UM] = um;
+    f[T_PREFC] = prefC;
+    f[T_H] = h;
+  }
+
+  // ---- radial constants, kgeo/kerr_raytracing_ana.py:389-624
+  int rcase = RCASE_NONE;
+  bool c4 = R.r1.im != 0;
+  bool c3 = (R.r3.im != 0) && !c4;
+  bool c2 = (R.r3.im == 0.) && !c3;
+  if (c4) {
+    rcase = RCASE_4;
+    double a1 = R.r4.im, b1 = R.r4.re, a2i = R.r2.im, b2 = R.r2.re;
+    double CC = sqrt((a1 - a2i) * (a1 - a2i) + (b1 - b2) * (b1 - b2));
+    double DD = sqrt((a1 + a2i) * (a1 + a2i) + (b1 - b2) * (b1 - b2));
+    double k4 = (4 * CC * DD) / ((CC + DD) * (CC + DD));
+    double x4rp = (rplus + b1) / a2i;
+    double x4rm = (rminus + b1) / a2i;
+    double x4ro = o.r_o_inf ? kg_inf() : (r_o + b1) / a2i;
+    double g0 = sqrt((4 * (a2i * a2i) - (CC - DD) * (CC - DD)) / ((CC + DD) * (CC + DD) - 4 * (a2i * a2i)));
+    double gp = (g0 * x4rp - 1.) / (g0 + x4rp);
+    double gm = (g0 * x4rm - 1.) / (g0 + x4rm);
+    double aux = atan(x4ro) + atan(g0);
+    double pref = 2. / (CC + DD);
+    double Ir_o = pref * ellip_f(aux, k4);
+    double S1b0, S2b0, S1bp, S1bm, dummy;
+    s1s2_at(g0, aux, k4, true, &S1b0, &S2b0);
+    s1s2_at(gp, aux, k4, false, &S1bp, &dummy);
+    s1s2_at(gm, aux, k4, false, &S1bm, &dummy);
+    double aa0 = (a2i / g0) * (1 + g0 * g0);
+    double aa1 = (a2i / g0 - b1);
+    f[R_XS] = 1. / pref;
+    f[R_IRO] = Ir_o;
+    f[R_M] = k4;
+    f[R_KC] = ellip_k(k4);
+    f[R_K2] = 2.0 * f[R_KC];
+    f[R_EC] = ellip_e(k4);
+    f[R_N0] = 1 + g0 * g0;
+    f[R_N1] = 1 + gp * gp;
+    f[R_N2] = 1 + gm * gm;
+    f[R_PIC0] = ellip_pi_ref(f[R_N0], HALFPI, k4);
+    f[R_PIC1] = ellip_pi_ref(f[R_N1], HALFPI, k4);
+    f[R_PIC2] = ellip_pi_ref(f[R_N2], HALFPI, k4);
+    f[R_C0] = a2i;
+    f[R_C1] = b1;
+    f[R_C2] = g0;
+    f[R_C3] = gp;
+    f[R_C4] = gm;
+    f[R_C5] = S1b0;
+    f[R_C6] = S2b0;
+    f[R_C7] = S1bp;
+    f[R_C8] = S1bm;
+    f[R_C9] = pref * aa0;                                     // Pi_1 = s*pref*aa0*(..)
+    f[R_C10] = pref * (aa0 * aa0);                            // Pi_2
+    f[R_C11] = pref * (1 + g0 * g0) / (g0 * g0 + g0 * x4rp);  // Pi_p
+    f[R_C12] = pref * (1 + g0 * g0) / (g0 * g0 + g0 * x4rm);  // Pi_m
+    f[R_C13] = aa1;
+    f[R_C14] = g0 / (a2i - a2i * g0 * x4rp);
+    f[R_C15] = g0 / (a2i - a2i * g0 * x4rm);
+  }
+  if (c3) {
+    rcase = RCASE_3;
+    double a1 = R.r4.im, b1 = R.r4.re, rr1 = R.r1.re, rr2 = R.r2.re;
+    double rr21 = rr2 - rr1;
+    double rrp1 = rplus - rr1, rrp2 = rplus - rr2, rrm1 = rminus - rr1, rrm2 = rminus - rr2;
+    double AA = sqrt(a1 * a1 + (b1 - rr2) * (b1 - rr2));
+    double BB = sqrt(a1 * a1 + (b1 - rr1) * (b1 - rr1));
+    double k3 = ((AA + BB) * (AA + BB) - rr21 * rr21) / (4 * AA * BB);
+    double x3rp = (AA * rrp1 - BB * rrp2) / (AA * rrp1 + BB * rrp2);
+    double x3rm = (AA * rrm1 - BB * rrm2) / (AA * rrm1 + BB * rrm2);
+    double x3ro;
+    if (o.r_o_inf) x3ro = (AA - BB) / (AA + BB);
+    else x3ro = (AA * (r_o - rr1) - BB * (r_o - rr2)) / (AA * (r_o - rr1) + BB * (r_o - rr2));
+    double alp = -1. / x3rp;
+    double alm = -1. / x3rm;
+    double al0 = (BB + AA) / (BB - AA);
+    double aux = acos(x3ro);
+    double pref = (1. / sqrt(AA * BB));
+    double Ir_o = pref * ellip_f(aux, k3);
+    double R1b0, R2b0, R1bp, R1bm = 0.0, dummy;
+    r1r2_at(al0, aux, k3, true, &R1b0, &R2b0);
+    r1r2_at(alp, aux, k3, false, &R1bp, &dummy);
+    if (fabs(a) > MINSPIN) r1r2_at(alm, aux, k3, false, &R1bm, &dummy);
+    double sAB = sqrt(AA * BB);
+    f[R_XS] = 1. / pref;
+    f[R_IRO] = Ir_o;
+    f[R_M] = k3;
+    f[R_KC] = ellip_k(k3);
+    f[R_K2] = 2.0 * f[R_KC];
+    f[R_EC] = ellip_e(k3);
+    double a0s = al0 * al0, aps = alp * alp, ams = alm * alm;
+    f[R_N0] = a0s / (a0s - 1);
+    f[R_N1] = aps / (aps - 1);
+    f[R_N2] = ams / (ams - 1);
+    f[R_PIC0] = ellip_pi_ref(f[R_N0], HALFPI, k3);
+    f[R_PIC1] = ellip_pi_ref(f[R_N1], HALFPI, k3);
+    f[R_PIC2] = ellip_pi_ref(f[R_N2], HALFPI, k3);
+    f[R_C0] = AA;
+    f[R_C1] = BB;
+    f[R_C2] = rr1;
+    f[R_C3] = rr2;
+    f[R_C4] = al0;
+    f[R_C5] = alp;
+    f[R_C6] = alm;
+    f[R_C7] = R1b0;
+    f[R_C8] = R2b0;
+    f[R_C9] = R1bp;
+    f[R_C10] = R1bm;
+    f[R_C11] = (2 * rr21 * sAB) / (BB * BB - AA * AA);    // Pi_1 coefficient
+    f[R_C12] = (2 * rr21 * sAB) / (BB * rrp2 - AA * rrp1);  // Pi_p
+    f[R_C13] = (2 * rr21 * sAB) / (BB * rrm2 - AA * rrm1);  // Pi_m
+    f[R_C14] = ((BB * rr2 + AA * rr1) / (BB + AA));        // pref of I1/I2
+    f[R_C15] = sAB;
+    f[R_C16] = (BB * rrp2 + AA * rrp1);
+    f[R_C17] = (BB * rrm2 + AA * rrm1);
+    f[R_C18] = sqrt((a0s - 1) / (k3 + (1 - k3) * a0s));  // p1 of R1_R2 for al0, alp, alm
+    f[R_C19] = sqrt((aps - 1) / (k3 + (1 - k3) * aps));
+    // p1 of alm is evaluated per sample (R_C slots are full)
+  }
+  if (c2) {
+    rcase = RCASE_2;
+    double rr1 = R.r1.re, rr2 = R.r2.re, rr3 = R.r3.re, rr4 = R.r4.re;
+    double rr31 = rr3 - rr1, rr32 = rr3 - rr2, rr41 = rr4 - rr1, rr42 = rr4 - rr2, rr43 = rr4 - rr3;
+    double rrp3 = rplus - rr3, rrm3 = rminus - rr3, rrp4 = rplus - rr4, rrm4 = rminus - rr4;
+    double k2 = (rr32 * rr41) / (rr31 * rr42);
+    double x2ro = o.r_o_inf ? sqrt(rr31 / rr41) : sqrt((rr31 * (r_o - rr4)) / (rr41 * (r_o - rr3)));
+    double aux = asin(x2ro);
+    double Ir_o = 2 * ellip_f(aux, k2) / sqrt(rr31 * rr42);
+    double n1 = rr41 / rr31;
+    double np = (rrp3 * rr41) / (rrp4 * rr31);
+    double nm = (rrm3 * rr41) / (rrm4 * rr31);
+    double Rpot_o = (r_o - rr1) * (r_o - rr2) * (r_o - rr3) * (r_o - rr4);
+    double drs_o = sqrt(Rpot_o);
+    double c2c = 2. / sqrt(rr31 * rr42);
+    f[R_XS] = 0.5 * sqrt(rr31 * rr42);
+    f[R_IRO] = Ir_o;
+    f[R_M] = k2;
+    f[R_KC] = ellip_k(k2);
+    f[R_K2] = 2.0 * f[R_KC];
+    f[R_EC] = ellip_e(k2);
+    f[R_N0] = n1;
+    f[R_N1] = np;
+    f[R_N2] = nm;
+    f[R_PIC0] = ellip_pi_ref(n1, HALFPI, k2);
+    f[R_PIC1] = ellip_pi_ref(np, HALFPI, k2);
+    f[R_PIC2] = ellip_pi_ref(nm, HALFPI, k2);
+    f[R_C0] = rr1;
+    f[R_C1] = rr2;
+    f[R_C2] = rr3;
+    f[R_C3] = rr4;
+    f[R_C4] = ellip_e_inc(aux, k2);          // E(aux)
+    f[R_C5] = ellip_pi_ref(n1, aux, k2);     // Pi(n1; aux)
+    f[R_C6] = ellip_pi_ref(np, aux, k2);
+    f[R_C7] = ellip_pi_ref(nm, aux, k2);
+    f[R_C8] = drs_o / (r_o - rr3);           // second term of H
+    f[R_C9] = c2c;
+    f[R_C10] = c2c * (rr43 / (rrp3 * rrp4));
+    f[R_C11] = c2c * (rr43 / (rrm3 * rrm4));
+    f[R_C12] = sqrt(rr31 * rr42);
+    f[R_C13] = rrp3;
+    f[R_C14] = rrm3;
+    f[R_C15] = 0.5 * (rr1 * rr4 + rr2 * rr3);
+    f[R_C16] = rr31;
+    f[R_C17] = rr41;
+    f[R_C18] = rr43;
+  }
+  rec->code = rcase | (th << 4) | ((kk0 ? 1 : 0) << 8) | ((o.minspin ? 1 : 0) << 9);
+  return flags;
+}
+
+// ---------------------------------------------------------------------------
+// per-sample evaluation
+// ---------------------------------------------------------------------------
+
+struct Sample {
+  double t, r, th, ph, sig;
+};
+
+// Pi(n; Phi | m) for the amplitude Phi = nr*pi + phi0, |phi0| <= pi/2, from the
+// shared Carlson values; mirrors the special cases of kgeo/scipy_ellip_binding.py:125-162.
+// inc = Pi(n; phi0 | m) already evaluated (finite path), pic = Pi(n | m).
+KG_HD double pi_assemble(double n, double Phi, double nr, double inc, double pic, double m) {
+  double aphi = fabs(Phi);
+  if (aphi <= PHI_ZERO) return Phi;
+  if (m < M_NEG_INF) return 0.0;
+  if (aphi > HALFPI && n == 1.0) return kg_inf();
+  if (std::isinf(n)) return 0.0;
+  return nr == 0.0 ? inc : 2.0 * nr * pic + inc;
+}
+
+// One Carlson evaluation at (x, y, z) = (cn^2, dn^2-ish ...) for up to three Pi's plus
+// R_D; p[i] = the (scaled) rho_i. For rho_i <= 0 the DLMF 19.20.14 transform is used,
+// rho == 0 gives +inf like the reference.
+template <int NP>
+KG_HD void carlson_set(double x, double y, double z, const double* rho, double* rj, double* rd, double* rf) {
+  double p[NP + 1];
+  double q[NP];
+  bool neg[NP];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    neg[i] = !(rho[i] > 0.0);
+    q[i] = -rho[i];
+    p[i] = neg[i] ? (z * (x + y + q[i]) - x * y) / (z + q[i]) : rho[i];
+    if (rho[i] == 0.0) p[i] = z;  // placeholder, result replaced below
+  }
+  p[NP] = z;  // R_D(x,y,z) = R_J(x,y,z,z)
+  double out[NP + 1];
+  rj_multi<NP + 1>(x, y, z, p, out, rf);
+  *rd = out[NP];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    if (rho[i] == 0.0) {
+      rj[i] = kg_inf();
+    } else if (neg[i]) {
+      double pq = p[i] * q[i];
+      double xy = x * y;
+      double rc = carlson_rc(xy + pq, pq);
+      rj[i] = ((p[i] - z) * out[i] - 3.0 * (*rf) + 3.0 * sqrt((xy * z) / (xy + pq)) * rc) / (q[i] + z);
+    } else {
+      rj[i] = out[i];
+    }
+  }
+}
+
+struct ThetaOut {
+  double th, Gph, Gt;
+};
+
+template <class FV>
+KG_HD ThetaOut sample_theta(const FV& f, int code, double tau, bool ordinary_active) {
+  ThetaOut out{0.0, 0.0, 0.0};
+  int th = code_th(code);
+  if (th == TH_ZERO) return out;
+  if (th == TH_ORD && !ordinary_active) return out;
+  const double s = f[F_S];
+  double snarg = f[T_SCALE] * (-tau + s * f[T_GTH]);
+  const double m = f[T_M], s1m = f[T_S1M];
+  double x = snarg / s1m;
+  double v;
+  double nr = reduce_half_period(x, f[T_K2], &v);
+  Jacobi J = jacobi_landen(v, m);
+  double odd = fmod(fabs(nr), 2.0) == 1.0 ? -1.0 : 1.0;
+  double ys = s1m * J.sn;               // sin(phi0) * dn
+  double phi0 = atan2(ys, J.cn);
+  double Phi = nr * PI + phi0;
+  double sinphi0 = ys / J.dn;
+  double sinPhi = odd * sinphi0;
+  // Carlson at (cn^2, 1, dn^2) scaled by dn^2, see header comment
+  const double n = f[T_N], kk = f[T_KK];
+  double xc = J.cn * J.cn, zc = J.dn * J.dn;
+  double rho = zc - n * (ys * ys);
+  double rj, rd, rf;
+  carlson_set<1>(xc, 1.0, zc, &rho, &rj, &rd, &rf);
+  double ys3 = ys * ys * ys;
+  double pi0 = ys * rf + (n / 3.0) * ys3 * rj;
+  double Pi = pi_assemble(n, Phi, nr, pi0, f[T_PIC], kk);
+  out.Gph = f[T_PREF] * Pi - s * f[T_GPH];
+  if (th == TH_ORD) {
+    const double up = f[T_UP];
+    out.th = acos(-s * sqrt(up) * sinPhi);
+    double gt;
+    if (code_kk0(code)) {
+      gt = -2 * up * f[T_PREF] * 0.125 * (-2 * Phi + sin(2 * Phi));
+    } else {
+      // (E - F)(Phi | kk) = 2 nr (E(kk) - K(kk)) - (kk/3) sin^3(phi0) R_D
+      double emf = -(kk / 3.0) * ys3 * rd;
+      if (nr != 0.0) emf += 2.0 * nr * (f[T_EC] - f[T_KC]);
+      gt = -(2 * up * f[T_PREF] * emf) / (2 * kk);
+    }
+    out.Gt = gt - s * f[T_GT];
+  } else {
+    const double up = f[T_UP], um = f[T_UM];
+    out.th = acos(f[T_H] * sqrt(um + (up - um) * (sinPhi * sinPhi)));
+    double E = ys * rf - (kk / 3.0) * ys3 * rd;
+    if (nr != 0.0) E += 2.0 * nr * f[T_EC];
+    out.Gt = f[T_PREFC] * E - s * f[T_GT];
+  }
+  return out;
+}
+
+struct RadialOut {
+  double r, Ip, Im, I1, I2;
+};
+
+template <class FV>
+KG_HD RadialOut sample_radial(const FV& f, int code, double tau, bool want_phi_t) {
+  RadialOut o{0.0, 0.0, 0.0, 0.0, 0.0};
+  int rc = code_rcase(code);
+  if (rc == RCASE_NONE) return o;
+  double X = f[R_XS] * (-tau + f[R_IRO]);
+  double v;
+  double nr = reduce_half_period(X, f[R_K2], &v);
+  const double k = f[R_M];
+  Jacobi J = jacobi_landen(v, k);
+  double odd = fmod(fabs(nr), 2.0) == 1.0 ? -1.0 : 1.0;
+  double snX = odd * J.sn, cnX = odd * J.cn, dnX = J.dn;
+  double amX = nr * PI + atan2(J.sn, J.cn);
+  double sn3 = J.sn * J.sn * J.sn;
+  if (rc == RCASE_2) {
+    const double rr1 = f[R_C0], rr2 = f[R_C1], rr3 = f[R_C2], rr4 = f[R_C3];
+    const double rr31 = f[R_C16], rr41 = f[R_C17], rr43 = f[R_C18];
+    double sn2 = snX * snX;
+    double rs = (rr4 * rr31 - rr3 * rr41 * sn2) / (rr31 - rr41 * sn2);
+    o.r = rs;
+    if (!want_phi_t) return o;
+    double dX = -f[R_XS];
+    double dsn2 = 2 * snX * cnX * dnX * dX;
+    double den = rr31 - rr41 * sn2;
+    double drs = -(rr31 * rr43 * rr41 * dsn2 / (den * den));
+    double H = drs / (rs - rr3) - f[R_C8];
+    double rho[3];
+    double s2r = J.sn * J.sn;
+    rho[0] = 1.0 - f[R_N0] * s2r;
+    rho[1] = 1.0 - f[R_N1] * s2r;
+    rho[2] = 1.0 - f[R_N2] * s2r;
+    double rj[3], rd, rf;
+    carlson_set<3>(J.cn * J.cn, J.dn * J.dn, 1.0, rho, rj, &rd, &rf);
+    double Finc = J.sn * rf;
+    double Einc = Finc - (k / 3.0) * sn3 * rd;
+    double E = nr == 0.0 ? Einc : Einc + 2.0 * nr * f[R_EC];
+    double Eterm = f[R_C12] * (E - f[R_C4]);
+    double P1 = pi_assemble(f[R_N0], amX, nr, Finc + (f[R_N0] / 3.0) * sn3 * rj[0], f[R_PIC0], k);
+    double Pp = pi_assemble(f[R_N1], amX, nr, Finc + (f[R_N1] / 3.0) * sn3 * rj[1], f[R_PIC1], k);
+    double Pm = pi_assemble(f[R_N2], amX, nr, Finc + (f[R_N2] / 3.0) * sn3 * rj[2], f[R_PIC2], k);
+    double Pi_1 = f[R_C9] * (P1 - f[R_C5]);
+    double Pi_p = f[R_C10] * (Pp - f[R_C6]);
+    double Pi_m = f[R_C11] * (Pm - f[R_C7]);
+    o.I1 = rr3 * (-tau) + rr43 * Pi_1;
+    o.I2 = H - f[R_C15] * (-tau) - Eterm;
+    o.Ip = tau / f[R_C13] - Pi_p;
+    o.Im = tau / f[R_C14] - Pi_m;
+    return o;
+  }
+  if (rc == RCASE_3) {
+    const double AA = f[R_C0], BB = f[R_C1], rr1 = f[R_C2], rr2 = f[R_C3];
+    o.r = ((BB * rr2 - AA * rr1) + (BB * rr2 + AA * rr1) * cnX) / ((BB - AA) + (BB + AA) * cnX);
+    if (!want_phi_t) return o;
+    const double al[3] = {f[R_C4], f[R_C5], f[R_C6]};
+    double s2r = J.sn * J.sn;
+    double rho[3];
+    rho[0] = 1.0 - f[R_N0] * s2r;
+    rho[1] = 1.0 - f[R_N1] * s2r;
+    rho[2] = 1.0 - f[R_N2] * s2r;
+    double rj[3], rd, rf;
+    carlson_set<3>(J.cn * J.cn, J.dn * J.dn, 1.0, rho, rj, &rd, &rf);
+    double Finc = J.sn * rf;
+    double F = nr == 0.0 ? Finc : Finc + 2.0 * nr * f[R_KC];
+    double Einc = Finc - (k / 3.0) * sn3 * rd;
+    double E = nr == 0.0 ? Einc : Einc + 2.0 * nr * f[R_EC];
+    const double nn[3] = {f[R_N0], f[R_N1], f[R_N2]};
+    const double pic[3] = {f[R_PIC0], f[R_PIC1], f[R_PIC2]};
+    double R1[3];
+    const bool use_m = !code_minspin(code);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      double a_ = al[i];
+      double al2 = a_ * a_;
+      double p1 = (i == 0) ? f[R_C18] : (i == 1 ? f[R_C19] : sqrt((al2 - 1) / (k + (1 - k) * al2)));
+      double f1 = 0.5 * p1 * log(fabs((p1 * dnX + snX) / (p1 * dnX - snX)));
+      double P = pi_assemble(nn[i], amX, nr, Finc + (nn[i] / 3.0) * sn3 * rj[i], pic[i], k);
+      R1[i] = (P - a_ * f1) / (1 - al2);
+    }
+    double al2 = al[0] * al[0];
+    double jd = k + (1 - k) * al2;
+    double R2 = (F - (al2 / jd) * (E - al[0] * snX * dnX / (1 + al[0] * cnX))) / (al2 - 1);
+    R2 = R2 + (2 * k - nn[0]) * R1[0] / jd;
+    double R1m = use_m ? R1[2] : 0.0;
+    double R1bm = use_m ? f[R_C10] : 0.0;
+    double c0 = f[R_C11];
+    double Pi_1 = c0 * (R1[0] - f[R_C7]);
+    double Pi_2 = (c0 * c0) * (R2 - f[R_C8]);
+    double Pi_p = f[R_C12] * (R1[1] - f[R_C9]);
+    double Pi_m = f[R_C13] * (R1m - R1bm);
+    double pr = f[R_C14];
+    o.I1 = pr * (-tau) + Pi_1;
+    o.I2 = (pr * pr) * (-tau) + 2 * pr * Pi_1 + f[R_C15] * Pi_2;
+    o.Ip = -((BB + AA) * (-tau) + Pi_p) / f[R_C16];
+    o.Im = -((BB + AA) * (-tau) + Pi_m) / f[R_C17];
+    return o;
+  }
+  // RCASE_4
+  {
+    const double a2i = f[R_C0], b1 = f[R_C1], g0 = f[R_C2];
+    double sc = snX / cnX;
+    o.r = -a2i * (g0 - sc) / (1 + g0 * sc) - b1;
+    if (!want_phi_t) return o;
+    double s2r = J.sn * J.sn;
+    double rho[3];
+    rho[0] = 1.0 - f[R_N0] * s2r;
+    rho[1] = 1.0 - f[R_N1] * s2r;
+    rho[2] = 1.0 - f[R_N2] * s2r;
+    double rj[3], rd, rf;
+    carlson_set<3>(J.cn * J.cn, J.dn * J.dn, 1.0, rho, rj, &rd, &rf);
+    double Finc = J.sn * rf;
+    double F = nr == 0.0 ? Finc : Finc + 2.0 * nr * f[R_KC];
+    double Einc = Finc - (k / 3.0) * sn3 * rd;
+    double E = nr == 0.0 ? Einc : Einc + 2.0 * nr * f[R_EC];
+    const double gs[3] = {g0, f[R_C3], f[R_C4]};
+    const double nn[3] = {f[R_N0], f[R_N1], f[R_N2]};
+    const double pic[3] = {f[R_PIC0], f[R_PIC1], f[R_PIC2]};
+    double S1[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      double al = gs[i];
+      double al2 = al * al;
+      double al2p1 = 1 + al2;
+      double al2j = 1 - k + al2;
+      double p2 = sqrt(al2p1 / al2j);
+      double f2 = 0.5 * p2 * log(fabs(((1 - p2) * (1 + p2 * dnX)) / ((1 + p2) * (1 - p2 * dnX))));
+      double P = pi_assemble(nn[i], amX, nr, Finc + (nn[i] / 3.0) * sn3 * rj[i], pic[i], k);
+      S1[i] = (F + al2 * P - al * f2) / al2p1;
+    }
+    double al2 = g0 * g0, al2p1 = 1 + al2, al2j = 1 - k + al2;
+    double S2a = (1 - k) * F + al2 * E + al2 * dnX * (g0 - sc) / (1 + g0 * sc) - al2 * g0;
+    S2a = -S2a / (al2p1 * al2j);
+    double S2b = S1[0] * (1. / al2p1 + (1 - k) / al2j);
+    double S2 = S2a + S2b;
+    double Pi_1 = f[R_C9] * (S1[0] - f[R_C5]);
+    double Pi_2 = f[R_C10] * (S2 - f[R_C6]);
+    double Pi_p = f[R_C11] * (S1[1] - f[R_C7]);
+    double Pi_m = f[R_C12] * (S1[2] - f[R_C8]);
+    double aa1 = f[R_C13];
+    o.I1 = aa1 * (-tau) - Pi_1;
+    o.I2 = (aa1 * aa1) * (-tau) - 2 * aa1 * Pi_1 + Pi_2;
+    o.Ip = f[R_C14] * (-tau - Pi_p);
+    o.Im = f[R_C15] * (-tau - Pi_m);
+    return o;
+  }
+}
+
+// Element g of numpy.linspace(0, stop, G) for an array stop (numpy's arithmetic:
+// g * (stop / (G - 1)), or (g / (G - 1)) * stop when any step of the array is zero,
+// then + start, and the last element set to stop exactly).
+KG_HD double linspace_at(int64_t g, int64_t G, double stop, bool any_step_zero) {
+  if (G == 1) return 0.0 * stop + 0.0;
+  if (g == G - 1) return stop;
+  double div = (double)(G - 1);
+  if (any_step_zero) return ((double)g / div) * stop + 0.0;
+  return (double)g * (stop / div) + 0.0;
+}
+
+// All five coordinates at Mino time tau (kgeo/kerr_raytracing_ana.py:186-188, 626-633).
+template <class FV>
+KG_HD Sample sample_all(const Observer& ob, const FV& f, int code, double tau, bool ordinary_active) {
+  ThetaOut T = sample_theta(f, code, tau, ordinary_active);
+  RadialOut R = sample_radial(f, code, tau, true);
+  const double a = ob.a, rp = ob.rplus, rm = ob.rminus, lam = f[F_LAM];
+  double I_0 = -tau;
+  double I_phi = (2 * a / (rp - rm)) * ((rp - 0.5 * a * lam) * R.Ip - (rm - 0.5 * a * lam) * R.Im);
+  double I_tA = (4 / (rp - rm)) * ((rp * rp - 0.5 * a * lam * rp) * R.Ip - (rm * rm - 0.5 * a * lam * rm) * R.Im);
+  double I_t = I_tA + 4 * I_0 + 2 * R.I1 + R.I2;
+  Sample S;
+  S.sig = 0 + R.I2 + ob.a2 * T.Gt;
+  S.t = 0 + I_t + ob.a2 * T.Gt;
+  S.ph = 0 + I_phi + lam * T.Gph;
+  S.r = R.r;
+  S.th = T.th;
+  return S;
+}
+
+}  // namespace kg

@@ -1,0 +1,56 @@
+// Per-sample kernel: one thread per (pixel, Mino sample) item, items ordered pixel-major so
+// that the lanes of a warp walk consecutive samples of the same ray and take the same
+// branches; stores go to the (nsamp, npix) row-major outputs.
+#include "kg_launch.h"
+
+namespace kg {
+
+__global__ void __launch_bounds__(256) samples_kernel(SampleArgs a) {
+  const uint32_t fl = *a.flags;
+  const bool ordinary_active = (fl & FLAG_ANY_ETA_POS) != 0;
+  const bool step_zero = (fl & FLAG_ANY_STEP_ZERO) != 0;
+  const int64_t total = a.npix * a.nsamp;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+    const int64_t p = i / a.nsamp;
+    const int64_t g = i - p * a.nsamp;
+    RecView f{a.rec + p, a.npix};
+    double tau = a.tau ? a.tau[g * a.npix + p] : linspace_at(g, a.nsamp, f[F_TAUMAX], step_zero);
+    const int code = __ldg(a.code + p);
+    const int64_t o = g * a.npix + p;
+    if (a.do_phi_t) {
+      Sample S = sample_all(a.obs, f, code, tau, ordinary_active);
+      if (a.t) a.t[o] = S.t;
+      if (a.r) a.r[o] = S.r;
+      if (a.th) a.th[o] = S.th;
+      if (a.ph) a.ph[o] = S.ph;
+      if (a.sig) a.sig[o] = S.sig;
+    } else {
+      ThetaOut T = sample_theta(f, code, tau, ordinary_active);
+      RadialOut R = sample_radial(f, code, tau, false);
+      if (a.r) a.r[o] = R.r;
+      if (a.th) a.th[o] = T.th;
+      // without phi and t the reference's sums reduce to I_t = 4 I_0 = -4 tau, I_phi = I_sig = 0
+      if (a.t) a.t[o] = 0 + 4 * (-tau);
+      if (a.ph) a.ph[o] = 0.0;
+      if (a.sig) a.sig[o] = 0.0;
+    }
+    if (a.mino) a.mino[o] = tau;
+  }
+}
+
+cudaError_t launch_samples(const SampleArgs& a, cudaStream_t s) {
+  const int64_t total = a.npix * a.nsamp;
+  if (total <= 0) return cudaSuccess;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int block = 256;
+  int64_t grid = (total + block - 1) / block;
+  const int64_t cap = (int64_t)sms * 16;  // grid-stride beyond 16 resident-ish blocks per SM
+  if (grid > cap) grid = cap;
+  samples_kernel<<<(unsigned)grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace kg

@@ -1,0 +1,936 @@
+"""CPU oracle for the analytic Kerr null-geodesic tracer (FP64, numpy + scipy.special).
+
+TEST INFRASTRUCTURE ONLY. The oracle is the checker: only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline / reference legs of ``bench.py``
+import it. The product package ``kgeo_gb300`` never imports, calls or links it.
+
+It restates, operation for operation, the FP64 algorithm of kgeo (achael/kgeo)
+for the hot path: conserved quantities, angular turning points, the radial
+quartic, the Mino-time totals, the theta and r antiderivatives, the elliptic-Pi
+adapter, the equatorial source radius and the unpolarised equatorial image.
+Each function cites the reference file:line it follows. The elementary special
+functions are scipy.special's (``ellipkinc``, ``ellipeinc``, ``ellipj``,
+``ellipk``, ``elliprf``, ``elliprj``, ``elliprc``), called exactly where the
+reference calls them, so on the same platform the oracle reproduces the
+reference's output bit for bit. ``tests/golden/`` holds fixtures produced by
+running the reference itself (``tests/golden/make_golden.py``); the CPU test
+``tests/test_oracle_golden.py`` pins the oracle to them.
+
+scipy.special (third-party, compiled) is the arithmetic the reference relies
+on; it is called, never restated here.
+"""
+import numpy as np
+import scipy.special as sp
+
+MINSPIN = 1.0e-4          # kgeo/kerr_raytracing_utils.py:9
+EP = 1.0e-12              # kgeo/kerr_raytracing_utils.py:12
+MAXTAUFRAC = 1.0 - 1.0e-10  # kgeo/kerr_raytracing_ana.py:26
+HALFPI = 0.5 * np.pi
+
+# ----------------------------------------------------------------------------
+# argument checks (same messages as the reference)
+# ----------------------------------------------------------------------------
+
+
+def check_spin(a):
+    """kgeo/kerr_raytracing_ana.py:59-60"""
+    if not (isinstance(a, float) and (0 <= np.abs(a) < 1)):
+        raise Exception("|a| should be a float in range [0,1)")
+
+
+def check_observer(r_o, th_o):
+    """kgeo/kerr_raytracing_ana.py:62-65"""
+    if not (isinstance(r_o, float) and (r_o >= 100)):
+        raise Exception("r_o should be a float > 100")
+    if not (isinstance(th_o, float) and (0 < th_o < np.pi) and th_o != 0.5 * np.pi):
+        raise Exception("th_o should be a float in range (0,pi/2) or (pi/2,pi)")
+
+
+def as_pixels(alpha, beta):
+    """kgeo/kerr_raytracing_ana.py:68-71"""
+    if not isinstance(alpha, np.ndarray):
+        alpha = np.array([alpha]).flatten()
+    if not isinstance(beta, np.ndarray):
+        beta = np.array([beta]).flatten()
+    if len(alpha) != len(beta):
+        raise Exception("alpha, beta are different lengths!")
+    return alpha, beta
+
+
+# ----------------------------------------------------------------------------
+# per-pixel kinematics
+# ----------------------------------------------------------------------------
+
+
+def conserved(a, th_o, alpha, beta, clamp=True):
+    """(lambda, eta) of each pixel; kgeo/kerr_raytracing_ana.py:76-82 (151-158).
+
+    With ``clamp`` the a < MINSPIN rule that lifts eta < 0 to EP is applied.
+    """
+    lam = -alpha * np.sin(th_o)
+    eta = (alpha ** 2 - a ** 2) * np.cos(th_o) ** 2 + beta ** 2
+    if clamp and np.abs(a) < MINSPIN and np.any(eta < 0):
+        eta = eta.copy()
+        eta[eta < 0] = EP
+    return lam, eta
+
+
+def beta_sign(beta):
+    """+1 for beta >= 0, -1 otherwise; kgeo/kerr_raytracing_utils.py:857-864."""
+    out = np.zeros(beta.shape)
+    out[beta >= 0] = 1
+    out[beta < 0] = -1
+    return out
+
+
+def u_roots(a, th_o, lam, eta):
+    """u_+, u_-, u_+/u_-, a^2 u_- with the reference's clamps.
+
+    kgeo/kerr_raytracing_utils.py:276-328. Below MINSPIN the reference binds
+    u_- and u_+ to the same array, so every clamp applied to one applies to
+    both; that aliasing is kept here on purpose.
+    """
+    c2 = np.cos(th_o) ** 2
+    if np.abs(a) < MINSPIN:
+        up = eta / (eta + lam * lam)
+        um = up
+    else:
+        half = 0.5 * (1 - (eta + lam * lam) / (a * a))
+        up = half + np.sqrt(half ** 2 + eta / (a * a))
+        um = half - np.sqrt(half ** 2 + eta / (a * a))
+    up[(c2 - up) > 0] = c2
+    up[up ** 2 > 1] = 1
+    um[(um == 0) * (eta < 0)] = EP
+    um[(um == 0) * (eta >= 0)] = -EP
+    vort = eta < 0
+    lift = np.zeros(eta.shape, dtype=bool)
+    lift[vort] = (c2 - um[vort]) < 0
+    um[lift] = c2
+    if np.abs(a) < MINSPIN:
+        ratio = 0.0 * um
+        a2um = -(eta + lam ** 2)
+    else:
+        ratio = up / um
+        a2um = a ** 2 * um
+    return up, um, ratio, a2um
+
+
+def theta_turning(a, th_o, lam, eta):
+    """(u_+, u_-, th_+, th_-, thclass); kgeo/kerr_raytracing_utils.py:242-274."""
+    up, um, _, _ = u_roots(a, th_o, lam, eta)
+    th_plus = np.arccos(-np.sqrt(up))
+    th_minus = np.arccos(np.sqrt(up))
+    th_plus[eta < 0] = np.arccos(np.sqrt(um[eta < 0]))
+    thclass = np.zeros(lam.shape).astype(int)
+    thclass[eta > 0] = 1
+    thclass[eta < 0] = 2
+    thclass[eta == 0] = 3
+    return up, um, th_plus, th_minus, thclass
+
+
+def cbrt_max_real(x):
+    """Complex cube root with the largest real part; real inputs keep their sign.
+
+    kgeo/kerr_raytracing_utils.py:828-855.
+    """
+    s = np.sign(x)
+    r = np.abs(x)
+    th = np.angle(x)
+    out = np.empty(x.shape).astype(complex)
+    real = np.imag(x) == 0
+    out[real] = (s * np.cbrt(r))[real]
+    if np.any(~real):
+        c0 = np.cbrt(r) * np.exp(1j * th / 3.)
+        c1 = np.cbrt(r) * np.exp(1j * th / 3. + 2j * np.pi / 3.)
+        c2 = np.cbrt(r) * np.exp(1j * th / 3. - 2j * np.pi / 3.)
+        x0, x1, x2 = np.real(c0), np.real(c1), np.real(c2)
+        pick0 = ~real * (x0 > x1) * (x0 > x2)
+        pick1 = ~real * (x1 > x0) * (x1 > x2)
+        pick2 = ~real * (x2 > x0) * (x2 > x1)
+        out[pick0] = c0[pick0]
+        out[pick1] = c1[pick1]
+        out[pick2] = c2[pick2]
+    return out
+
+
+def quartic_roots(a, lam, eta):
+    """Radial roots r1..r4 (complex) and rclass; kgeo/kerr_raytracing_utils.py:330-380."""
+    rplus = 1 + np.sqrt(1 - a ** 2)
+    A = a ** 2 - eta - lam ** 2
+    B = 2 * (eta + (lam - a) ** 2)
+    C = -(a ** 2) * eta
+    P = -(A ** 2) / 12. - C
+    Q = (-A / 3.) * ((A ** 2) / 36. - C) - (B ** 2) / 8.
+    disc = (4 * (P ** 3) + 27 * (Q ** 2)).astype(complex)
+    wp3 = -0.5 * Q + np.sqrt(disc / 108.)
+    wm3 = -0.5 * Q - np.sqrt(disc / 108.)
+    xi0 = cbrt_max_real(wp3) + cbrt_max_real(wm3) - A / 3.
+    z = np.sqrt(0.5 * xi0)
+    w_lo = (-0.5 * A - z ** 2 + 0.25 * B / z).astype(complex)
+    w_hi = (-0.5 * A - z ** 2 - 0.25 * B / z).astype(complex)
+    r1 = -z - np.sqrt(w_lo)
+    r2 = -z + np.sqrt(w_lo)
+    r3 = z - np.sqrt(w_hi)
+    r4 = z + np.sqrt(w_hi)
+    rclass = np.zeros(r1.shape).astype(int)
+    rclass[np.imag(r2) != 0] = 4
+    rclass[(np.imag(r2) == 0) * (np.imag(r4) != 0)] = 3
+    rclass[(np.imag(r2) == 0) * (np.imag(r4) == 0) * (np.real(r4) < rplus)] = 2
+    rclass[(np.imag(r2) == 0) * (np.imag(r4) == 0) * (np.real(r4) > rplus)] = 1
+    return r1, r2, r3, r4, rclass
+
+
+def _case4_params(a, r_o, r2, r4):
+    """Region-IV constants (GL19a B83-B88); kgeo/kerr_raytracing_utils.py:418-433."""
+    a1 = np.imag(r4)
+    b1 = np.real(r4)
+    a2 = np.imag(r2)
+    b2 = np.real(r2)
+    CC = np.sqrt((a1 - a2) ** 2 + (b1 - b2) ** 2)
+    DD = np.sqrt((a1 + a2) ** 2 + (b1 - b2) ** 2)
+    k4 = (4 * CC * DD) / ((CC + DD) ** 2)
+    g0 = np.sqrt((4 * a2 ** 2 - (CC - DD) ** 2) / ((CC + DD) ** 2 - 4 * a2 ** 2))
+    return a1, b1, a2, b2, CC, DD, k4, g0
+
+
+def _case3_params(r1, r2, r4):
+    """Region-III constants (GL19a B55-B59); kgeo/kerr_raytracing_utils.py:451-466."""
+    a1 = np.imag(r4)
+    b1 = np.real(r4)
+    rr1 = np.real(r1)
+    rr2 = np.real(r2)
+    rr21 = rr2 - rr1
+    AA = np.sqrt(a1 ** 2 + (b1 - rr2) ** 2)
+    BB = np.sqrt(a1 ** 2 + (b1 - rr1) ** 2)
+    k3 = ((AA + BB) ** 2 - rr21 ** 2) / (4 * AA * BB)
+    return a1, b1, rr1, rr2, rr21, AA, BB, k3
+
+
+def mino_total(a, r_o, eta, r1, r2, r3, r4):
+    """Total Mino time from the observer to the horizon or back out to infinity.
+
+    kgeo/kerr_raytracing_utils.py:382-548 (regions IV, III, II, I).
+    """
+    rplus = 1 + np.sqrt(1 - a ** 2)
+    rminus = 1 - np.sqrt(1 - a ** 2)
+    out = np.zeros(r1.shape)
+
+    m4 = np.imag(r1) != 0
+    if np.any(m4):
+        a1, b1, a2, b2, CC, DD, k4, g0 = _case4_params(a, r_o, r2[m4], r4[m4])
+        x_hor = (rplus + b1) / a2
+        x_obs = np.inf if r_o == np.inf else (r_o + b1) / a2
+        pref = 2. / (CC + DD)
+        i_hor = pref * sp.ellipkinc(np.arctan(x_hor) + np.arctan(g0), k4)
+        i_obs = pref * sp.ellipkinc(np.arctan(x_obs) + np.arctan(g0), k4)
+        out[m4] = i_obs - i_hor
+
+    m3 = (np.imag(r3) != 0) * (~m4)
+    if np.any(m3):
+        a1, b1, rr1, rr2, rr21, AA, BB, k3 = _case3_params(r1[m3], r2[m3], r4[m3])
+        rrp1 = rplus - rr1
+        rrp2 = rplus - rr2
+        x_hor = (AA * rrp1 - BB * rrp2) / (AA * rrp1 + BB * rrp2)
+        if r_o == np.inf:
+            x_obs = (AA - BB) / (AA + BB)
+        else:
+            x_obs = (AA * (r_o - rr1) - BB * (r_o - rr2)) / (AA * (r_o - rr1) + BB * (r_o - rr2))
+        pref = 1. / np.sqrt(AA * BB)
+        out[m3] = pref * sp.ellipkinc(np.arccos(x_obs), k3) - pref * sp.ellipkinc(np.arccos(x_hor), k3)
+
+    m2 = (np.imag(r3) == 0.) * (r3 < rplus) * (~m3)
+    if np.any(m2):
+        rr1, rr2, rr3, rr4 = (np.real(r)[m2] for r in (r1, r2, r3, r4))
+        rr31, rr32, rr41, rr42 = rr3 - rr1, rr3 - rr2, rr4 - rr1, rr4 - rr2
+        k2 = (rr32 * rr41) / (rr31 * rr42)
+        x_hor = np.sqrt((rr31 * (rplus - rr4)) / (rr41 * (rplus - rr3)))
+        if r_o == np.inf:
+            x_obs = np.sqrt(rr31 / rr41)
+        else:
+            x_obs = np.sqrt((rr31 * (r_o - rr4)) / (rr41 * (r_o - rr3)))
+        pref = 2. / np.sqrt(rr31 * rr42)
+        out[m2] = pref * sp.ellipkinc(np.arcsin(x_obs), k2) - pref * sp.ellipkinc(np.arcsin(x_hor), k2)
+
+    m1 = (np.imag(r3) == 0.) * (r3 > rplus) * (~m2)
+    if np.any(m1):
+        rr1, rr2, rr3, rr4 = (np.real(r)[m1] for r in (r1, r2, r3, r4))
+        rr31, rr32, rr41, rr42 = rr3 - rr1, rr3 - rr2, rr4 - rr1, rr4 - rr2
+        k2 = (rr32 * rr41) / (rr31 * rr42)
+        if r_o == np.inf:
+            x_obs = np.sqrt(rr31 / rr41)
+        else:
+            x_obs = np.sqrt((rr31 * (r_o - rr4)) / (rr41 * (r_o - rr3)))
+        pref = 2. / np.sqrt(rr31 * rr42)
+        out[m1] = 2 * (pref * sp.ellipkinc(np.arcsin(x_obs), k2))
+    return out
+
+
+# ----------------------------------------------------------------------------
+# elliptic Pi adapter
+# ----------------------------------------------------------------------------
+
+
+def ellip_pi(n, phi, m):
+    """Pi(n; phi | m), Abramowitz & Stegun convention, any real phi.
+
+    kgeo/scipy_ellip_binding.py:87-237: the special-case masks in their order
+    (phi ~ 0, m -> -inf, y < 0, |phi| > pi/2 with m >= 1 or n == 1, rho == 0,
+    n == inf), the periodic reductions for |phi| > pi and pi/2 < |phi| <= pi,
+    then sin(phi) R_F + (n/3) sin^3(phi) R_J with the DLMF 19.20.14 transform
+    for rho < 0.
+    """
+    n = np.atleast_1d(np.asarray(n, dtype=float))
+    phi = np.atleast_1d(np.asarray(phi, dtype=float))
+    m = np.atleast_1d(np.asarray(m, dtype=float))
+    if n.ndim != phi.ndim:
+        n = np.outer(np.ones(phi.shape[0]), n)
+    if m.ndim != phi.ndim:
+        m = np.outer(np.ones(phi.shape[0]), m)
+
+    cphi = np.cos(phi)
+    sphi = np.sin(phi)
+    x = cphi ** 2
+    y = 1. - m * sphi ** 2
+    z = np.ones(x.shape)
+    rho = 1. - n * sphi ** 2
+
+    out = np.zeros(phi.shape)
+    done = np.zeros(phi.shape).astype(bool)
+
+    sel = np.abs(phi) <= 1.e-10
+    out[sel] = phi[sel]
+    done += sel
+    sel = (m < -1.e14) * ~done
+    out[sel] = 0.
+    done += sel
+    sel = (y < 0) * ~done
+    out[sel] = np.nan
+    done += sel
+    sel = (np.abs(phi) > HALFPI) * (m >= 1) * ~done
+    out[sel] = np.nan
+    done += sel
+    sel = (np.abs(phi) > HALFPI) * (n == 1) * ~done
+    out[sel] = np.inf
+    done += sel
+    sel = (rho == 0) * ~done
+    out[sel] = np.inf
+    done += sel
+    sel = np.isinf(n) * ~done
+    out[sel] = 0
+    done += sel
+
+    sel = (np.abs(phi) > np.pi) * ~done
+    if np.any(sel):
+        s = np.sign(phi[sel])
+        k = s * np.floor(np.abs(phi[sel]) / np.pi)
+        rem = phi[sel] - k * np.pi
+        out[sel] = 2 * k * ellip_pi(n[sel], HALFPI * np.ones(rem.shape), m[sel]) \
+            + ellip_pi(n[sel], rem, m[sel])
+    done += sel
+
+    sel = (np.abs(phi) > HALFPI) * (np.abs(phi) <= np.pi) * ~done
+    if np.any(sel):
+        s = np.sign(phi[sel])
+        rem = -phi[sel] + s * np.pi
+        out[sel] = s * 2 * ellip_pi(n[sel], HALFPI * np.ones(rem.shape), m[sel]) \
+            - ellip_pi(n[sel], rem, m[sel])
+    done += sel
+
+    sel = ~done
+    if np.any(sel):
+        xs, ys, zs, rs, ss, ns = x[sel], y[sel], z[sel], rho[sel], sphi[sel], n[sel]
+        qs = -rs
+        ps = (zs * (xs + ys + qs) - xs * ys) / (zs + qs)
+        rf = sp.elliprf(xs, ys, zs)
+        rj = np.zeros(xs.shape)
+        pos = rs > 0
+        if np.any(pos):
+            rj[pos] = sp.elliprj(xs[pos], ys[pos], zs[pos], rs[pos])
+        neg = ~pos
+        if np.any(neg):
+            rj0 = sp.elliprj(xs[neg], ys[neg], zs[neg], ps[neg])
+            rc = sp.elliprc((xs * ys + ps * qs)[neg], (ps * qs)[neg])
+            w = 3 * np.sqrt((xs * ys * zs)[neg] / (xs * ys + ps * qs)[neg])
+            rj[neg] = ((ps - zs)[neg] * rj0 - 3 * rf[neg] + w * rc)
+            rj[neg] = rj[neg] / (qs + zs)[neg]
+        out[sel] = ss * rf + (ns / 3.) * (ss ** 3) * rj
+    return out
+
+
+# ----------------------------------------------------------------------------
+# theta motion
+# ----------------------------------------------------------------------------
+
+
+def _am_beyond_quarter(snarg, kk):
+    """sin(Phi) and Phi = am(snarg | kk) for kk < 0 via the m = kk/(kk-1) transform.
+
+    kgeo/kerr_raytracing_ana.py:257-277 (and 333-352): sn from ellipj at
+    snarg/sqrt(1-m), the amplitude as pi/2 - am(K(m) - x | m).
+    """
+    sin_amp = np.zeros(snarg.shape)
+    amp = np.zeros(snarg.shape)
+    small = np.abs(snarg) < EP
+    sin_amp[small] = snarg[small]
+    amp[small] = snarg[small]
+    if np.any(~small):
+        m = (kk / (kk - 1))
+        m = np.outer(np.ones(snarg.shape[0]), m)[~small]
+        sn, cn, dn, ph = sp.ellipj(snarg[~small] / np.sqrt(1 - m), m)
+        sin_amp[~small] = np.sqrt(1 - m) * sn / dn
+        amp[~small] = 0.5 * np.pi - sp.ellipj(sp.ellipk(m) - snarg[~small] / np.sqrt(1 - m), m)[3]
+    return sin_amp, amp
+
+
+def theta_solution(a, th_o, s_o, lam, eta, up, um, tau, do_phi_and_t=True):
+    """theta(tau), G_phi(tau), G_t(tau); kgeo/kerr_raytracing_ana.py:195-365."""
+    th_s = np.zeros(tau.shape)
+    G_ph = np.zeros(tau.shape)
+    G_t = np.zeros(tau.shape)
+
+    # ordinary motion (eta >= 0), only when some eta > 0: :216-296
+    if np.any(eta > 0.):
+        sel = eta >= 0.
+        u_p = up[sel]
+        u_m = um[sel]
+        s = s_o[sel]
+        if np.abs(a) < MINSPIN:
+            kk = np.zeros(eta.shape)[sel]
+            a2um = -(eta + lam ** 2)[sel]
+        else:
+            kk = u_p / u_m
+            a2um = a ** 2 * u_m
+        pref = 1 / np.sqrt(-a2um)
+        arg_o = np.arcsin(np.cos(th_o) / np.sqrt(u_p))
+        F_o = sp.ellipkinc(arg_o, kk)
+        Gth_o = -pref * F_o
+        if do_phi_and_t:
+            Gph_o = -pref * ellip_pi(u_p, arg_o, kk)
+            zk = kk == 0
+            Gt_o = np.zeros(kk.shape)
+            if np.any(zk):
+                Gt_o[zk] = 2 * u_p * pref * 0.125 * (-2 * arg_o + np.sin(2 * arg_o))[zk]
+            if np.any(~zk):
+                Gt_o[~zk] = 2 * u_p * pref * (sp.ellipeinc(arg_o, kk) - F_o)[~zk] / (2 * kk[~zk])
+        snarg = (np.sqrt(-a2um) * (-tau[:, sel] + s * Gth_o)).astype(float)
+        sin_amp, amp = _am_beyond_quarter(snarg, kk)
+        th_s[:, sel] = (np.arccos(-s * np.sqrt(u_p) * sin_amp)).astype(float)
+        if do_phi_and_t:
+            G_ph[:, sel] = (pref * ellip_pi(u_p, amp, kk) - s * Gph_o).astype(float)
+            zk = kk == 0
+            gt = np.zeros(amp.shape)
+            if np.any(zk):
+                gt[:, zk] = -2 * u_p * pref * 0.125 * (-2 * amp + np.sin(2 * amp))[:, zk]
+            if np.any(~zk):
+                gt[:, ~zk] = -(2 * u_p * pref * (sp.ellipeinc(amp, kk) - sp.ellipkinc(amp, kk)))[:, ~zk] / (2 * kk[~zk])
+            G_t[:, sel] = gt - s * Gt_o
+
+    # vortical motion (eta < 0), entered whenever some eta <= 0: :298-363
+    if np.any(eta <= 0.):
+        if np.abs(a) < MINSPIN:
+            raise Exception("below MINSPIN but there are eta<0 points in th_integrate!")
+        sel = eta < 0.
+        u_p = up[sel]
+        u_m = um[sel]
+        s = s_o[sel]
+        ratio = u_p / u_m
+        a2um = a ** 2 * u_m
+        h = 1. if th_o <= np.pi / 2 else -1
+        prefA = 1 / np.sqrt(a2um)
+        prefB = prefA / (1. - u_m)
+        prefC = np.sqrt(u_m / a ** 2)
+        nu_o = np.arcsin(np.sqrt((np.cos(th_o) ** 2 - u_m) / (u_p - u_m)))
+        kk = 1 - ratio
+        upm = (u_p - u_m) / (1. - u_m)
+        Gth_o = -h * prefA * sp.ellipkinc(nu_o, kk)
+        if do_phi_and_t:
+            Gph_o = -h * prefB * ellip_pi(upm, nu_o, kk)
+            Gt_o = -h * prefC * sp.ellipeinc(nu_o, kk)
+        snarg = (np.sqrt(a2um) * (-tau[:, sel] + s * Gth_o)).astype(float)
+        sin_nu, nu = _am_beyond_quarter(snarg, kk)
+        th_s[:, sel] = (np.arccos(h * np.sqrt(u_m + (u_p - u_m) * sin_nu ** 2))).astype(float)
+        if do_phi_and_t:
+            G_ph[:, sel] = (prefB * ellip_pi(upm, nu, kk) - s * Gph_o).astype(float)
+            G_t[:, sel] = (prefC * sp.ellipeinc(nu, kk) - s * Gt_o).astype(float)
+    return th_s, G_ph, G_t
+
+
+# ----------------------------------------------------------------------------
+# radial motion
+# ----------------------------------------------------------------------------
+
+
+def S1_S2(al, phi, j, ret_s2=True):
+    """GL19a B92/B93 building blocks; kgeo/kerr_raytracing_ana.py:638-663."""
+    al2 = al * al
+    al2p1 = 1 + al2
+    al2j = 1 - j + al2
+    s2phi = np.sqrt(1. - j * (np.sin(phi)) ** 2)
+    p2 = np.sqrt(al2p1 / al2j)
+    f2 = 0.5 * p2 * np.log(np.abs(((1 - p2) * (1 + p2 * s2phi)) / ((1 + p2) * (1 - p2 * s2phi))))
+    F = sp.ellipkinc(phi, j)
+    S1 = (F + al2 * ellip_pi(al2p1, phi, j) - al * f2) / al2p1
+    S2 = np.nan
+    if ret_s2:
+        E = sp.ellipeinc(phi, j)
+        tanphi = np.tan(phi)
+        S2a = (1 - j) * F + al2 * E + al2 * s2phi * (al - tanphi) / (1 + al * tanphi) - al2 * al
+        S2a = -S2a / (al2p1 * al2j)
+        S2b = S1 * (1. / al2p1 + (1 - j) / al2j)
+        S2 = S2a + S2b
+    return S1, S2
+
+
+def R1_R2(al, phi, j, ret_r2=True):
+    """GL19a B62/B65 building blocks; kgeo/kerr_raytracing_ana.py:666-683."""
+    al2 = al ** 2
+    s2phi = np.sqrt(1 - j * np.sin(phi) ** 2)
+    p1 = np.sqrt((al2 - 1) / (j + (1 - j) * al2))
+    f1 = 0.5 * p1 * np.log(np.abs((p1 * s2phi + np.sin(phi)) / (p1 * s2phi - np.sin(phi))))
+    nn = al2 / (al2 - 1)
+    R1 = (ellip_pi(nn, phi, j) - al * f1) / (1 - al2)
+    R2 = np.nan
+    if ret_r2:
+        F = sp.ellipkinc(phi, j)
+        E = sp.ellipeinc(phi, j)
+        R2 = (F - (al2 / (j + (1 - j) * al2)) * (E - al * np.sin(phi) * s2phi / (1 + al * np.cos(phi)))) / (al2 - 1)
+        R2 = R2 + (2 * j - nn) * R1 / (j + (1 - j) * al2)
+    return R1, R2
+
+
+def radial_solution(a, r_o, lam, eta, r1, r2, r3, r4, tau, do_phi_and_t=True):
+    """r(tau), I_phi, I_t, I_sigma; kgeo/kerr_raytracing_ana.py:368-633."""
+    rplus = 1 + np.sqrt(1 - a ** 2)
+    rminus = 1 - np.sqrt(1 - a ** 2)
+    r_s = np.zeros(tau.shape)
+    I_p = np.zeros(tau.shape)
+    I_m = np.zeros(tau.shape)
+    I_1 = np.zeros(tau.shape)
+    I_2 = np.zeros(tau.shape)
+    s = 1
+
+    # region IV: :404-471
+    m4 = np.imag(r1) != 0
+    if np.any(m4):
+        t4 = tau[:, m4]
+        a1, b1, a2, b2, CC, DD, k4, g0 = _case4_params(a, r_o, r2[m4], r4[m4])
+        x_p = (rplus + b1) / a2
+        x_m = (rminus + b1) / a2
+        x_o = np.inf if r_o == np.inf else (r_o + b1) / a2
+        gp = (g0 * x_p - 1.) / (g0 + x_p)
+        gm = (g0 * x_m - 1.) / (g0 + x_m)
+        aux = np.arctan(x_o) + np.arctan(g0)
+        pref = 2. / (CC + DD)
+        Ir_o = pref * sp.ellipkinc(aux, k4)
+        X4 = (1. / pref) * (s * (-t4) + Ir_o)
+        sn, cn, dn, am = sp.ellipj(X4, k4)
+        sc = sn / cn
+        r_s[:, m4] = -a2 * (g0 - sc) / (1 + g0 * sc) - b1
+        if do_phi_and_t:
+            S1a0, S2a0 = S1_S2(g0, am, k4, ret_s2=True)
+            S1b0, S2b0 = S1_S2(g0, aux, k4, ret_s2=True)
+            S1ap, _ = S1_S2(gp, am, k4, ret_s2=False)
+            S1bp, _ = S1_S2(gp, aux, k4, ret_s2=False)
+            S1am, _ = S1_S2(gm, am, k4, ret_s2=False)
+            S1bm, _ = S1_S2(gm, aux, k4, ret_s2=False)
+            aa0 = (a2 / g0) * (1 + g0 ** 2)
+            Pi_1 = s * pref * aa0 * (S1a0 - S1b0)
+            Pi_2 = s * pref * (aa0 ** 2) * (S2a0 - S2b0)
+            Pi_p = s * pref * (1 + g0 ** 2) / (g0 ** 2 + g0 * x_p) * (S1ap - S1bp)
+            Pi_m = s * pref * (1 + g0 ** 2) / (g0 ** 2 + g0 * x_m) * (S1am - S1bm)
+            aa1 = (a2 / g0 - b1)
+            I_1[:, m4] = aa1 * (-t4) - Pi_1
+            I_2[:, m4] = (aa1 ** 2) * (-t4) - 2 * aa1 * Pi_1 + Pi_2
+            I_p[:, m4] = g0 / (a2 - a2 * g0 * x_p) * (-t4 - Pi_p)
+            I_m[:, m4] = g0 / (a2 - a2 * g0 * x_m) * (-t4 - Pi_m)
+
+    # region III: :473-552
+    m3 = (np.imag(r3) != 0) * (~m4)
+    if np.any(m3):
+        t3 = tau[:, m3]
+        a1, b1, rr1, rr2, rr21, AA, BB, k3 = _case3_params(r1[m3], r2[m3], r4[m3])
+        rrp1, rrp2 = rplus - rr1, rplus - rr2
+        rrm1, rrm2 = rminus - rr1, rminus - rr2
+        x_p = (AA * rrp1 - BB * rrp2) / (AA * rrp1 + BB * rrp2)
+        x_m = (AA * rrm1 - BB * rrm2) / (AA * rrm1 + BB * rrm2)
+        if r_o == np.inf:
+            x_o = (AA - BB) / (AA + BB)
+        else:
+            x_o = (AA * (r_o - rr1) - BB * (r_o - rr2)) / (AA * (r_o - rr1) + BB * (r_o - rr2))
+        alp = -1. / x_p
+        alm = -1. / x_m
+        al0 = (BB + AA) / (BB - AA)
+        aux = np.arccos(x_o)
+        pref = (1. / np.sqrt(AA * BB))
+        Ir_o = pref * sp.ellipkinc(aux, k3)
+        X3 = (1. / pref) * (-t3 + s * Ir_o)
+        sn, cn, dn, am = sp.ellipj(X3, k3)
+        r_s[:, m3] = ((BB * rr2 - AA * rr1) + (BB * rr2 + AA * rr1) * cn) / ((BB - AA) + (BB + AA) * cn)
+        if do_phi_and_t:
+            R1a0, R2a0 = R1_R2(al0, am, k3)
+            R1b0, R2b0 = R1_R2(al0, aux, k3)
+            R1ap, _ = R1_R2(alp, am, k3, ret_r2=False)
+            R1bp, _ = R1_R2(alp, aux, k3, ret_r2=False)
+            if np.abs(a) > MINSPIN:
+                R1am, _ = R1_R2(alm, am, k3, ret_r2=False)
+                R1bm, _ = R1_R2(alm, aux, k3, ret_r2=False)
+            else:
+                R1am = np.zeros(R1ap.shape)
+                R1bm = np.zeros(R1ap.shape)
+            c0 = (2 * rr21 * np.sqrt(AA * BB)) / (BB ** 2 - AA ** 2)
+            Pi_1 = c0 * (R1a0 - s * R1b0)
+            Pi_2 = c0 ** 2 * (R2a0 - s * R2b0)
+            Pi_p = ((2 * rr21 * np.sqrt(AA * BB)) / (BB * rrp2 - AA * rrp1)) * (R1ap - s * R1bp)
+            Pi_m = ((2 * rr21 * np.sqrt(AA * BB)) / (BB * rrm2 - AA * rrm1)) * (R1am - s * R1bm)
+            pr = ((BB * rr2 + AA * rr1) / (BB + AA))
+            I_1[:, m3] = pr * (-t3) + Pi_1
+            I_2[:, m3] = pr ** 2 * (-t3) + 2 * pr * Pi_1 + np.sqrt(AA * BB) * Pi_2
+            I_p[:, m3] = -((BB + AA) * (-t3) + Pi_p) / (BB * rrp2 + AA * rrp1)
+            I_m[:, m3] = -((BB + AA) * (-t3) + Pi_m) / (BB * rrm2 + AA * rrm1)
+
+    # regions II and I (all roots real): :554-624
+    m2 = (np.imag(r3) == 0.) * (~m3)
+    if np.any(m2):
+        t2 = tau[:, m2]
+        rr1, rr2, rr3, rr4 = (np.real(r)[m2] for r in (r1, r2, r3, r4))
+        rr31, rr32, rr41, rr42, rr43 = rr3 - rr1, rr3 - rr2, rr4 - rr1, rr4 - rr2, rr4 - rr3
+        rrp3, rrm3, rrp4, rrm4 = rplus - rr3, rminus - rr3, rplus - rr4, rminus - rr4
+        k2 = (rr32 * rr41) / (rr31 * rr42)
+        if r_o == np.inf:
+            x_o = np.sqrt(rr31 / rr41)
+        else:
+            x_o = np.sqrt((rr31 * (r_o - rr4)) / (rr41 * (r_o - rr3)))
+        aux = np.arcsin(x_o)
+        Ir_o = 2 * sp.ellipkinc(aux, k2) / np.sqrt(rr31 * rr42)
+        X2 = 0.5 * np.sqrt(rr31 * rr42) * (-t2 + s * Ir_o)
+        sn, cn, dn, am = sp.ellipj(X2, k2)
+        rs = (rr4 * rr31 - rr3 * rr41 * (sn) ** 2) / (rr31 - rr41 * (sn) ** 2)
+        r_s[:, m2] = rs
+        if do_phi_and_t:
+            dX = -0.5 * np.sqrt(rr31 * rr42)
+            dsn2 = 2 * sn * cn * dn * dX
+            drs = rr31 * rr43 * rr41 * dsn2 / ((rr31 - rr41 * sn ** 2) ** 2)
+            drs *= -1
+            Rpot_o = (r_o - rr1) * (r_o - rr2) * (r_o - rr3) * (r_o - rr4)
+            drs_o = s * np.sqrt(Rpot_o)
+            H = drs / (rs - rr3) - drs_o / (r_o - rr3)
+            E = np.sqrt(rr31 * rr42) * (sp.ellipeinc(am, k2) - s * sp.ellipeinc(aux, k2))
+            c2 = 2. / np.sqrt(rr31 * rr42)
+            Pi_1 = c2 * (ellip_pi(rr41 / rr31, am, k2) - s * ellip_pi(rr41 / rr31, aux, k2))
+            npl = (rrp3 * rr41) / (rrp4 * rr31)
+            nmi = (rrm3 * rr41) / (rrm4 * rr31)
+            Pi_p = c2 * (rr43 / (rrp3 * rrp4)) * (ellip_pi(npl, am, k2) - s * ellip_pi(npl, aux, k2))
+            Pi_m = c2 * (rr43 / (rrm3 * rrm4)) * (ellip_pi(nmi, am, k2) - s * ellip_pi(nmi, aux, k2))
+            I_1[:, m2] = rr3 * (-t2) + rr43 * Pi_1
+            I_2[:, m2] = H - 0.5 * (rr1 * rr4 + rr2 * rr3) * (-t2) - E
+            I_p[:, m2] = t2 / rrp3 - Pi_p
+            I_m[:, m2] = t2 / rrm3 - Pi_m
+
+    # combination, B1/B2: :626-633
+    I_0 = -tau
+    I_phi = (2 * a / (rplus - rminus)) * ((rplus - 0.5 * a * lam) * I_p - (rminus - 0.5 * a * lam) * I_m)
+    I_tA = (4 / (rplus - rminus)) * ((rplus ** 2 - 0.5 * a * lam * rplus) * I_p - (rminus ** 2 - 0.5 * a * lam * rminus) * I_m)
+    I_t = I_tA + 4 * I_0 + 2 * I_1 + I_2
+    I_sig = I_2
+    return r_s, I_phi, I_t, I_sig
+
+
+# ----------------------------------------------------------------------------
+# drivers
+# ----------------------------------------------------------------------------
+
+
+def coords_at_tau(a, r_o, th_o, alpha, beta, tau, do_phi_and_t=True):
+    """(sigma, [t, r, theta, phi]) at Mino times tau; kgeo/kerr_raytracing_ana.py:126-193."""
+    if tau.ndim == 1:
+        tau = tau.reshape(1, tau.shape[0])
+    lam, eta = conserved(a, th_o, alpha, beta)
+    s_o = beta_sign(beta)
+    up, um, _, _, _ = theta_turning(a, th_o, lam, eta)
+    r1, r2, r3, r4, _ = quartic_roots(a, lam, eta)
+    th_s, G_ph, G_t = theta_solution(a, th_o, s_o, lam, eta, up, um, tau, do_phi_and_t)
+    r_s, I_ph, I_t, I_sig = radial_solution(a, r_o, lam, eta, r1, r2, r3, r4, tau, do_phi_and_t)
+    sig = 0 + I_sig + a ** 2 * G_t
+    t = 0 + I_t + a ** 2 * G_t
+    ph = 0 + I_ph + lam * G_ph
+    return sig, [t, r_s, th_s, ph]
+
+
+def raytrace(a, r_o, th_o, alpha, beta, ngeo, maxtaufrac=MAXTAUFRAC):
+    """Full-range analytic trace; kgeo/kerr_raytracing_ana.py:46-122.
+
+    Returns a dict with mino_times (ngeo, npix), affine_times, t, r, th, ph
+    and the per-ray classification (lam, eta, rclass, thclass, tau_tot).
+    """
+    check_spin(a)
+    check_observer(r_o, th_o)
+    alpha, beta = as_pixels(alpha, beta)
+    lam, eta = conserved(a, th_o, alpha, beta)
+    r1, r2, r3, r4, rclass = quartic_roots(a, lam, eta)
+    tau_tot = mino_total(a, r_o, eta, r1, r2, r3, r4)
+    tau = np.linspace(0, maxtaufrac * tau_tot, ngeo)
+    sig, (t, r, th, ph) = coords_at_tau(a, r_o, th_o, alpha, beta, tau)
+    _, _, _, _, thclass = theta_turning(a, th_o, lam, eta)
+    return dict(mino_times=tau, affine_times=sig, t=t, r=r, th=th, ph=ph,
+                lam=lam, eta=eta, rclass=rclass, thclass=thclass, tau_tot=tau_tot,
+                roots=np.stack([r1, r2, r3, r4]))
+
+
+def n_equatorial_crossings(a, th_o, alpha, beta, tau):
+    """Fractional-floor count of equatorial crossings; kgeo/kerr_raytracing_utils.py:605-684."""
+    one = tau.ndim == 1
+    if one:
+        tau = tau.reshape(1, tau.shape[0])
+    lam = -alpha * np.sin(th_o)
+    eta = (alpha ** 2 - a ** 2) * np.cos(th_o) ** 2 + beta ** 2
+    out = np.empty(tau.shape)
+    vort = eta <= 0
+    out[:, vort] = -2
+    if np.any(~vort):
+        up, um, ratio, a2um = u_roots(a, th_o, lam[~vort], eta[~vort])
+        b = beta[~vort]
+        tr = tau[:, ~vort]
+        F0 = sp.ellipkinc(np.arcsin(np.cos(th_o) / np.sqrt(up)), ratio)
+        K = sp.ellipkinc(0.5 * np.pi, ratio)
+        res = np.empty(tr.shape)
+        if th_o < (np.pi / 2.):
+            lo = b <= 0
+            res[:, lo] = (np.floor((tr * np.sqrt(-a2um) - F0) / (2 * K)))[:, lo]
+            res[:, ~lo] = (np.floor((tr * np.sqrt(-a2um) + F0) / (2 * K)) - 1)[:, ~lo]
+        else:
+            hi = b >= 0
+            res[:, hi] = (np.floor((tr * np.sqrt(-a2um) + F0) / (2 * K)))[:, hi]
+            res[:, ~hi] = (np.floor((tr * np.sqrt(-a2um) - F0) / (2 * K)) - 1)[:, ~hi]
+        out[:, ~vort] = res
+    return out[0] if one else out
+
+
+def n_poloidal_orbits(a, th_o, alpha, beta, tau):
+    """Fractional number of poloidal orbits; kgeo/kerr_raytracing_utils.py:551-603."""
+    one = tau.ndim == 1
+    if one:
+        tau = tau.reshape(1, tau.shape[0])
+    lam = -alpha * np.sin(th_o)
+    eta = (alpha ** 2 - a ** 2) * np.cos(th_o) ** 2 + beta ** 2
+    out = np.empty(tau.shape)
+    vort = eta <= 0
+    out[:, vort] = -2
+    if np.any(~vort):
+        up, um, ratio, a2um = u_roots(a, th_o, lam[~vort], eta[~vort])
+        K = sp.ellipk(ratio)
+        npol = (np.sqrt(-a2um.astype(complex)) * tau[:, ~vort]) / (4 * K)
+        out[:, ~vort] = np.real(npol.astype(complex))
+    return out[0] if one else out
+
+
+def outside_critical(a, th_o, alpha, beta):
+    """1 where real r4 > r_h and eta >= 0, else 0; kgeo/kerr_raytracing_utils.py:794-826."""
+    rh = 1 + np.sqrt(1 - a ** 2)
+    lam = -alpha * np.sin(th_o)
+    eta = (alpha ** 2 - a ** 2) * (np.cos(th_o)) ** 2 + beta ** 2
+    r1, r2, r3, r4, _ = quartic_roots(a, lam, eta)
+    sel = (np.imag(r4) == 0) * (r4 > rh) * ~(eta < 0)
+    out = np.empty(alpha.shape)
+    out[sel] = 1
+    out[~sel] = 0
+    return out
+
+
+# ----------------------------------------------------------------------------
+# equatorial lensing
+# ----------------------------------------------------------------------------
+
+
+def r_equatorial(a, r_o, th_o, mbar, alpha, beta):
+    """(r_s, Ir, Imax, Nmax) of the mbar-th equatorial crossing.
+
+    kgeo/equatorial_lensing.py:85-196 (GL19b eq. 81 with the C8 typo fixed).
+    """
+    lam = -alpha * np.sin(th_o)
+    eta = (alpha ** 2 - a ** 2) * np.cos(th_o) ** 2 + beta ** 2
+    r_s = np.empty(alpha.shape)
+    Ir = np.empty(alpha.shape)
+    Imax = np.empty(alpha.shape)
+    Nmax = np.empty(alpha.shape)
+    vort = eta <= 0
+    r_s[vort] = -1
+    Ir[vort] = -1
+    Imax[vort] = -1
+    Nmax[vort] = -2
+    if np.any(~vort):
+        lam_r = lam[~vort]
+        eta_r = eta[~vort]
+        b = beta[~vort]
+        up, um, ratio, a2um = u_roots(a, th_o, lam_r, eta_r)
+        F0 = sp.ellipkinc(np.arcsin(np.cos(th_o) / np.sqrt(up)), ratio)
+        K = sp.ellipkinc(0.5 * np.pi, ratio)
+        r1, r2, r3, r4, _ = quartic_roots(a, lam_r, eta_r)
+        imax = mino_total(a, r_o, eta_r, r1, r2, r3, r4)
+        nmax = np.empty(imax.shape)
+        ir = np.empty(imax.shape)
+        if th_o < (np.pi / 2.):
+            m = mbar + np.heaviside(b, 0)
+            lo = b <= 0
+            nmax[lo] = (np.floor((imax * np.sqrt(-a2um) - F0) / (2 * K)))[lo]
+            ir[lo] = ((2 * m * K + F0) / np.sqrt(-a2um))[lo]
+            nmax[~lo] = (np.floor((imax * np.sqrt(-a2um) + F0) / (2 * K)) - 1)[~lo]
+            ir[~lo] = ((2 * m * K - F0) / np.sqrt(-a2um))[~lo]
+        else:
+            m = mbar + np.heaviside(-b, 0)
+            hi = b >= 0
+            nmax[hi] = (np.floor((imax * np.sqrt(-a2um) + F0) / (2 * K)))[hi]
+            ir[hi] = ((2 * m * K - F0) / np.sqrt(-a2um))[hi]
+            nmax[~hi] = (np.floor((imax * np.sqrt(-a2um) - F0) / (2 * K)) - 1)[~hi]
+            ir[~hi] = ((2 * m * K + F0) / np.sqrt(-a2um))[~hi]
+        rs = radial_solution(a, r_o, lam_r, eta_r, r1, r2, r3, r4,
+                             ir.reshape(1, len(ir)), do_phi_and_t=False)[0][0]
+        rs[nmax < mbar] = 0
+        r_s[~vort] = rs
+        Ir[~vort] = ir
+        Imax[~vort] = imax
+        Nmax[~vort] = nmax
+    return r_s, Ir, Imax, Nmax
+
+
+# ----------------------------------------------------------------------------
+# equatorial image: velocity and emissivity models (config-5 subset)
+# ----------------------------------------------------------------------------
+
+
+def r_isco(a, s=1):
+    """ISCO radius; kgeo/velocities.py:300-302."""
+    z1 = 1 + np.cbrt(1 - a ** 2) * (np.cbrt(1 + a) + np.cbrt(1 - a))
+    z2 = np.sqrt(3 * a ** 2 + z1 ** 2)
+    return 3 + z2 - s * np.sqrt((3 - z1) * (3 + z1 + 2 * z2))
+
+
+def u_infall(a, r):
+    """Geodesic infall from rest at infinity; kgeo/velocities.py:211-226."""
+    Delta = r ** 2 + a ** 2 - 2 * r
+    Xi = (r ** 2 + a ** 2) ** 2 - Delta * a ** 2
+    u0 = Xi / (r ** 2 * Delta)
+    u1 = -np.sqrt(2 * r * (r ** 2 + a ** 2)) / (r ** 2)
+    u3 = 2 * a / (r * Delta)
+    return u0, u1, 0, u3
+
+
+def u_subkep(a, r, fac_subkep=1, retrograde=False):
+    """Sub-Keplerian outside the ISCO, conserved-quantity infall inside; kgeo/velocities.py:284-359."""
+    s = -1 if retrograde else 1
+    ri = r_isco(a, s)
+    u0 = np.zeros(r.shape)
+    u1 = np.zeros(r.shape)
+    u3 = np.zeros(r.shape)
+    out = r >= ri
+    spin = np.abs(a)
+    asign = np.sign(a)
+    if np.any(out):
+        rr = r[out]
+        Delta = (rr ** 2 - 2 * rr + a ** 2)
+        Xi = (rr ** 2 + a ** 2) ** 2 - Delta * a ** 2
+        ell = asign * s * (rr ** 2 + spin ** 2 - s * 2 * spin * np.sqrt(rr)) / (rr ** 1.5 - 2 * np.sqrt(rr) + s * spin)
+        ell *= fac_subkep
+        gam = np.sqrt(Delta / (Xi / rr ** 2 - 4 * a * ell / rr - (1 - 2 / rr) * ell ** 2))
+        H = (2 * rr - a * ell) / Delta
+        chi = 1 / (1 + (2 / rr) * (1 + H))
+        Omega = (chi / rr ** 2) * (ell + a * H)
+        u0[out] = gam / chi
+        u3[out] = (gam / chi) * Omega
+    if np.any(~out):
+        rr = r[~out]
+        Delta = (rr ** 2 - 2 * rr + a ** 2)
+        Xi = (rr ** 2 + a ** 2) ** 2 - Delta * a ** 2
+        Delta_i = (ri ** 2 - 2 * ri + a ** 2)
+        Xi_i = (ri ** 2 + a ** 2) ** 2 - Delta_i * a ** 2
+        ell_i = asign * s * (ri ** 2 + spin ** 2 - s * 2 * spin * np.sqrt(ri)) / (ri ** 1.5 - 2 * np.sqrt(ri) + s * spin)
+        ell_i *= fac_subkep
+        gam_i = np.sqrt(Delta_i / (Xi_i / ri ** 2 - 4 * a * ell_i / ri - (1 - 2 / ri) * ell_i ** 2))
+        H = (2 * rr - a * ell_i) / Delta
+        chi = 1 / (1 + (2 / rr) * (1 + H))
+        Omega = (chi / rr ** 2) * (ell_i + a * H)
+        nu = (rr / Delta) * np.sqrt(Xi / rr ** 2 - 4 * a * ell_i / rr - (1 - 2 / rr) * ell_i ** 2 - Delta / gam_i ** 2)
+        u0[~out] = gam_i / chi
+        u1[~out] = -gam_i * (Delta / rr ** 2) * nu
+        u3[~out] = (gam_i / chi) * Omega
+    return u0, u1, 0, u3
+
+
+def u_general(a, r, fac_subkep=1, beta_phi=1, beta_r=1, retrograde=False):
+    """Infall / sub-Keplerian mix (AART); kgeo/velocities.py:442-470."""
+    Delta = r ** 2 + a ** 2 - 2 * r
+    u0i, u1i, _, u3i = u_infall(a, r)
+    Om_i = u3i / u0i
+    u0s, u1s, _, u3s = u_subkep(a, r, retrograde=retrograde, fac_subkep=fac_subkep)
+    Om_s = u3s / u0s
+    u1 = u1s + (1 - beta_r) * (u1i - u1s)
+    Omega = Om_s + (1 - beta_phi) * (Om_i - Om_s)
+    u0 = np.sqrt(1 + (r ** 2) * (u1 ** 2) / Delta)
+    u0 /= np.sqrt(1 - (r ** 2 + a ** 2) * Omega ** 2 - (2 / r) * (1 - a * Omega) ** 2)
+    u3 = u0 * Omega
+    return u0, u1, 0, u3
+
+
+def emis_bpl(a, r, p1=-2.0, p2=-0.5):
+    """Broken power law; kgeo/emissivities.py:121-127."""
+    rh = 1 + np.sqrt(1 - a ** 2)
+    return np.exp(p1 * np.log(r / rh) + p2 * np.log(r / rh) ** 2)
+
+
+def redshift(a, r, lam, eta, kr_sign, kth_sign, u0, u1, u2, u3, th=np.pi / 2):
+    """g = 1 / (-k.u); kgeo/equatorial_images.py:307-334."""
+    a2 = a ** 2
+    r2 = r ** 2
+    cth2 = np.cos(th) ** 2
+    sth2 = np.sin(th) ** 2
+    Delta = r2 - 2 * r + a2
+    R = (r2 + a2 - a * lam) ** 2 - Delta * (eta + (lam - a) ** 2)
+    TH = eta + a2 * cth2 - lam * lam * cth2 / sth2
+    return 1 / (1 * u0 - lam * u3 - np.sign(kth_sign) * u2 * np.sqrt(TH) - np.sign(kr_sign) * u1 * np.sqrt(R) / Delta)
+
+
+def image_order(a, r_o, th_o, mbar, alpha, beta, p1=-2.0, p2=-0.5,
+                fac_subkep=1, beta_phi=1, beta_r=1, retrograde=False,
+                specind=1, sinthb=np.pi / 4., emiscut_in=0, emiscut_out=1.e10):
+    """Unpolarised I, g, r_s, Ir, Imax, Nmax of one image order (bpl emissivity, general velocity).
+
+    kgeo/equatorial_images.py:124-264 with kgeo/emissivities.py:83-127 and
+    kgeo/velocities.py:442-470.
+    """
+    rh = 1 + np.sqrt(1 - a ** 2)
+    lam = -alpha * np.sin(th_o)
+    eta = (alpha ** 2 - a ** 2) * np.cos(th_o) ** 2 + beta ** 2
+    r_s, Ir, Imax, Nmax = r_equatorial(a, r_o, th_o, mbar, alpha, beta)
+    g = np.zeros(alpha.shape)
+    I = np.zeros(alpha.shape)
+    zero = (Nmax < mbar) + (Nmax == -1) + (r_s <= rh)
+    if emiscut_in > 0:
+        zero = zero + (r_s < emiscut_in)
+    if emiscut_out > 0:
+        zero = zero + (r_s > emiscut_out)
+    if np.any(~zero):
+        live = ~zero
+        inside = ~outside_critical(a, th_o, alpha[live], beta[live]).astype(bool)
+        kr = np.empty(inside.shape)
+        outgoing = inside + (Ir[live] <= 0.5 * Imax[live])
+        kr[outgoing] = 1
+        kr[~outgoing] = -1
+        kth = -1 * np.power(-1, np.mod(mbar, 2)) if th_o < 0.5 * np.pi else 1 * np.power(-1, np.mod(mbar, 2))
+        u0, u1, u2, u3 = u_general(a, r_s[live], fac_subkep=fac_subkep, beta_phi=beta_phi,
+                                   beta_r=beta_r, retrograde=retrograde)
+        gg = redshift(a, r_s[live], lam[live], eta[live], kr, kth, u0, u1, u2, u3)
+        g[live] = gg
+        j = emis_bpl(a, r_s[live], p1=p1, p2=p2)
+        j *= (gg ** specind)
+        j *= (sinthb ** (1 + specind))
+        I[live] = (gg ** 2) * j
+    return I, g, r_s, Ir, Imax, Nmax
+
+
+def image_grid(alpha_min, alpha_max, beta_min, beta_max, psize):
+    """Pixel grid of make_image; kgeo/equatorial_images.py:48-55 (spacing is (max-min)/(n-1))."""
+    n_a = int(np.floor(alpha_max - alpha_min) / psize)
+    alphas = np.linspace(alpha_min, alpha_min + n_a * psize, n_a)
+    n_b = int(np.floor(beta_max - beta_min) / psize)
+    betas = np.linspace(beta_min, beta_min + n_b * psize, n_b)
+    A, B = np.meshgrid(alphas, betas)
+    return A.flatten(), B.flatten()

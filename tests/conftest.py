@@ -1,0 +1,24 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, 'tests', 'golden')
+
+
+def pytest_configure(config):
+    config.addinivalue_line('markers', 'gpu: needs a CUDA GPU (GB300, sm_103a) and the built extension')
+
+
+@pytest.fixture
+def golden():
+    import numpy as np
+
+    def load(name):
+        with np.load(os.path.join(GOLDEN, name + '.npz')) as f:
+            return {k: f[k] for k in f.files}
+    return load

@@ -1,0 +1,225 @@
+"""Generate the golden fixtures in this folder by running the reference kgeo itself.
+
+Run from the repository root, in a container that has the reference checked out:
+
+    python tests/golden/make_golden.py [path-to-kgeo-checkout]
+
+The reference is imported unmodified. Its optional plotting / HDF5 / ehtim
+imports are replaced by inert stand-ins, numpy-2 removed aliases (np.infty,
+np.NaN) are restored, and the B-field data table that kgeo loads at import
+time (absent from the checkout) is regenerated into a temporary folder from
+the recipe in kgeo/bfields.py:7-20. None of those touch the hot path.
+
+Each fixture is a compressed .npz holding the inputs and the reference's
+outputs; tests/test_oracle_golden.py pins the CPU oracle to them and the GPU
+parity tests check the CUDA path against them.
+"""
+import contextlib
+import io
+import os
+import sys
+import tempfile
+import types
+import warnings
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def import_reference(path):
+    """Import kgeo from ``path`` with the stand-ins described in the module docstring."""
+    np.infty = np.inf
+    np.NaN = np.nan
+    np.Inf = np.inf
+
+    def stub(name, **attrs):
+        mod = types.ModuleType(name)
+        mod.__dict__.update(attrs)
+        sys.modules[name] = mod
+        return mod
+
+    class Inert:
+        def __getattr__(self, k):
+            return Inert()
+
+        def __call__(self, *a, **k):
+            return Inert()
+
+    mpl = stub('matplotlib')
+    plt = stub('matplotlib.pyplot')
+    plt.__getattr__ = lambda k: Inert()
+    mpl.pyplot = plt
+    stub('h5py', File=lambda *a, **k: Inert())
+    stub('ehtim')
+    stub('ehtim.parloop', Counter=Inert)
+    stub('ehtim.observing')
+    stub('ehtim.observing.obs_helpers', prog_msg=lambda *a, **k: None)
+
+    import pkg_resources
+    table = os.path.join(tempfile.mkdtemp(prefix='kgeo_bz_'), 'bz_fr_data.dat')
+    orig = pkg_resources.resource_stream
+
+    def resource_stream(pkg, name):
+        if name == 'bz_fr_data.dat':
+            if not os.path.exists(table):
+                import mpmath
+
+                def f(r):
+                    r = r + 0j
+                    out = (mpmath.polylog(2, 2. / r) - np.log(1 - 2. / r) * np.log(r / 2.)) * r * r * (2 * r - 3) / 8.
+                    out += (1 + 3 * r - 6 * r * r) * np.log(r / 2.) / 12.
+                    out += 11. / 72. + 1. / (3. * r) + r / 2. - r * r / 2.
+                    return float(np.real(complex(out)))
+                rs = np.linspace(1, 100, 2000)
+                np.savetxt(table, np.vstack((rs, np.array([f(r) for r in rs]))))
+            return open(table, 'rb')
+        return orig(pkg, name)
+
+    pkg_resources.resource_stream = resource_stream
+    sys.path.insert(0, path)
+    import kgeo  # noqa: F401
+    import kgeo.kerr_raytracing_ana as ana
+    import kgeo.kerr_raytracing_utils as utils
+    import kgeo.equatorial_lensing as lensing
+    import kgeo.equatorial_images as images
+    import kgeo.scipy_ellip_binding as binding
+    import kgeo.velocities as vel
+    import kgeo.emissivities as emis
+    return types.SimpleNamespace(ana=ana, utils=utils, lensing=lensing, images=images,
+                                 binding=binding, vel=vel, emis=emis)
+
+
+def quiet(fn, *a, **k):
+    with contextlib.redirect_stdout(io.StringIO()):
+        return fn(*a, **k)
+
+
+def trace_case(ref, a, r_o, th_o, alpha, beta, ngeo):
+    alpha = np.asarray(alpha, dtype=float)
+    beta = np.asarray(beta, dtype=float)
+    g = quiet(ref.ana.raytrace_ana, a=a, observer_coords=[0, r_o, th_o, 0],
+              image_coords=[alpha, beta], ngeo=ngeo, plotdata=False)
+    t, r, th, ph = g.geo_coords
+    lam = -alpha * np.sin(th_o)
+    eta = (alpha ** 2 - a ** 2) * np.cos(th_o) ** 2 + beta ** 2
+    if abs(a) < ref.utils.MINSPIN and np.any(eta < 0):
+        eta[eta < 0] = ref.utils.EP
+    r1, r2, r3, r4, rclass = ref.utils.radial_roots(a, lam, eta)
+    thclass = ref.utils.angular_turning(a, th_o, lam, eta)[4]
+    return dict(a=a, r_o=r_o, th_o=th_o, ngeo=ngeo, alpha=alpha, beta=beta,
+                mino=g.mino_times, sig=g.affine_times, t=t, r=r, th=th, ph=ph,
+                rclass=rclass, thclass=thclass, tau_tot=g.tautot, nmax_eq=quiet(lambda: g.nmax_eq),
+                roots=np.stack([r1, r2, r3, r4]))
+
+
+def save(name, d):
+    path = os.path.join(HERE, name + '.npz')
+    np.savez_compressed(path, **{k: np.asarray(v) for k, v in d.items()})
+    print('wrote', path, os.path.getsize(path), 'bytes')
+
+
+def grid(lo, hi, n):
+    x = np.linspace(lo, hi, n)
+    A, B = np.meshgrid(x, x)
+    return A.flatten(), B.flatten()
+
+
+def main(path):
+    warnings.filterwarnings('ignore')
+    ref = import_reference(path)
+    deg = np.pi / 180.
+
+    # configuration-1 geometry on a coarser grid
+    A, B = grid(-8, 8, 16)
+    save('trace_a094_i20_16x16', trace_case(ref, 0.94, 1.e4, 20 * deg, A, B, 48))
+
+    # edge rays: alpha = 0 (u_+ clamped to 1), tiny alpha, vortical, eta ~ 0, large impact
+    ea = [0., 0., 1e-9, 3., -4., 0.05, 0.3, -0.2, 12., -9., 2.5, 0.0001]
+    eb = [3., -3., 3., 0., 0., 0.05, -0.1, 0.15, 7., -11., 1.0, -4.0]
+    save('trace_edge_a094_i20', trace_case(ref, 0.94, 1.e4, 20 * deg, ea, eb, 32))
+    save('trace_edge_a050_i120', trace_case(ref, 0.5, 1.e4, 120 * deg, ea, eb, 32))
+    save('trace_lowspin_a5e-5_i20', trace_case(ref, 5e-5, 1.e4, 20 * deg, [3., -4., 0.5, 6.], [2., 1., 0.3, -2.], 24))
+    save('trace_spin0_i45', trace_case(ref, 0.0, 1.e4, 45 * deg, [3., -4., 0.5, 6.], [2., 1., 0.3, -2.], 24))
+    save('trace_rinf_a07_i30', trace_case(ref, 0.7, np.inf, 30 * deg, [3., -4., 0.5, 6., 1.], [2., 1., 0.3, -2., -6.], 24))
+
+    # configuration-2 draws (a ~ U[0, 0.998), th_o ~ U[1, 89] deg), coarse grids
+    rng = np.random.default_rng(0)
+    A, B = grid(-10, 10, 12)
+    for i in range(3):
+        a = float(rng.uniform(0, 0.998))
+        th = float(rng.uniform(1, 89)) * deg
+        save('trace_rand%d' % i, trace_case(ref, a, 1.e4, th, A, B, 24))
+
+    # the midplane-crossing rays of tests/test_geodesics_kerr_ana.py:54-70 (r_o = 1000, ngeo = 10000)
+    keys = [(0.42, 60., -17., 0.), (0.42, 60., -9., 0.), (0.42, 60., -4., 0.), (0.42, 60., 1., 0.),
+            (0.42, 60., 6., 0.), (0.42, 60., 8., 0.), (0.9, 10., -12., 0.), (0.9, 10., -4., 0.),
+            (0.9, 10., 1., 0.), (0.9, 10., 2., 0.), (0.73, 35., 0.0001, -10), (0.73, 35., 0.0001, -1.),
+            (0.73, 35., 0.0001, 1.), (0.73, 35., 0.0001, 3.), (0.73, 35., 0.0001, 4.)]
+    xs, ys, rows = [], [], []
+    for (spin, inc, al, be) in keys:
+        g = quiet(ref.ana.raytrace_ana, a=spin, observer_coords=[0, 1000., inc / 180. * np.pi, 0],
+                  ngeo=10000, image_coords=[al, be], plotdata=False)
+        t, r, h, p = np.array(g.geo_coords)[:, :, 0]
+        x = r * np.sin(h) * np.cos(p)
+        y = r * np.sin(h) * np.sin(p)
+        z = r * np.cos(h)
+        if z[0] > z[1]:
+            xi, yi, zi = x[::-1], y[::-1], z[::-1]
+        else:
+            xi, yi, zi = x, y, z
+        xs.append(np.interp(0, zi, xi))
+        ys.append(np.interp(0, zi, yi))
+        rows.append((spin, inc, al, be))
+    save('midplane_crossings', dict(keys=np.array(rows), x0=np.array(xs), y0=np.array(ys)))
+
+    # equatorial source radius, orders 0..2
+    rng = np.random.default_rng(1)
+    A, B = grid(-10, 10, 32)
+    for i, (a, th) in enumerate([(float(rng.uniform(0, 0.998)), float(rng.uniform(1, 89)) * deg),
+                                 (0.94, 17 * deg), (0.5, 120 * deg)]):
+        out = dict(a=a, r_o=1.e4, th_o=th, alpha=A, beta=B)
+        for m in range(3):
+            r_s, Ir, Imax, Nmax = ref.lensing.r_equatorial(a, 1.e4, th, m, A, B)
+            out.update({'r_s%d' % m: r_s, 'Ir%d' % m: Ir, 'Imax%d' % m: Imax, 'Nmax%d' % m: Nmax})
+        out['outside_crit'] = ref.utils.is_outside_crit(a, th, A, B)
+        save('requatorial_%d' % i, out)
+
+    # configuration-5 image (general velocity, bpl emissivity) on a coarse grid
+    em = ref.emis.Emissivity('bpl', p1=-2.0, p2=0.0)
+    ve = ref.vel.Velocity('general', fac_subkep=0.8, beta_r=0.5)
+    psize = 16. / 40
+    res = quiet(ref.images.make_image, 0.5, 1.e4, 60 * deg, 2, -8., 8., -8., 8., psize,
+                emissivity=em, velocity=ve)
+    n_side = int(np.floor(8. - -8.) / psize)
+    side = np.linspace(-8., -8. + n_side * psize, n_side)
+    Ai, Bi = np.meshgrid(side, side)
+    save('image_a05_i60', dict(a=0.5, r_o=1.e4, th_o=60 * deg, psize=psize, alpha=Ai.flatten(), beta=Bi.flatten(),
+                               I=res[0], r=res[3], g=res[5], n=res[7], np_=res[8],
+                               p1=-2.0, p2=0.0, fac_subkep=0.8, beta_r=0.5, beta_phi=1.0))
+
+    # elliptic Pi adapter: random in-domain points plus every special-case mask
+    rng = np.random.default_rng(2)
+    n = np.concatenate([rng.uniform(-3, 0.95, 400), rng.uniform(1.05, 6, 200),
+                        [1., 1., 0.5, 0.5, 2., np.inf, 0.3, 0.7]])
+    phi = np.concatenate([rng.uniform(-9, 9, 400), rng.uniform(-1.4, 1.4, 200),
+                          [2.0, -4.0, 1e-11, -1e-11, np.arcsin(np.sqrt(0.5)), 0.7, 3.0, 0.4]])
+    m = np.concatenate([rng.uniform(-5, 0.99, 400), rng.uniform(-2, 0.9, 200),
+                        [0.3, -0.2, 0.5, 0.5, 0.1, 0.4, 1.5, -2e14]])
+    save('ellip_pi', dict(n=n, phi=phi, m=m, pi=ref.binding.ellip_pi_arr(n, phi, m)))
+
+    # general velocity on a radial grid and at the ipole-checked points of tests/test_velocities.py
+    rr = np.linspace(1.2, 30., 200)
+    vout = {}
+    for i, (a, xi, bp, br, retro) in enumerate([(0.5, 0.8, 1.0, 0.5, False), (0.9375, 0.3, 0.1, 0.4, False),
+                                                (0.42, 0.24, 0.42, 0.24, True)]):
+        rh = 1 + np.sqrt(1 - a * a)
+        r = rr[rr > rh]
+        u0, u1, u2, u3 = ref.vel.u_general(a, r, fac_subkep=xi, beta_phi=bp, beta_r=br, retrograde=retro)
+        vout.update({'r%d' % i: r, 'u%d' % i: np.stack([u0, u1, u3]),
+                     'par%d' % i: np.array([a, xi, bp, br, float(retro)])})
+    save('velocity_general', vout)
+
+
+if __name__ == '__main__':
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')

@@ -1,0 +1,57 @@
+// Host (g++) build of the device arithmetic headers, for CPU unit checks of the
+// same code the CUDA kernels compile. Test-only: never loaded by the product.
+#include "../../kgeo_gb300/csrc/kg_ray.cuh"
+
+using namespace kg;
+
+static Observer make_obs(const double* ob) {
+  Observer o;
+  o.a = ob[0]; o.a2 = ob[1]; o.r_o = ob[2]; o.th_o = ob[3]; o.sin_th = ob[4]; o.cos_th = ob[5];
+  o.cos2 = ob[6]; o.rplus = ob[7]; o.rminus = ob[8]; o.minspin = (int)ob[9]; o.r_o_inf = (int)ob[10];
+  return o;
+}
+
+extern "C" {
+int hm_num_fields() { return NUM_FIELDS; }
+double hm_rf(double x, double y, double z) { return carlson_rf(x, y, z); }
+double hm_rj(double x, double y, double z, double p) { return carlson_rj(x, y, z, p); }
+double hm_rd(double x, double y, double z) { return carlson_rd(x, y, z); }
+double hm_rc(double x, double y) { return carlson_rc(x, y); }
+double hm_ellipf(double phi, double m) { return ellip_f(phi, m); }
+double hm_ellipe(double phi, double m) { return ellip_e_inc(phi, m); }
+double hm_ellippi(double n, double phi, double m) { return ellip_pi_ref(n, phi, m); }
+void hm_jacobi(double u, double m, double* out) {
+  Jacobi J = jacobi_landen(u, m);
+  out[0] = J.sn; out[1] = J.cn; out[2] = J.dn;
+}
+void hm_roots(const double* ob, double lam, double eta, double* out, int* rclass) {
+  Observer o = make_obs(ob);
+  Roots R = radial_roots(o, lam, eta);
+  out[0] = R.r1.re; out[1] = R.r1.im; out[2] = R.r2.re; out[3] = R.r2.im;
+  out[4] = R.r3.re; out[5] = R.r3.im; out[6] = R.r4.re; out[7] = R.r4.im;
+  *rclass = R.rclass;
+}
+unsigned hm_setup(const double* ob, const double* alpha, const double* beta, long n, double maxtaufrac,
+                  double* rec, int* code, int* rclass, int* thclass) {
+  Observer o = make_obs(ob);
+  unsigned flags = 0;
+  for (long i = 0; i < n; ++i) {
+    RayRec R;
+    flags |= ray_setup(o, alpha[i], beta[i], maxtaufrac, &R, rclass + i, thclass + i);
+    for (int k = 0; k < NUM_FIELDS; ++k) rec[k * n + i] = R.f[k];
+    code[i] = R.code;
+  }
+  return flags;
+}
+void hm_samples(const double* ob, const double* rec, const int* code, long n, const double* tau, long ntau,
+                int ordinary_active, double* t, double* r, double* th, double* ph, double* sig) {
+  Observer o = make_obs(ob);
+  for (long i = 0; i < n; ++i) {
+    RecView f{rec + i, n};
+    for (long g = 0; g < ntau; ++g) {
+      Sample S = sample_all(o, f, code[i], tau[g * n + i], ordinary_active != 0);
+      t[g * n + i] = S.t; r[g * n + i] = S.r; th[g * n + i] = S.th; ph[g * n + i] = S.ph; sig[g * n + i] = S.sig;
+    }
+  }
+}
+}
