@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the analytic Kerr ray tracer on GB300.
+
+Workload (one "step"): the production-size FP64 drop-in case — a 512 x 512 image-plane
+grid over alpha, beta in [-10, 10] M, spin a ~ U[0, 0.998) and inclination
+theta_o ~ U[1, 89] deg drawn with numpy default_rng(seed = rank), observer at r_o = 1e4 M,
+raytrace_ana with ngeo = 400 Mino samples per ray, plus the equatorial source radius
+r_equatorial for the orders n = 0, 1, 2 on every pixel. Inputs are synthetic (the
+reference has no dataset); they live in HBM before the timed region.
+
+Metric: rays/s (whole job, all ranks). Also reported: geodesic points/s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--case full|small]
+
+--impl reference times the reference's own CPU algorithm for this path (the oracle port
+under oracle/, numpy + scipy.special) on all host cores over a bounded seeded sample of
+the same workload. --case small runs a 128 x 128 grid of the same draw (for ncu captures).
+Multi-GPU: launched by torch.distributed.run, one rank per GPU, each rank traces its own
+image (weak scaling, no data-path collective); a barrier + CUDA synchronize bracket the
+timed steps and the max time over ranks is reported.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GRID = 512
+LIM = 10.0
+NGEO = 400
+ORDERS = (0, 1, 2)
+R_O = 1.0e4
+CPU_SAMPLE_RAYS = 16384      # rays of the bounded CPU sample (every 16th pixel of the grid)
+# FP64 floating-point work of the sample kernel per geodesic point on this workload, from the
+# ncu capture summarised in profiles/geo_samples_fp64_config2.md:
+# (dadd + dmul + 2 dfma thread instructions) / points. Used for roofline.achieved.
+FP64_FLOP_PER_POINT = None
+BYTES_PER_POINT = 48          # t, r, theta, phi, sigma, Mino tau written per point (8 B each)
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload(seed, grid=GRID):
+    rng = np.random.default_rng(seed)
+    a = float(rng.uniform(0, 0.998))
+    th_o = float(rng.uniform(1, 89)) * np.pi / 180
+    x = np.linspace(-LIM, LIM, grid)
+    A, B = np.meshgrid(x, x)
+    return a, th_o, A.flatten(), B.flatten()
+
+
+# ---------------------------------------------------------------------------
+# CPU: the reference algorithm (oracle port) on host cores
+# ---------------------------------------------------------------------------
+
+def _cpu_chunk(args):
+    a, th_o, A, B, ngeo = args
+    from oracle import kgeo_oracle as ko
+    import warnings
+    warnings.filterwarnings('ignore')
+    ko.raytrace(a, R_O, th_o, A, B, ngeo)
+    for m in ORDERS:
+        ko.r_equatorial(a, R_O, th_o, m, A, B)
+    return len(A)
+
+
+def cpu_sample(seed):
+    a, th_o, A, B = workload(seed)
+    idx = np.arange(0, A.size, A.size // CPU_SAMPLE_RAYS)[:CPU_SAMPLE_RAYS]
+    return a, th_o, A[idx], B[idx]
+
+
+def make_pool():
+    import multiprocessing as mp
+    cores = len(os.sched_getaffinity(0))
+    os.environ.setdefault('OMP_NUM_THREADS', '1')
+    os.environ.setdefault('OPENBLAS_NUM_THREADS', '1')
+    return mp.get_context('spawn').Pool(cores), cores
+
+
+def cpu_run(pool, cores, seed):
+    """One pass of the bounded sample over all cores; returns (rays, seconds)."""
+    a, th_o, A, B = cpu_sample(seed)
+    chunks = np.array_split(np.arange(A.size), cores * 4)
+    t0 = time.perf_counter()
+    n = sum(pool.map(_cpu_chunk, [(a, th_o, A[c], B[c], NGEO) for c in chunks if c.size]))
+    return n, time.perf_counter() - t0
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+
+class Clocks:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+         'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+         'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.idx), '--query-gpu=' + self.Q,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {'sm_mhz': float(np.median(sm)), 'sm_max_mhz': mx, 'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args):
+    rank, world, local = dist_env()
+    pool = cores = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        pool, cores = make_pool()  # spawn the CPU workers before any CUDA initialisation
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl' if torch.cuda.is_available() else 'gloo')
+    from kgeo_gb300 import device as dev
+    from kgeo_gb300 import equatorial_lensing as el
+    from kgeo_gb300 import kerr_raytracing_ana as kra
+
+    grid = GRID if args.case == 'full' else 128
+    a, th_o, A, B = workload(rank, grid)
+    npix = A.size
+    al, be = dev.as_device(A), dev.as_device(B)
+    prep = dev.PreparedRays(a, R_O, th_o, al, be, ngeo=NGEO)
+    out = prep.alloc()
+    flags = torch.zeros(1, dtype=torch.int32, device=al.device)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=al.device)
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def step(rec=None):
+        flush.zero_()
+        e = [ev() for _ in range(4)] if rec is not None else None
+        if e:
+            e[0].record(stream)
+        prep.setup()
+        if e:
+            e[1].record(stream)
+        prep.samples(out, flags=flags)
+        if e:
+            e[2].record(stream)
+        el.r_equatorial_device(a, R_O, th_o, ORDERS, al, be)
+        if e:
+            e[3].record(stream)
+            rec.append(e)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    recs = []
+    t0 = ev()
+    t1 = ev()
+    t0.record(stream)
+    for _ in range(args.steps):
+        step(recs)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    elapsed = t0.elapsed_time(t1) / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([elapsed], dtype=torch.float64, device=al.device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dist.barrier()
+        elapsed = float(tt.item())
+    setup_ms = np.mean([r[0].elapsed_time(r[1]) for r in recs])
+    samp_ms = np.mean([r[1].elapsed_time(r[2]) for r in recs])
+    eq_ms = np.mean([r[2].elapsed_time(r[3]) for r in recs])
+    rays = npix * args.steps * world
+    value = rays / elapsed
+    points = npix * NGEO
+    launches = 3 * args.steps
+
+    # end to end through the public API with host buffers: numpy in, numpy out
+    e2e = None
+    if args.steps > 0:
+        torch.cuda.synchronize()
+        t_e = time.perf_counter()
+        nsteps_e = max(1, min(args.steps, 3))
+        for _ in range(nsteps_e):
+            g = kra.raytrace_ana(a=a, observer_coords=[0, R_O, th_o, 0], image_coords=[A, B], ngeo=NGEO,
+                                 plotdata=False)
+            rq = [el.r_equatorial(a, R_O, th_o, m, A, B) for m in ORDERS]
+            del g, rq
+        dt = (time.perf_counter() - t_e) / nsteps_e
+        h2d = 2 * npix * 8 * (1 + len(ORDERS))
+        d2h = 6 * points * 8 + len(ORDERS) * 4 * npix * 8
+        e2e = {'value': npix * world / dt, 'unit': 'rays/s', 'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
+               'ms_per_step': dt * 1e3, 'path': 'kgeo_gb300.kerr_raytracing_ana.raytrace_ana + '
+                                                'equatorial_lensing.r_equatorial (numpy in/out)'}
+
+    if rank != 0:
+        return
+    pk = peaks()
+    fp64_peak = dev.fp64_peak_tflops()
+    roof = {'bound': 'fp64', 'unit': 'TFLOP/s', 'peak': fp64_peak,
+            'peak_source': 'FP64 FMA loop measured live by bench.py (kgeo_measure_fp64_peak)',
+            'kernel': 'samples_kernel', 'launch_ms': samp_ms, 'points_per_launch': points,
+            'traffic': None}
+    if FP64_FLOP_PER_POINT:
+        ach = FP64_FLOP_PER_POINT * points / (samp_ms * 1e-3) / 1e12
+        roof.update({'achieved': ach, 'frac': ach / fp64_peak, 'fp64_flop_per_point': FP64_FLOP_PER_POINT})
+    else:
+        roof.update({'achieved': None, 'frac': None})
+    hbm = BYTES_PER_POINT * points / (samp_ms * 1e-3) / 1e9
+    roof['hbm_write'] = {'achieved_gbs': hbm, 'peak_gbs': pk.get('hbm_gbs'),
+                         'frac': (hbm / pk['hbm_gbs']) if pk.get('hbm_gbs') else None,
+                         'bytes_per_point': BYTES_PER_POINT}
+    cpu = None
+    if pool is not None:
+        cpu_run(pool, cores, rank)  # warm the workers (imports)
+        n, dt = cpu_run(pool, cores, rank)
+        pool.close()
+        cpu = {'value': n / dt, 'unit': 'rays/s', 'cores': cores, 'kind': 'port',
+               'sample': '%d rays (every %dth pixel of the same grid and draw), ngeo=%d, r_equatorial n=0..2; '
+                         'oracle/kgeo_oracle.py (numpy+scipy restatement of the reference) on a %d-process pool, '
+                         '%.1f s wall' % (n, npix // CPU_SAMPLE_RAYS, NGEO, cores, dt)}
+    line = {
+        'metric': 'Kerr rays/s: FP64 raytrace_ana (ngeo=400) + r_equatorial n=0..2, 512x512 image',
+        'value': value, 'unit': 'rays/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': elapsed / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f64',
+        'data': 'synthetic: uniform image-plane grid, a and theta_o drawn from default_rng(rank)',
+        'config': {'workload': 'FP64 drop-in at production size (512x512 over [-10,10] M, a~U[0,0.998), '
+                               'theta_o~U[1,89] deg, r_o=1e4, ngeo=400, r_equatorial n=0,1,2)',
+                   'npix': npix, 'ngeo': NGEO, 'a': a, 'th_o_deg': th_o * 180 / np.pi, 'orders': list(ORDERS),
+                   'precision': 'fp64', 'case': args.case,
+                   'l2': 'flushed between steps (256 MiB memset); outputs 5 GB per step'},
+        'points_per_s': value * NGEO, 'kernel_ms': {'ray_setup': setup_ms, 'samples': samp_ms,
+                                                    'r_equatorial': eq_ms},
+        'roofline': roof, 'cpu_baseline': cpu, 'e2e': e2e, 'gpu_launches': launches, 'clocks': ck,
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the reference algorithm on the host cores
+# ---------------------------------------------------------------------------
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    pool, cores = make_pool()
+    a, th_o, A, B = cpu_sample(0)
+    for _ in range(args.warmup):
+        cpu_run(pool, cores, 0)
+    tot_n, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        n, dt = cpu_run(pool, cores, 0)
+        tot_n += n
+        tot_t += dt
+    pool.close()
+    value = tot_n / tot_t
+    line = {
+        'impl': 'reference',
+        'metric': 'Kerr rays/s: FP64 raytrace_ana (ngeo=400) + r_equatorial n=0..2, 512x512 image',
+        'value': value, 'unit': 'rays/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': tot_t / max(args.steps, 1) * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic: uniform image-plane grid, seeded a and theta_o',
+        'config': {'workload': 'FP64 drop-in at production size (512x512 over [-10,10] M, a~U[0,0.998), '
+                               'theta_o~U[1,89] deg, r_o=1e4, ngeo=400, r_equatorial n=0,1,2)',
+                   'npix': GRID * GRID, 'ngeo': NGEO, 'precision': 'fp64'},
+        'cpu_baseline': {'value': value, 'unit': 'rays/s', 'cores': cores, 'kind': 'port',
+                         'sample': 'each step: %d rays (every 16th pixel) of the seed-0 draw, ngeo=%d, '
+                                   'r_equatorial n=0..2, oracle/kgeo_oracle.py on %d processes'
+                                   % (A.size, NGEO, cores)},
+        'e2e': {'value': value, 'unit': 'rays/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=5)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', choices=('ours', 'reference'), default='ours')
+    p.add_argument('--case', choices=('full', 'small'), default='full')
+    p.add_argument('--no-cpu-baseline', action='store_true')
+    args = p.parse_args()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == '__main__':
+    main()

@@ -90,6 +90,46 @@ int kgeo_coords_at_tau(const kgeo_observer* obs, const double* alpha, const doub
                        const double* tau, int32_t ntau, int32_t do_phi_and_t, kgeo_geodesics* out,
                        void* workspace, size_t workspace_bytes, void* stream);
 
+/* The two halves of kgeo_raytrace, for callers that sample the same rays repeatedly
+ * (e.g. at new Mino times inside an iterative solver):
+ * kgeo_ray_setup evaluates every per-ray quantity (conserved quantities, turning points,
+ * radial roots and class, Mino totals, antiderivative constants: the per-pixel part of
+ * kgeo/kerr_raytracing_ana.py:76-94 and 151-167 and of kgeo/kerr_raytracing_utils.py:242-548)
+ * into the caller's workspace; per_ray may carry tau_tot / rclass / thclass outputs (the
+ * sample pointers are ignored). ngeo is the linspace length the samples will use (0 if
+ * tau is given later).
+ * kgeo_ray_samples evaluates t, r, theta, phi, sigma (and the Mino times) of those rays:
+ * at tau (nsamp, npix) when tau is non-NULL, else at the ngeo-point linspace of the setup
+ * (the sample loop of kgeo/kerr_raytracing_ana.py:169-188). The workspace must not be
+ * modified between the two calls. */
+int kgeo_ray_setup(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix, int32_t ngeo,
+                   double maxtaufrac, void* workspace, size_t workspace_bytes, kgeo_geodesics* per_ray,
+                   void* stream);
+int kgeo_ray_samples(const kgeo_observer* obs, const void* workspace, size_t workspace_bytes, int64_t npix,
+                     const double* tau, int32_t nsamp, int32_t do_phi_and_t, kgeo_geodesics* out, void* stream);
+
+/* r_equatorial(a, r_o, th_o, mbar, alpha, beta) (kgeo/equatorial_lensing.py:85-196) for the
+ * orders mbar = mbar_lo .. mbar_lo + n_orders - 1 in one pass: r_s and Ir are (n_orders, npix),
+ * Imax and Nmax (npix) are order-independent (either may be NULL). Vortical pixels
+ * (eta <= 0) get r_s = Ir = Imax = -1, Nmax = -2; r_s = 0 where Nmax < mbar. */
+int kgeo_r_equatorial(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha,
+                      const double* beta, int64_t npix, double* r_s, double* Ir, double* Imax, double* Nmax,
+                      void* stream);
+
+/* Per-pixel crossing counts at Mino times tau (ntau, npix):
+ * n_eq  = n_equatorial_crossings (kgeo/kerr_raytracing_utils.py:605-684; Geodesics.nmax_eq),
+ * n_pol = n_poloidal_orbits (kgeo/kerr_raytracing_utils.py:551-603; Geodesics.n_poloidal),
+ * and outside_crit (npix) = is_outside_crit (kgeo/kerr_raytracing_utils.py:794-826).
+ * Any of the three outputs may be NULL; tau is only read when n_eq or n_pol is requested. */
+int kgeo_equatorial_crossings(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                              const double* tau, int32_t ntau, double* n_eq, double* n_pol,
+                              double* outside_crit, void* stream);
+
+/* Measurement helper (no counterpart in the reference): runs a fixed FP64 fused
+ * multiply-add loop on every SM and returns the achieved FP64 rate in TFLOP/s (an FMA
+ * counts as 2 FLOP). Used as the FP64 roofline denominator; blocks until done. */
+int kgeo_measure_fp64_peak(double* tflops, void* stream);
+
 /* Human-readable text of a kgeo_status code (the reference's exception message where one exists). */
 const char* kgeo_status_string(int status);
 

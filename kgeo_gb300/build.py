@@ -24,6 +24,7 @@ UNITS = [
     ('kg_setup.cu', ['-fmad=false']),
     ('kg_samples.cu', []),
     ('kg_abi.cu', []),
+    ('kg_peak.cu', []),
 ]
 
 

@@ -58,6 +58,52 @@ int get_scratch(Scratch& sc, void* workspace, size_t bytes, int64_t npix, cudaSt
   return KGEO_OK;
 }
 
+int setup_common(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix, int64_t ngeo,
+                 double maxtaufrac, const Workspace& w, kgeo_geodesics* out, cudaStream_t s) {
+  if (cudaMemsetAsync(w.flags, 0, sizeof(uint32_t), s) != cudaSuccess) return KGEO_ERR_CUDA;
+  if (npix == 0) return KGEO_OK;
+  SetupArgs sa;
+  sa.obs = make_observer(obs);
+  sa.alpha = alpha;
+  sa.beta = beta;
+  sa.npix = npix;
+  sa.ngeo = ngeo;
+  sa.maxtaufrac = maxtaufrac;
+  sa.rec = w.rec;
+  sa.code = w.code;
+  sa.rclass = out ? out->rclass : nullptr;
+  sa.thclass = out ? out->thclass : nullptr;
+  sa.tau_tot = out ? out->tau_tot : nullptr;
+  sa.flags = w.flags;
+  return launch_ray_setup(sa, s) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
+}
+
+int samples_common(const kgeo_observer* obs, const Workspace& w, int64_t npix, int64_t nsamp, const double* tau,
+                   int do_phi_t, kgeo_geodesics* out, cudaStream_t s) {
+  if (npix > 0) {
+    SampleArgs pa;
+    pa.obs = make_observer(obs);
+    pa.rec = w.rec;
+    pa.code = w.code;
+    pa.npix = npix;
+    pa.nsamp = nsamp;
+    pa.tau = tau;
+    pa.do_phi_t = do_phi_t;
+    pa.flags = w.flags;
+    pa.t = out->t;
+    pa.r = out->r;
+    pa.th = out->th;
+    pa.ph = out->ph;
+    pa.sig = out->sig;
+    pa.mino = out->mino;
+    if (launch_samples(pa, s) != cudaSuccess) return KGEO_ERR_CUDA;
+  }
+  if (out->flags &&
+      cudaMemcpyAsync(out->flags, w.flags, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return KGEO_ERR_CUDA;
+  return KGEO_OK;
+}
+
 int trace_common(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
                  int64_t nsamp, const double* tau, int do_phi_t, double maxtaufrac, kgeo_geodesics* out,
                  void* workspace, size_t workspace_bytes_, void* stream) {
@@ -72,45 +118,9 @@ int trace_common(const kgeo_observer* obs, const double* alpha, const double* be
   st = get_scratch(sc, workspace, workspace_bytes_, npix, s);
   if (st) return st;
   Workspace w = carve_workspace(sc.ptr, npix);
-  if (cudaMemsetAsync(w.flags, 0, sizeof(uint32_t), s) != cudaSuccess) return KGEO_ERR_CUDA;
-  if (npix == 0) {
-    if (out->flags && cudaMemsetAsync(out->flags, 0, sizeof(uint32_t), s) != cudaSuccess) return KGEO_ERR_CUDA;
-    return KGEO_OK;
-  }
-  SetupArgs sa;
-  sa.obs = make_observer(obs);
-  sa.alpha = alpha;
-  sa.beta = beta;
-  sa.npix = npix;
-  sa.ngeo = tau ? 0 : nsamp;
-  sa.maxtaufrac = maxtaufrac;
-  sa.rec = w.rec;
-  sa.code = w.code;
-  sa.rclass = out->rclass;
-  sa.thclass = out->thclass;
-  sa.tau_tot = out->tau_tot;
-  sa.flags = w.flags;
-  if (launch_ray_setup(sa, s) != cudaSuccess) return KGEO_ERR_CUDA;
-  SampleArgs pa;
-  pa.obs = sa.obs;
-  pa.rec = w.rec;
-  pa.code = w.code;
-  pa.npix = npix;
-  pa.nsamp = nsamp;
-  pa.tau = tau;
-  pa.do_phi_t = do_phi_t;
-  pa.flags = w.flags;
-  pa.t = out->t;
-  pa.r = out->r;
-  pa.th = out->th;
-  pa.ph = out->ph;
-  pa.sig = out->sig;
-  pa.mino = out->mino;
-  if (launch_samples(pa, s) != cudaSuccess) return KGEO_ERR_CUDA;
-  if (out->flags &&
-      cudaMemcpyAsync(out->flags, w.flags, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
-    return KGEO_ERR_CUDA;
-  return KGEO_OK;
+  st = setup_common(obs, alpha, beta, npix, tau ? 0 : nsamp, maxtaufrac, w, out, s);
+  if (st) return st;
+  return samples_common(obs, w, npix, nsamp, tau, do_phi_t, out, s);
 }
 
 }  // namespace
@@ -132,6 +142,76 @@ int kgeo_coords_at_tau(const kgeo_observer* obs, const double* alpha, const doub
   if (ntau > 0 && npix > 0 && !tau) return KGEO_ERR_NULL;
   return trace_common(obs, alpha, beta, npix, ntau, tau, do_phi_and_t ? 1 : 0, 1.0, out, workspace,
                       workspace_bytes_, stream);
+}
+
+int kgeo_r_equatorial(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha,
+                      const double* beta, int64_t npix, double* r_s, double* Ir, double* Imax, double* Nmax,
+                      void* stream) {
+  int st = check_observer(obs);
+  if (st) return st;
+  if (mbar_lo < 0 || n_orders < 0) return KGEO_ERR_MBAR;
+  if (npix < 0) return KGEO_ERR_LENGTHS;
+  if (npix > 0 && (!alpha || !beta || (n_orders > 0 && (!r_s || !Ir)))) return KGEO_ERR_NULL;
+  EquatorialArgs ea;
+  ea.obs = make_observer(obs);
+  ea.alpha = alpha;
+  ea.beta = beta;
+  ea.npix = npix;
+  ea.mbar_lo = mbar_lo;
+  ea.nord = n_orders;
+  ea.r_s = r_s;
+  ea.Ir = Ir;
+  ea.Imax = Imax;
+  ea.Nmax = Nmax;
+  return launch_equatorial(ea, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
+}
+
+int kgeo_equatorial_crossings(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                              const double* tau, int32_t ntau, double* n_eq, double* n_pol,
+                              double* outside_crit, void* stream) {
+  if (!obs) return KGEO_ERR_NULL;
+  if (!(std::fabs(obs->a) >= 0 && std::fabs(obs->a) < 1)) return KGEO_ERR_SPIN;
+  if (npix < 0) return KGEO_ERR_LENGTHS;
+  if (ntau < 0) return KGEO_ERR_NGEO;
+  if (npix > 0 && (!alpha || !beta)) return KGEO_ERR_NULL;
+  if (npix > 0 && ntau > 0 && (n_eq || n_pol) && !tau) return KGEO_ERR_NULL;
+  CrossingArgs ca;
+  ca.obs = make_observer(obs);
+  ca.alpha = alpha;
+  ca.beta = beta;
+  ca.npix = npix;
+  ca.tau = tau;
+  ca.ntau = ntau;
+  ca.n_eq = n_eq;
+  ca.n_pol = n_pol;
+  ca.outside = outside_crit;
+  return launch_crossings(ca, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
+}
+
+int kgeo_ray_setup(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix, int32_t ngeo,
+                   double maxtaufrac, void* workspace, size_t workspace_bytes_, kgeo_geodesics* per_ray,
+                   void* stream) {
+  int st = check_observer(obs);
+  if (st) return st;
+  if (npix < 0) return KGEO_ERR_LENGTHS;
+  if (ngeo < 0) return KGEO_ERR_NGEO;
+  if (!workspace) return KGEO_ERR_NULL;
+  if (workspace_bytes_ < workspace_bytes(npix)) return KGEO_ERR_WORKSPACE;
+  if (npix > 0 && (!alpha || !beta)) return KGEO_ERR_NULL;
+  Workspace w = carve_workspace(workspace, npix);
+  return setup_common(obs, alpha, beta, npix, ngeo, maxtaufrac, w, per_ray, static_cast<cudaStream_t>(stream));
+}
+
+int kgeo_ray_samples(const kgeo_observer* obs, const void* workspace, size_t workspace_bytes_, int64_t npix,
+                     const double* tau, int32_t nsamp, int32_t do_phi_and_t, kgeo_geodesics* out, void* stream) {
+  int st = check_observer(obs);
+  if (st) return st;
+  if (npix < 0) return KGEO_ERR_LENGTHS;
+  if (nsamp < 0) return KGEO_ERR_NGEO;
+  if (!workspace || !out) return KGEO_ERR_NULL;
+  if (workspace_bytes_ < workspace_bytes(npix)) return KGEO_ERR_WORKSPACE;
+  Workspace w = carve_workspace(const_cast<void*>(workspace), npix);
+  return samples_common(obs, w, npix, nsamp, tau, do_phi_and_t ? 1 : 0, out, static_cast<cudaStream_t>(stream));
 }
 
 const char* kgeo_status_string(int status) {

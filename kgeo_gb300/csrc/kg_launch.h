@@ -4,7 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
-#include "kg_ray.cuh"
+#include "kg_equatorial.cuh"
 
 namespace kg {
 
@@ -67,7 +67,34 @@ struct SampleArgs {
   double* mino;
 };
 
+struct EquatorialArgs {
+  Observer obs;
+  const double* alpha;
+  const double* beta;
+  int64_t npix;
+  int mbar_lo;
+  int nord;
+  double* r_s;   // (nord, npix)
+  double* Ir;    // (nord, npix)
+  double* Imax;  // (npix)
+  double* Nmax;  // (npix)
+};
+
+struct CrossingArgs {
+  Observer obs;
+  const double* alpha;
+  const double* beta;
+  int64_t npix;
+  const double* tau;  // (ntau, npix)
+  int64_t ntau;
+  double* n_eq;       // (ntau, npix)
+  double* n_pol;      // (ntau, npix)
+  double* outside;    // (npix) is_outside_crit
+};
+
 cudaError_t launch_ray_setup(const SetupArgs& a, cudaStream_t s);
+cudaError_t launch_equatorial(const EquatorialArgs& a, cudaStream_t s);
+cudaError_t launch_crossings(const CrossingArgs& a, cudaStream_t s);
 cudaError_t launch_samples(const SampleArgs& a, cudaStream_t s);
 
 }  // namespace kg

@@ -130,6 +130,49 @@ KG_HD void r1r2_at(double al, double phi, double j, bool want_r2, double* R1, do
 // per-ray setup
 // ---------------------------------------------------------------------------
 
+struct Turning {
+  double up, um;
+};
+
+// u_+, u_- with the reference's clamps (kgeo/kerr_raytracing_utils.py:290-326). Below
+// MINSPIN the reference binds u_- to the same array as u_+, so every clamp lands on both.
+KG_HD Turning u_turning(const Observer& o, double lam, double eta) {
+  double up, um;
+  if (o.minspin) {
+    up = eta / (eta + lam * lam);
+    if ((o.cos2 - up) > 0) up = o.cos2;
+    if (up * up > 1) up = 1;
+    if (up == 0 && eta < 0) up = EP;
+    if (up == 0 && eta >= 0) up = -EP;
+    if (eta < 0 && (o.cos2 - up) < 0) up = o.cos2;
+    um = up;
+  } else {
+    const double a = o.a;
+    double half = 0.5 * (1 - (eta + lam * lam) / (a * a));
+    double root = sqrt(half * half + eta / (a * a));
+    up = half + root;
+    um = half - root;
+    if ((o.cos2 - up) > 0) up = o.cos2;
+    if (up * up > 1) up = 1;
+    if (um == 0 && eta < 0) um = EP;
+    if (um == 0 && eta >= 0) um = -EP;
+    if (eta < 0 && (o.cos2 - um) < 0) um = o.cos2;
+  }
+  return Turning{up, um};
+}
+
+// u_+/u_- and a^2 u_- as uplus_uminus returns them (0 and -(eta + lam^2) below MINSPIN).
+KG_HD void u_ratio(const Observer& o, double lam, double eta, const Turning& U, double* ratio, double* a2um) {
+  if (o.minspin) {
+    *ratio = 0. * U.um;
+    *a2um = -(eta + lam * lam);
+  } else {
+    *ratio = U.up / U.um;
+    *a2um = o.a2 * U.um;
+  }
+}
+
+
 struct Roots {
   cplx r1, r2, r3, r4;
   int rclass;
@@ -168,56 +211,10 @@ KG_HD Roots radial_roots(const Observer& o, double lam, double eta) {
   return R;
 }
 
-// Everything that depends only on the ray. Writes the record, returns the flags it raises.
-// `anyflags` are the launch-wide flags (only FLAG_ANY_ETA_POS is read, and only by
-// eta == 0 rays; pass FLAG_ANY_ETA_POS when unknown and fix up later).
-KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double maxtaufrac,
-                         RayRec* rec, int* rclass_out, int* thclass_out) {
-  unsigned flags = 0;
-  double* f = rec->f;
-  for (int i = 0; i < NUM_FIELDS; ++i) f[i] = 0.0;
-  const double a = o.a, a2 = o.a2;
-
-  // conserved quantities, kgeo/kerr_raytracing_ana.py:151-158
-  double lam = -alpha * o.sin_th;
-  double eta = (alpha * alpha - a2) * o.cos2 + beta * beta;
-  if (o.minspin && eta < 0) eta = EP;
-  if (eta > 0) flags |= FLAG_ANY_ETA_POS;
-  if (eta <= 0) flags |= FLAG_ANY_ETA_NONPOS;
-  if (o.minspin && eta <= 0) flags |= FLAG_MINSPIN_VORTICAL;
-  double s = beta >= 0 ? 1.0 : -1.0;  // my_sign, kgeo/kerr_raytracing_utils.py:857-864
-  f[F_LAM] = lam;
-  f[F_S] = s;
-
-  // u_+, u_- with clamps, kgeo/kerr_raytracing_utils.py:290-326 (aliased below MINSPIN)
-  double up, um;
-  if (o.minspin) {
-    up = eta / (eta + lam * lam);
-    if ((o.cos2 - up) > 0) up = o.cos2;
-    if (up * up > 1) up = 1;
-    if (up == 0 && eta < 0) up = EP;
-    if (up == 0 && eta >= 0) up = -EP;
-    if (eta < 0 && (o.cos2 - up) < 0) up = o.cos2;
-    um = up;
-  } else {
-    double half = 0.5 * (1 - (eta + lam * lam) / (a * a));
-    double root = sqrt(half * half + eta / (a * a));
-    up = half + root;
-    um = half - root;
-    if ((o.cos2 - up) > 0) up = o.cos2;
-    if (up * up > 1) up = 1;
-    if (um == 0 && eta < 0) um = EP;
-    if (um == 0 && eta >= 0) um = -EP;
-    if (eta < 0 && (o.cos2 - um) < 0) um = o.cos2;
-  }
-  *thclass_out = eta > 0 ? 1 : (eta < 0 ? 2 : 3);
-
-  // radial roots and rclass
-  Roots R = radial_roots(o, lam, eta);
-  *rclass_out = R.rclass;
-
-  // ---- total Mino time, kgeo/kerr_raytracing_utils.py:382-548
-  const double rplus = o.rplus, rminus = o.rminus, r_o = o.r_o;
+// Total Mino time from the observer to the horizon or back out to infinity
+// (kgeo/kerr_raytracing_utils.py:382-548, regions IV, III, II, I).
+KG_HD double mino_total(const Observer& o, const Roots& R) {
+  const double rplus = o.rplus, r_o = o.r_o;
   double tau_tot = 0.0;
   bool m4 = R.r1.im != 0;
   bool m3 = (R.r3.im != 0) && !m4;
@@ -268,6 +265,42 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
       tau_tot = 2 * I2ro;
     }
   }
+  return tau_tot;
+}
+
+// Everything that depends only on the ray. Writes the record, returns the flags it raises.
+// `anyflags` are the launch-wide flags (only FLAG_ANY_ETA_POS is read, and only by
+// eta == 0 rays; pass FLAG_ANY_ETA_POS when unknown and fix up later).
+KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double maxtaufrac,
+                         RayRec* rec, int* rclass_out, int* thclass_out) {
+  unsigned flags = 0;
+  double* f = rec->f;
+  for (int i = 0; i < NUM_FIELDS; ++i) f[i] = 0.0;
+  const double a = o.a, a2 = o.a2;
+
+  // conserved quantities, kgeo/kerr_raytracing_ana.py:151-158
+  double lam = -alpha * o.sin_th;
+  double eta = (alpha * alpha - a2) * o.cos2 + beta * beta;
+  if (o.minspin && eta < 0) eta = EP;
+  if (eta > 0) flags |= FLAG_ANY_ETA_POS;
+  if (eta <= 0) flags |= FLAG_ANY_ETA_NONPOS;
+  if (o.minspin && eta <= 0) flags |= FLAG_MINSPIN_VORTICAL;
+  double s = beta >= 0 ? 1.0 : -1.0;  // my_sign, kgeo/kerr_raytracing_utils.py:857-864
+  f[F_LAM] = lam;
+  f[F_S] = s;
+
+  // u_+, u_- with clamps, kgeo/kerr_raytracing_utils.py:290-326
+  Turning U = u_turning(o, lam, eta);
+  const double up = U.up, um = U.um;
+  *thclass_out = eta > 0 ? 1 : (eta < 0 ? 2 : 3);
+
+  // radial roots and rclass
+  Roots R = radial_roots(o, lam, eta);
+  *rclass_out = R.rclass;
+
+  // ---- total Mino time, kgeo/kerr_raytracing_utils.py:382-548
+  const double rplus = o.rplus, rminus = o.rminus, r_o = o.r_o;
+  double tau_tot = mino_total(o, R);
   f[F_TAUTOT] = tau_tot;
   double taumax = maxtaufrac * tau_tot;
   f[F_TAUMAX] = taumax;

@@ -86,3 +86,68 @@ def trace(a, r_o, th_o, alpha, beta, ngeo=None, tau=None, maxtaufrac=1.0 - 1.0e-
                                       ctypes.c_void_p(s.cuda_stream))
     _lib.check(code)
     return res
+
+
+class PreparedRays:
+    """Rays set up once on the device (kgeo_ray_setup), sampled any number of times (kgeo_ray_samples)."""
+
+    def __init__(self, a, r_o, th_o, alpha, beta, ngeo=0, maxtaufrac=1.0 - 1.0e-10, stream=None):
+        require_cuda()
+        self.lib = _lib.load()
+        self.dev = alpha.device
+        self.npix = alpha.numel()
+        self.ngeo = int(ngeo)
+        self.obs = _lib.Observer(float(a), float(r_o), float(th_o))
+        self.ws_bytes = int(self.lib.kgeo_workspace_size(self.npix))
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=self.dev)
+        self.alpha, self.beta, self.maxtaufrac = alpha, beta, float(maxtaufrac)
+        self.tau_tot = torch.empty(self.npix, dtype=torch.float64, device=self.dev)
+        self.rclass = torch.empty(self.npix, dtype=torch.int32, device=self.dev)
+        self.thclass = torch.empty(self.npix, dtype=torch.int32, device=self.dev)
+        self.setup(stream)
+
+    def _stream(self, stream):
+        return ctypes.c_void_p((stream if stream is not None else torch.cuda.current_stream(self.dev)).cuda_stream)
+
+    def setup(self, stream=None):
+        per = _lib.GeodesicsOut(None, None, None, None, None, None, _ptr(self.tau_tot), _ptr(self.rclass),
+                                _ptr(self.thclass), None)
+        _lib.check(self.lib.kgeo_ray_setup(ctypes.byref(self.obs), _ptr(self.alpha), _ptr(self.beta), self.npix,
+                                           self.ngeo, self.maxtaufrac, _ptr(self.ws), self.ws_bytes,
+                                           ctypes.byref(per), self._stream(stream)))
+
+    def alloc(self, nsamp=None, keys=('t', 'r', 'th', 'ph', 'sig', 'mino')):
+        n = self.ngeo if nsamp is None else nsamp
+        return {k: torch.empty((n, self.npix), dtype=torch.float64, device=self.dev) for k in keys}
+
+    def samples(self, out, tau=None, do_phi_and_t=True, flags=None, stream=None):
+        nsamp = tau.shape[0] if tau is not None else self.ngeo
+        g = _lib.GeodesicsOut(*[_ptr(out.get(k)) for k in ('t', 'r', 'th', 'ph', 'sig', 'mino')],
+                              None, None, None, _ptr(flags))
+        _lib.check(self.lib.kgeo_ray_samples(ctypes.byref(self.obs), _ptr(self.ws), self.ws_bytes, self.npix,
+                                             _ptr(tau), nsamp, 1 if do_phi_and_t else 0, ctypes.byref(g),
+                                             self._stream(stream)))
+        return out
+
+
+def fp64_peak_tflops():
+    """Measured FP64 FMA throughput of this GPU (TFLOP/s), from the library's probe kernel."""
+    require_cuda()
+    v = ctypes.c_double(0.0)
+    _lib.check(_lib.load().kgeo_measure_fp64_peak(ctypes.byref(v), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return v.value
+
+
+def to_host(tensors):
+    """Copy CUDA tensors to numpy through pinned staging buffers (one synchronisation).
+
+    The returned arrays are views of pinned host tensors (kept alive by the arrays),
+    so the device-to-host copies run at the link's full rate.
+    """
+    outs = []
+    for t in tensors:
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t, non_blocking=True)
+        outs.append(h)
+    torch.cuda.current_stream().synchronize()
+    return [h.numpy() for h in outs]

@@ -56,10 +56,6 @@ def _flags_check(a, flags):
         print("WARNING: there were eta<0 points for spin %f<MINSPIN!" % a)
 
 
-def _host(x, device_arrays):
-    return x if device_arrays else x.cpu().numpy()
-
-
 def raytrace_ana(a=SPIN, observer_coords=[0, ROUT, INC, 0], image_coords=[alpha_default, beta_default],
                  ngeo=NGEO, maxtaufrac=MAXTAUFRAC, do_phi_and_t=True, savedata=False, plotdata=True,
                  device_arrays=False):
@@ -76,9 +72,9 @@ def raytrace_ana(a=SPIN, observer_coords=[0, ROUT, INC, 0], image_coords=[alpha_
     be = _dev.as_device(beta)
     res = _dev.trace(a, r_o, th_o, al, be, ngeo=ngeo, maxtaufrac=maxtaufrac)
     _flags_check(a, res['flags'])
-    geo = [_host(res[k], device_arrays) for k in ('t', 'r', 'th', 'ph')]
-    return Geodesics(a, observer_coords, image_coords, _host(res['mino'], device_arrays),
-                     _host(res['sig'], device_arrays), geo)
+    keys = ('mino', 'sig', 't', 'r', 'th', 'ph')
+    vals = [res[k] for k in keys] if device_arrays else _dev.to_host([res[k] for k in keys])
+    return Geodesics(a, observer_coords, image_coords, vals[0], vals[1], list(vals[2:]))
 
 
 def coords_at_tau(a, observer_coords, image_coords, tau, do_phi_and_t=True, device_arrays=False):
@@ -97,4 +93,6 @@ def coords_at_tau(a, observer_coords, image_coords, tau, do_phi_and_t=True, devi
     res = _dev.trace(a, r_o, th_o, _dev.as_device(alpha), _dev.as_device(beta), tau=_dev.as_device(tau),
                      do_phi_and_t=do_phi_and_t, outputs=('t', 'r', 'th', 'ph', 'sig'), per_ray=())
     _flags_check(a, res['flags'])
-    return _host(res['sig'], device_arrays), [_host(res[k], device_arrays) for k in ('t', 'r', 'th', 'ph')]
+    keys = ('sig', 't', 'r', 'th', 'ph')
+    vals = [res[k] for k in keys] if device_arrays else _dev.to_host([res[k] for k in keys])
+    return vals[0], list(vals[1:])

@@ -1,6 +1,6 @@
 // Host (g++) build of the device arithmetic headers, for CPU unit checks of the
 // same code the CUDA kernels compile. Test-only: never loaded by the product.
-#include "../../kgeo_gb300/csrc/kg_ray.cuh"
+#include "../../kgeo_gb300/csrc/kg_equatorial.cuh"
 
 using namespace kg;
 
@@ -51,6 +51,30 @@ void hm_samples(const double* ob, const double* rec, const int* code, long n, co
     for (long g = 0; g < ntau; ++g) {
       Sample S = sample_all(o, f, code[i], tau[g * n + i], ordinary_active != 0);
       t[g * n + i] = S.t; r[g * n + i] = S.r; th[g * n + i] = S.th; ph[g * n + i] = S.ph; sig[g * n + i] = S.sig;
+    }
+  }
+}
+void hm_requatorial(const double* ob, const double* alpha, const double* beta, long n, int mbar_lo, int nord,
+                    double* r_s, double* Ir, double* Imax, double* Nmax) {
+  Observer o = make_obs(ob);
+  for (long i = 0; i < n; ++i) {
+    EqResult r = r_equatorial_px(o, alpha[i], beta[i], mbar_lo, nord, r_s + i, Ir + i, n);
+    Imax[i] = r.Imax;
+    Nmax[i] = r.Nmax;
+  }
+}
+void hm_crossings(const double* ob, const double* alpha, const double* beta, long n, const double* tau, long ntau,
+                  double* n_eq, double* n_pol, double* outside) {
+  Observer o = make_obs(ob);
+  for (long i = 0; i < n; ++i) {
+    double lam = -alpha[i] * o.sin_th;
+    double eta = (alpha[i] * alpha[i] - o.a2) * o.cos2 + beta[i] * beta[i];
+    outside[i] = outside_crit(o, lam, eta);
+    EqConsts c = eq_consts(o, lam, eta);
+    double Kc = c.vort ? 0.0 : ellip_k(c.ratio);
+    for (long g = 0; g < ntau; ++g) {
+      n_eq[g * n + i] = n_eq_at(o, c, beta[i], tau[g * n + i]);
+      n_pol[g * n + i] = n_pol_at(c, Kc, tau[g * n + i]);
     }
   }
 }

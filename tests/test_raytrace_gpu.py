@@ -39,12 +39,15 @@ def test_trace_vs_reference_fixture(kg, golden, name):
     ref = dict(t=g['t'], r=g['r'], th=g['th'], ph=g['ph'], sig=g['sig'])
     if not np.isfinite(r_o):
         # r_o = inf: the reference's t and sigma are inf - inf garbage, and r at tau = 0 divides
-        # by a rounding-level denominator; parity is checked on r, theta, phi from sample 1 on
+        # by a rounding-level denominator; parity is checked on r, theta, phi from sample 1 on.
+        # The last sample of every ray is 1e-10 tau_tot from the horizon or from r = infinity
+        # (r ~ 1/(tau_tot - tau)), condition number ~1e10: held to 1e-4 there.
         for k in ('r', 'th', 'ph'):
-            x, y = got[k][1:], ref[k][1:]
-            assert np.array_equal(np.isfinite(x), np.isfinite(y))
-            fin = np.isfinite(y)
-            assert np.all(np.abs(x[fin] - y[fin]) <= 1e-9 * np.maximum(np.abs(y[fin]), 1.0))
+            for sl, tol in ((slice(1, -1), 1e-9), (slice(-1, None), 1e-4)):
+                x, y = got[k][sl], ref[k][sl]
+                assert np.array_equal(np.isfinite(x), np.isfinite(y))
+                fin = np.isfinite(y)
+                assert np.all(np.abs(x[fin] - y[fin]) <= tol * np.maximum(np.abs(y[fin]), 1.0))
         return
     check_trace(got, ref, r_o, g['rclass'], name)
 
@@ -142,3 +145,51 @@ def test_empty_and_single_sample(kg):
     ref = ko.raytrace(0.5, 1e4, 0.3, A, B, 1)
     assert g.mino_times.shape == (1, 2) and np.array_equal(g.mino_times, ref['mino_times'])
     assert np.allclose(g.geo_coords[1], ref['r'], rtol=1e-12)
+
+
+@pytest.mark.parametrize('idx', [0, 1, 2])
+def test_r_equatorial_vs_reference_fixture(kg, golden, idx):
+    from kgeo_gb300 import equatorial_lensing as el
+    g = golden('requatorial_%d' % idx)
+    a, r_o, th_o = float(g['a']), float(g['r_o']), float(g['th_o'])
+    for m in range(3):
+        r_s, Ir, Imax, Nmax = el.r_equatorial(a, r_o, th_o, m, g['alpha'], g['beta'])
+        assert np.array_equal(Nmax, g['Nmax%d' % m])
+        assert np.array_equal(r_s == 0, g['r_s%d' % m] == 0) and np.array_equal(r_s < 0, g['r_s%d' % m] < 0)
+        np.testing.assert_allclose(r_s, g['r_s%d' % m], rtol=1e-10, atol=0)
+        np.testing.assert_allclose(Ir, g['Ir%d' % m], rtol=1e-10, atol=1e-12)
+        np.testing.assert_allclose(Imax, g['Imax%d' % m], rtol=1e-10, atol=1e-12)
+    assert np.array_equal(el.is_outside_crit(a, th_o, g['alpha'], g['beta']), g['outside_crit'])
+
+
+def test_crossing_counts_bit_exact(kg, golden):
+    from oracle import kgeo_oracle as ko
+    for name in TRACES:
+        g = golden(name)
+        a, r_o, th_o = float(g['a']), float(g['r_o']), float(g['th_o'])
+        got = kg.raytrace_ana(a=a, observer_coords=[0, r_o, th_o, 0], image_coords=[g['alpha'], g['beta']],
+                              ngeo=int(g['ngeo']), plotdata=False)
+        assert np.array_equal(got.nmax_eq, g['nmax_eq']), name
+        npol = ko.n_poloidal_orbits(a, th_o, g['alpha'], g['beta'], g['mino'])
+        np.testing.assert_allclose(got.n_poloidal, npol, rtol=1e-10, atol=1e-12)
+
+
+def test_r_equatorial_config2_grid_vs_oracle(kg):
+    """Full 512x512 grid of configuration 2 (seeded a, theta_o), orders 0..2, against the oracle."""
+    from oracle import kgeo_oracle as ko
+    from kgeo_gb300 import equatorial_lensing as el
+    from kgeo_gb300 import device as dev
+    rng = np.random.default_rng(0)
+    a = float(rng.uniform(0, 0.998))
+    th_o = float(rng.uniform(1, 89)) * np.pi / 180
+    x = np.linspace(-10, 10, 512)
+    A, B = np.meshgrid(x, x)
+    A, B = A.flatten(), B.flatten()
+    r_s, Ir, Imax, Nmax = (t.cpu().numpy() for t in el.r_equatorial_device(a, 1.e4, th_o, [0, 1, 2],
+                                                                           dev.as_device(A), dev.as_device(B)))
+    for m in range(3):
+        rr, ir, imax, nmax = ko.r_equatorial(a, 1.e4, th_o, m, A, B)
+        assert np.array_equal(Nmax, nmax)
+        assert np.array_equal(r_s[m] == 0, rr == 0)
+        np.testing.assert_allclose(r_s[m], rr, rtol=1e-10, atol=0)
+        np.testing.assert_allclose(Ir[m], ir, rtol=1e-10, atol=1e-12)
