@@ -40,7 +40,9 @@ CPU_SAMPLE_RAYS = 16384      # rays of the bounded CPU sample (every 16th pixel 
 # FP64 floating-point work of the sample kernel per geodesic point on this workload, from the
 # ncu capture summarised in profiles/geo_samples_fp64_config2.md:
 # (dadd + dmul + 2 dfma thread instructions) / points. Used for roofline.achieved.
-FP64_FLOP_PER_POINT = None
+FP64_FLOP_PER_POINT = 5556
+# DRAM bytes per point of the same capture (dram__bytes_read + dram__bytes_write) / points
+DRAM_BYTES_PER_POINT = 51.5
 BYTES_PER_POINT = 48          # t, r, theta, phi, sigma, Mino tau written per point (8 B each)
 L2_FLUSH_BYTES = 256 << 20
 
@@ -258,7 +260,8 @@ def run_ours(args):
     roof = {'bound': 'fp64', 'unit': 'TFLOP/s', 'peak': fp64_peak,
             'peak_source': 'FP64 FMA loop measured live by bench.py (kgeo_measure_fp64_peak)',
             'kernel': 'samples_kernel', 'launch_ms': samp_ms, 'points_per_launch': points,
-            'traffic': None}
+            'traffic': DRAM_BYTES_PER_POINT * points,
+            'traffic_source': 'ncu dram__bytes_read+write of a 128x128 capture, scaled by points'}
     if FP64_FLOP_PER_POINT:
         ach = FP64_FLOP_PER_POINT * points / (samp_ms * 1e-3) / 1e12
         roof.update({'achieved': ach, 'frac': ach / fp64_peak, 'fp64_flop_per_point': FP64_FLOP_PER_POINT})
