@@ -37,7 +37,8 @@ typedef enum {
   KGEO_ERR_WORKSPACE = 7,   /* workspace too small */
   KGEO_ERR_NULL = 8,        /* a required pointer is NULL */
   KGEO_ERR_CUDA = 9,        /* a CUDA runtime call failed */
-  KGEO_ERR_MODEL = 10       /* unknown / out-of-range emissivity or velocity model parameter */
+  KGEO_ERR_MODEL = 10,      /* unknown / out-of-range emissivity or velocity model parameter */
+  KGEO_ERR_NOALLOC_SIZE = 11 /* npix above KGEO_NOALLOC_MAX_PIXELS for kgeo_raytrace_noalloc */
 } kgeo_status;
 
 /* Bits of the device flags word written by the tracing entry points. */
@@ -124,6 +125,23 @@ int kgeo_r_equatorial(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_order
 int kgeo_equatorial_crossings(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
                               const double* tau, int32_t ntau, double* n_eq, double* n_pol,
                               double* outside_crit, void* stream);
+
+/* Allocation-free kgeo_raytrace. No counterpart in the reference: it exists for callers
+ * that may not allocate device memory when they call in — an application that owns all
+ * device memory under a fixed budget, a latency-critical loop that cannot afford an
+ * allocator call, or a host that offers no allocator. Same arguments, outputs and status
+ * codes as kgeo_raytrace minus the workspace: the per-ray scratch lives in a fixed array
+ * inside the library (room for KGEO_NOALLOC_MAX_PIXELS rays, about 7.4 MB of device memory
+ * that every GPU loading the library keeps until the process exits). Larger npix is
+ * refused with KGEO_ERR_NOALLOC_SIZE before any work. The call allocates and frees nothing.
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * once for that device; make that first call before any stream capture. Every call on a
+ * device shares the one array and it keeps the last call's contents, so calls whose work
+ * overlaps on the GPU (different streams, or different host threads) race: order them on one
+ * stream or serialise them. */
+#define KGEO_NOALLOC_MAX_PIXELS 16384
+int kgeo_raytrace_noalloc(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                          int32_t ngeo, double maxtaufrac, kgeo_geodesics* out, void* stream);
 
 /* Measurement helper (no counterpart in the reference): runs a fixed FP64 fused
  * multiply-add loop on every SM and returns the achieved FP64 rate in TFLOP/s (an FMA

@@ -25,6 +25,7 @@ UNITS = [
     ('kg_samples.cu', []),
     ('kg_abi.cu', []),
     ('kg_peak.cu', []),
+    ('kg_noalloc.cu', []),
 ]
 
 

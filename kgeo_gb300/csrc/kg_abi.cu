@@ -227,6 +227,7 @@ const char* kgeo_status_string(int status) {
     case KGEO_ERR_NULL: return "a required pointer is NULL";
     case KGEO_ERR_CUDA: return "CUDA runtime error";
     case KGEO_ERR_MODEL: return "emissivity / velocity model parameter out of range";
+    case KGEO_ERR_NOALLOC_SIZE: return "npix exceeds KGEO_NOALLOC_MAX_PIXELS (kgeo_raytrace_noalloc)";
     default: return "unknown status";
   }
 }
