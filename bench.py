@@ -37,12 +37,13 @@ NGEO = 400
 ORDERS = (0, 1, 2)
 R_O = 1.0e4
 CPU_SAMPLE_RAYS = 16384      # rays of the bounded CPU sample (every 16th pixel of the grid)
-# FP64 floating-point work of the sample kernel per geodesic point on this workload, from the
-# ncu capture summarised in profiles/geo_samples_fp64_config2.md:
-# (dadd + dmul + 2 dfma thread instructions) / points. Used for roofline.achieved.
-FP64_FLOP_PER_POINT = 5556
+# FP64 floating-point work of the sample kernel (addition-theorem recurrence, chunks of 50)
+# per geodesic point on this workload, from the ncu capture summarised in
+# profiles/geo_samples_fp64_config2.md: (dadd + dmul + 2 dfma thread instructions) / points.
+# Used for roofline.achieved.
+FP64_FLOP_PER_POINT = 1190
 # DRAM bytes per point of the same capture (dram__bytes_read + dram__bytes_write) / points
-DRAM_BYTES_PER_POINT = 51.5
+DRAM_BYTES_PER_POINT = 54.6
 BYTES_PER_POINT = 48          # t, r, theta, phi, sigma, Mino tau written per point (8 B each)
 L2_FLUSH_BYTES = 256 << 20
 
@@ -233,7 +234,7 @@ def run_ours(args):
     rays = npix * args.steps * world
     value = rays / elapsed
     points = npix * NGEO
-    launches = 3 * args.steps
+    launches = 5 * args.steps  # setup + bucket scan + bucket scatter, samples, r_equatorial
 
     # end to end through the public API with host buffers: numpy in, numpy out
     e2e = None
@@ -259,7 +260,7 @@ def run_ours(args):
     fp64_peak = dev.fp64_peak_tflops()
     roof = {'bound': 'fp64', 'unit': 'TFLOP/s', 'peak': fp64_peak,
             'peak_source': 'FP64 FMA loop measured live by bench.py (kgeo_measure_fp64_peak)',
-            'kernel': 'samples_kernel', 'launch_ms': samp_ms, 'points_per_launch': points,
+            'kernel': 'stepped_kernel', 'launch_ms': samp_ms, 'points_per_launch': points,
             'traffic': DRAM_BYTES_PER_POINT * points,
             'traffic_source': 'ncu dram__bytes_read+write of a 128x128 capture, scaled by points'}
     if FP64_FLOP_PER_POINT:

@@ -102,12 +102,17 @@ int kgeo_coords_at_tau(const kgeo_observer* obs, const double* alpha, const doub
  * kgeo_ray_samples evaluates t, r, theta, phi, sigma (and the Mino times) of those rays:
  * at tau (nsamp, npix) when tau is non-NULL, else at the ngeo-point linspace of the setup
  * (the sample loop of kgeo/kerr_raytracing_ana.py:169-188). The workspace must not be
- * modified between the two calls. */
+ * modified between the two calls. chunk selects the evaluation of the even grid: 0 evaluates
+ * every sample independently (Landen + Carlson per sample); k > 0 gives each thread k
+ * consecutive samples, the first (and the grid's last) evaluated directly and the rest by
+ * the addition theorems of sn/cn/dn, E and Pi from the previous sample (k is capped at 64);
+ * < 0 picks the library default. Caller-given tau always uses independent evaluation. */
 int kgeo_ray_setup(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix, int32_t ngeo,
                    double maxtaufrac, void* workspace, size_t workspace_bytes, kgeo_geodesics* per_ray,
                    void* stream);
 int kgeo_ray_samples(const kgeo_observer* obs, const void* workspace, size_t workspace_bytes, int64_t npix,
-                     const double* tau, int32_t nsamp, int32_t do_phi_and_t, kgeo_geodesics* out, void* stream);
+                     const double* tau, int32_t nsamp, int32_t do_phi_and_t, int32_t chunk, kgeo_geodesics* out,
+                     void* stream);
 
 /* r_equatorial(a, r_o, th_o, mbar, alpha, beta) (kgeo/equatorial_lensing.py:85-196) for the
  * orders mbar = mbar_lo .. mbar_lo + n_orders - 1 in one pass: r_s and Ir are (n_orders, npix),
@@ -131,7 +136,7 @@ int kgeo_equatorial_crossings(const kgeo_observer* obs, const double* alpha, con
  * device memory under a fixed budget, a latency-critical loop that cannot afford an
  * allocator call, or a host that offers no allocator. Same arguments, outputs and status
  * codes as kgeo_raytrace minus the workspace: the per-ray scratch lives in a fixed array
- * inside the library (room for KGEO_NOALLOC_MAX_PIXELS rays, about 7.4 MB of device memory
+ * inside the library (room for KGEO_NOALLOC_MAX_PIXELS rays, about 9.2 MB of device memory
  * that every GPU loading the library keeps until the process exits). Larger npix is
  * refused with KGEO_ERR_NOALLOC_SIZE before any work. The call allocates and frees nothing.
  * The first call on a device looks up the array's device address (cudaGetSymbolAddress)

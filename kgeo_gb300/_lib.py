@@ -36,7 +36,7 @@ SIGNATURES = {
     'kgeo_ray_setup': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_int32, c_double, c_void_p,
                                c_size_t, ctypes.POINTER(GeodesicsOut), c_void_p]),
     'kgeo_ray_samples': (c_int, [ctypes.POINTER(Observer), c_void_p, c_size_t, c_int64, c_void_p, c_int32, c_int32,
-                                 ctypes.POINTER(GeodesicsOut), c_void_p]),
+                                 c_int32, ctypes.POINTER(GeodesicsOut), c_void_p]),
     'kgeo_raytrace_noalloc': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_int32, c_double,
                                       ctypes.POINTER(GeodesicsOut), c_void_p]),
     'kgeo_measure_fp64_peak': (c_int, [ctypes.POINTER(c_double), c_void_p]),

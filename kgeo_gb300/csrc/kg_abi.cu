@@ -60,7 +60,8 @@ int get_scratch(Scratch& sc, void* workspace, size_t bytes, int64_t npix, cudaSt
 
 int setup_common(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix, int64_t ngeo,
                  double maxtaufrac, const Workspace& w, kgeo_geodesics* out, cudaStream_t s) {
-  if (cudaMemsetAsync(w.flags, 0, sizeof(uint32_t), s) != cudaSuccess) return KGEO_ERR_CUDA;
+  // counters and flags are adjacent: one memset clears both
+  if (cudaMemsetAsync(w.counts, 0, sizeof(uint32_t) * (2 * NBUCKET + 1), s) != cudaSuccess) return KGEO_ERR_CUDA;
   if (npix == 0) return KGEO_OK;
   SetupArgs sa;
   sa.obs = make_observer(obs);
@@ -75,11 +76,13 @@ int setup_common(const kgeo_observer* obs, const double* alpha, const double* be
   sa.thclass = out ? out->thclass : nullptr;
   sa.tau_tot = out ? out->tau_tot : nullptr;
   sa.flags = w.flags;
+  sa.counts = w.counts;
+  sa.perm = w.perm;
   return launch_ray_setup(sa, s) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
 }
 
 int samples_common(const kgeo_observer* obs, const Workspace& w, int64_t npix, int64_t nsamp, const double* tau,
-                   int do_phi_t, kgeo_geodesics* out, cudaStream_t s) {
+                   int do_phi_t, int chunk, kgeo_geodesics* out, cudaStream_t s) {
   if (npix > 0) {
     SampleArgs pa;
     pa.obs = make_observer(obs);
@@ -89,6 +92,8 @@ int samples_common(const kgeo_observer* obs, const Workspace& w, int64_t npix, i
     pa.nsamp = nsamp;
     pa.tau = tau;
     pa.do_phi_t = do_phi_t;
+    pa.chunk = chunk < 0 ? DEFAULT_CHUNK : (chunk > MAX_CHUNK ? MAX_CHUNK : chunk);
+    pa.perm = w.perm;
     pa.flags = w.flags;
     pa.t = out->t;
     pa.r = out->r;
@@ -120,7 +125,7 @@ int trace_common(const kgeo_observer* obs, const double* alpha, const double* be
   Workspace w = carve_workspace(sc.ptr, npix);
   st = setup_common(obs, alpha, beta, npix, tau ? 0 : nsamp, maxtaufrac, w, out, s);
   if (st) return st;
-  return samples_common(obs, w, npix, nsamp, tau, do_phi_t, out, s);
+  return samples_common(obs, w, npix, nsamp, tau, do_phi_t, -1, out, s);
 }
 
 }  // namespace
@@ -203,7 +208,8 @@ int kgeo_ray_setup(const kgeo_observer* obs, const double* alpha, const double* 
 }
 
 int kgeo_ray_samples(const kgeo_observer* obs, const void* workspace, size_t workspace_bytes_, int64_t npix,
-                     const double* tau, int32_t nsamp, int32_t do_phi_and_t, kgeo_geodesics* out, void* stream) {
+                     const double* tau, int32_t nsamp, int32_t do_phi_and_t, int32_t chunk, kgeo_geodesics* out,
+                     void* stream) {
   int st = check_observer(obs);
   if (st) return st;
   if (npix < 0) return KGEO_ERR_LENGTHS;
@@ -211,7 +217,7 @@ int kgeo_ray_samples(const kgeo_observer* obs, const void* workspace, size_t wor
   if (!workspace || !out) return KGEO_ERR_NULL;
   if (workspace_bytes_ < workspace_bytes(npix)) return KGEO_ERR_WORKSPACE;
   Workspace w = carve_workspace(const_cast<void*>(workspace), npix);
-  return samples_common(obs, w, npix, nsamp, tau, do_phi_and_t ? 1 : 0, out, static_cast<cudaStream_t>(stream));
+  return samples_common(obs, w, npix, nsamp, tau, do_phi_and_t ? 1 : 0, chunk, out, static_cast<cudaStream_t>(stream));
 }
 
 const char* kgeo_status_string(int status) {

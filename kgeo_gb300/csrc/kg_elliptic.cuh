@@ -108,7 +108,17 @@ KG_HD void rj_multi(double x, double y, double z, const double* p_in, double* rj
       double sp = sqrt(p[i]);
       double d = (sp + sx) * (sp + sy) * (sp + sz);
       double e = f3 * delta[i] / (d * d);
-      sum[i] += f / d * rc_one(e);
+      double term;
+      if (fabs(e) < 2.0e-3) {
+        term = rc_one(e) / d;  // R_C(1, 1 + e_m) / d_m, series
+      } else {
+        // the same term as R_C(alpha_m, beta_m) / 2 (Carlson's earlier form), which keeps
+        // full precision when 1 + e_m is small (p much smaller than x, y, z)
+        double al = p[i] * (sx + sy + sz) + sx * sy * sz;
+        double pl = p[i] + lam;
+        term = 0.5 * carlson_rc(al * al, p[i] * pl * pl);
+      }
+      sum[i] += f * term;
       p[i] = 0.25 * (p[i] + lam);
       A[i] = 0.25 * (A[i] + lam);
     }

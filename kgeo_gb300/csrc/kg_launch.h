@@ -9,19 +9,26 @@
 namespace kg {
 
 // Device scratch layout for npix pixels: the per-ray record (NUM_FIELDS doubles per ray,
-// structure of arrays), the per-ray code word, and one flags word.
+// structure of arrays), the per-ray code word, the class-sorted ray permutation, the
+// class-bucket counters and cursors, and one flags word.
+constexpr int NBUCKET = 32;
+
+KG_HD constexpr size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+KG_HD constexpr size_t workspace_bytes_n(size_t n) {
+  return align_up(sizeof(double) * NUM_FIELDS * n, 256) + 2 * align_up(sizeof(int) * n, 256) +
+         align_up(sizeof(uint32_t) * (2 * NBUCKET + 1), 256);
+}
+
+inline size_t workspace_bytes(int64_t npix) { return workspace_bytes_n((size_t)(npix > 0 ? npix : 1)); }
+
 struct Workspace {
   double* rec;
   int* code;
-  uint32_t* flags;
+  int* perm;          // rays ordered by class bucket
+  uint32_t* counts;   // NBUCKET ray counts, then NBUCKET cursors
+  uint32_t* flags;    // launch flags (follows the counters: one memset clears both)
 };
-
-KG_HD size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
-
-inline size_t workspace_bytes(int64_t npix) {
-  size_t n = (size_t)(npix > 0 ? npix : 1);
-  return align_up(sizeof(double) * NUM_FIELDS * n, 256) + align_up(sizeof(int) * n, 256) + 256;
-}
 
 inline Workspace carve_workspace(void* base, int64_t npix) {
   size_t n = (size_t)(npix > 0 ? npix : 1);
@@ -31,9 +38,15 @@ inline Workspace carve_workspace(void* base, int64_t npix) {
   p += align_up(sizeof(double) * NUM_FIELDS * n, 256);
   w.code = reinterpret_cast<int*>(p);
   p += align_up(sizeof(int) * n, 256);
-  w.flags = reinterpret_cast<uint32_t*>(p);
+  w.perm = reinterpret_cast<int*>(p);
+  p += align_up(sizeof(int) * n, 256);
+  w.counts = reinterpret_cast<uint32_t*>(p);
+  w.flags = w.counts + 2 * NBUCKET;
   return w;
 }
+
+// Class bucket of a ray: radial case, theta branch, recurrence flag.
+KG_HD int ray_bucket(int code) { return code_rcase(code) * 6 + code_th(code) * 2 + (code_step(code) ? 1 : 0); }
 
 struct SetupArgs {
   Observer obs;
@@ -48,6 +61,8 @@ struct SetupArgs {
   int32_t* thclass;
   double* tau_tot;
   uint32_t* flags;      // launch flags (workspace)
+  uint32_t* counts;     // class-bucket counters (workspace)
+  int* perm;            // class-sorted permutation (workspace)
 };
 
 struct SampleArgs {
@@ -58,6 +73,8 @@ struct SampleArgs {
   int64_t nsamp;
   const double* tau;    // (nsamp, npix) or NULL for the linspace grid
   int do_phi_t;
+  int chunk;            // > 0: even grid by the addition-theorem recurrence, chunk samples per thread
+  const int* perm;      // class-sorted rays for the recurrence kernel
   const uint32_t* flags;
   double* t;
   double* r;
@@ -91,6 +108,11 @@ struct CrossingArgs {
   double* n_pol;      // (ntau, npix)
   double* outside;    // (npix) is_outside_crit
 };
+
+// Default and largest samples per thread of the stepped kernel (longer recurrence chains
+// accumulate more rounding: 64 keeps every output within the FP64 parity bars).
+constexpr int DEFAULT_CHUNK = 50;
+constexpr int MAX_CHUNK = 64;
 
 cudaError_t launch_ray_setup(const SetupArgs& a, cudaStream_t s);
 cudaError_t launch_equatorial(const EquatorialArgs& a, cudaStream_t s);

@@ -8,7 +8,7 @@
 // allocator. kgeo_raytrace needs per-ray scratch (the ray records the sample kernel reads)
 // and either takes it from the caller or allocates it; this entry point does neither.
 //
-// The cost: the array below (KGEO_NOALLOC_MAX_PIXELS rays' records, about 7.4 MB) is part of
+// The cost: the array below (KGEO_NOALLOC_MAX_PIXELS rays' records and sort keys, about 9.2 MB) is part of
 // the library's device image, so every GPU that loads the library holds it until the
 // process exits, whether or not this entry point is called.
 #include <cstring>
@@ -23,10 +23,8 @@ namespace {
 
 constexpr int64_t kMaxPixels = KGEO_NOALLOC_MAX_PIXELS;
 
-// Scratch for kMaxPixels rays laid out exactly as kg::carve_workspace expects.
-constexpr size_t kRecBytes = (sizeof(double) * NUM_FIELDS * kMaxPixels + 255) / 256 * 256;
-constexpr size_t kCodeBytes = (sizeof(int) * kMaxPixels + 255) / 256 * 256;
-constexpr size_t kScratchBytes = kRecBytes + kCodeBytes + 256;
+// Scratch for kMaxPixels rays, sized by the same rule as kgeo_workspace_size.
+constexpr size_t kScratchBytes = workspace_bytes_n((size_t)kMaxPixels);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 

@@ -58,8 +58,14 @@ enum RecField : int {
   // radial, case-specific
   R_C0, R_C1, R_C2, R_C3, R_C4, R_C5, R_C6, R_C7, R_C8, R_C9, R_C10, R_C11, R_C12, R_C13,
   R_C14, R_C15, R_C16, R_C17, R_C18, R_C19,
+  // one step of the even Mino grid: theta Jacobi values / integrals at the step, r ditto
+  S_TSN, S_TCN, S_TDN, S_TE, S_TPI, S_TC,
+  S_RSN, S_RCN, S_RDN, S_RE, S_RP0, S_RP1, S_RP2, S_RC0, S_RC1, S_RC2,
   NUM_FIELDS
 };
+
+// code bit: the ray's samples may be produced by the addition-theorem recurrence
+constexpr int CODE_STEP = 1 << 10;
 
 // Strided view of one ray's record inside the structure-of-arrays buffer.
 struct RecView {
@@ -83,6 +89,7 @@ KG_HD int code_rcase(int code) { return code & 15; }
 KG_HD int code_th(int code) { return (code >> 4) & 15; }
 KG_HD bool code_kk0(int code) { return (code >> 8) & 1; }
 KG_HD bool code_minspin(int code) { return (code >> 9) & 1; }
+KG_HD bool code_step(int code) { return (code >> 10) & 1; }
 
 // ---------------------------------------------------------------------------
 // building blocks at a generic amplitude (ray constants)
@@ -547,6 +554,19 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
 
 // ---------------------------------------------------------------------------
 // per-sample evaluation
+//
+// A sample is evaluated in two stages: the elliptic state of the ray at that Mino time
+// (Jacobi sn, cn, dn of the theta and r arguments and the running values of E, E - F and
+// every Pi), then the assembly of r, theta, G_phi, G_t, I_phi, I_t, I_sigma from that state
+// (GL19a B46-B116 and 29-68, as kgeo/kerr_raytracing_ana.py:216-633 combines them).
+// The state comes either from a direct evaluation (Landen + Carlson, any tau) or from the
+// previous sample of an evenly spaced Mino grid by the addition theorems of sn, cn, dn
+// (DLMF 22.8.1-3), of E (DLMF 22.16.27 / 19.11.2) and of Pi:
+//   Pi(n; am(u+v)) = Pi(n; am u) + Pi(n; am v) + n S3 sgn(X) R_C(X^2, X^2 - n (m - n)(1 - n) S3^2),
+//   S3 = sn u sn v sn(u+v),  X = 1 - n sn^2(u+v) + n sn u sn v cn(u+v) dn(u+v),
+// which follows from Jacobi's addition theorem for the third kind after eliminating the
+// characteristic's parameter (n = m sn^2 a). For small steps the R_C ratio is tiny and
+// R_C is a short series.
 // ---------------------------------------------------------------------------
 
 struct Sample {
@@ -565,9 +585,9 @@ KG_HD double pi_assemble(double n, double Phi, double nr, double inc, double pic
   return nr == 0.0 ? inc : 2.0 * nr * pic + inc;
 }
 
-// One Carlson evaluation at (x, y, z) = (cn^2, dn^2-ish ...) for up to three Pi's plus
-// R_D; p[i] = the (scaled) rho_i. For rho_i <= 0 the DLMF 19.20.14 transform is used,
-// rho == 0 gives +inf like the reference.
+// One Carlson evaluation at (x, y, z) for up to three Pi's plus R_D; rho[i] = the (scaled)
+// 1 - n_i sin^2. For rho_i < 0 the DLMF 19.20.14 transform is used; rho == 0 gives +inf
+// like the reference.
 template <int NP>
 KG_HD void carlson_set(double x, double y, double z, const double* rho, double* rj, double* rd, double* rf) {
   double p[NP + 1];
@@ -599,83 +619,240 @@ KG_HD void carlson_set(double x, double y, double z, const double* rho, double* 
   }
 }
 
+// ---- addition theorems -----------------------------------------------------
+
+struct JacobiW {
+  double sn, cn, dn;
+};
+
+// sn, cn, dn(u + v | m) from the values at u and v (DLMF 22.8.1-3), any real m.
+KG_HD JacobiW jacobi_add(double snu, double cnu, double dnu, double snv, double cnv, double dnv, double m) {
+  double inv = 1.0 / (1.0 - m * (snu * snu) * (snv * snv));
+  JacobiW w;
+  w.sn = (snu * cnv * dnv + snv * cnu * dnu) * inv;
+  w.cn = (cnu * cnv - snu * snv * dnu * dnv) * inv;
+  w.dn = (dnu * dnv - m * snu * snv * cnu * cnv) * inv;
+  return w;
+}
+
+// Distance rho = 1 - n sn^2 to a pole (n > 1) or near-pole (n slightly below 1, at a
+// turning point close to the polar axis) of a Pi integrand below which a sample is not
+// produced by the recurrence: there the recurrence state's rounding is amplified by 1/rho,
+// so that sample and the one after it are evaluated directly and the recurrence is
+// re-seeded from them.
+constexpr double POLE_RHO = 2.0e-2;
+
+KG_HD bool near_pi_pole(double n, double sn) { return n > 0.0 && fabs(1.0 - n * (sn * sn)) < POLE_RHO; }
+
+// Pi(n; am(u+v)) - Pi(n; am u) - Pi(n; am v) for parameter m, c = n (m - n)(1 - n):
+//   n S3 sgn(X) R_C(X^2, X^2 - c S3^2)
+// written in branch-continuous form: (n / sqrt(-c)) atan2(sqrt(-c) S3, X) for c < 0 and
+// (n / 2 sqrt(c)) ln|(X + sqrt(c) S3) / (X - sqrt(c) S3)| for c > 0 (the principal value when
+// the step crosses a pole of the integrand, as the reference's Pi takes it there); the
+// R_C series when the ratio c S3^2 / X^2 is small.
+KG_HD double pi_add_term(double n, double c, double snu, double snv, const JacobiW& w) {
+  double S3 = snu * snv * w.sn;
+  double X = 1.0 - n * (w.sn * w.sn) + n * snu * snv * w.cn * w.dn;
+  double iX = 1.0 / X;
+  double t = S3 * iX;
+  double z2 = c * (t * t);
+  if (X > 0.0 && fabs(z2) < 2.0e-3) return n * t * rc_one(-z2);
+  if (c > 0.0) {
+    double sc = sqrt(c);
+    double q = sc * S3;
+    return n / (2.0 * sc) * log(fabs((X + q) / (X - q)));
+  }
+  if (c < 0.0) {
+    double sc = sqrt(-c);
+    return n / sc * atan2(sc * S3, X);
+  }
+  return n * S3 / X;
+}
+
+// ---- theta -----------------------------------------------------------------
+
+struct ThetaState {
+  double sn, cn, dn;  // Jacobi functions of snarg for the (negative) parameter kk
+  double e;           // (E - F)(Phi | kk) for ordinary motion, E(Phi | kk) for vortical
+  double pi;          // Pi(n; Phi | kk)
+  double Phi;         // amplitude (direct evaluations only)
+};
+
 struct ThetaOut {
   double th, Gph, Gt;
 };
 
+// Direct evaluation at snarg (kgeo/kerr_raytracing_ana.py:254-277, 330-352): the amplitude
+// Phi = am(snarg | kk) via the m = kk / (kk - 1) transform, the half period reduced.
 template <class FV>
-KG_HD ThetaOut sample_theta(const FV& f, int code, double tau, bool ordinary_active) {
-  ThetaOut out{0.0, 0.0, 0.0};
-  int th = code_th(code);
-  if (th == TH_ZERO) return out;
-  if (th == TH_ORD && !ordinary_active) return out;
-  const double s = f[F_S];
-  double snarg = f[T_SCALE] * (-tau + s * f[T_GTH]);
-  const double m = f[T_M], s1m = f[T_S1M];
+KG_HD ThetaState theta_state_direct(const FV& f, int code, double snarg) {
+  const double m = f[T_M], s1m = f[T_S1M], n = f[T_N], kk = f[T_KK];
   double x = snarg / s1m;
   double v;
   double nr = reduce_half_period(x, f[T_K2], &v);
   Jacobi J = jacobi_landen(v, m);
   double odd = fmod(fabs(nr), 2.0) == 1.0 ? -1.0 : 1.0;
-  double ys = s1m * J.sn;               // sin(phi0) * dn
-  double phi0 = atan2(ys, J.cn);
-  double Phi = nr * PI + phi0;
-  double sinphi0 = ys / J.dn;
-  double sinPhi = odd * sinphi0;
-  // Carlson at (cn^2, 1, dn^2) scaled by dn^2, see header comment
-  const double n = f[T_N], kk = f[T_KK];
+  double ys = s1m * J.sn;  // sin(phi0) * dn(v | m)
+  ThetaState st;
+  st.Phi = nr * PI + atan2(ys, J.cn);
+  double idn = 1.0 / J.dn;
+  st.sn = odd * ys * idn;
+  st.cn = odd * J.cn * idn;
+  st.dn = idn;
+  // Carlson at (cos^2 phi0, 1 - kk sin^2 phi0, 1) scaled by dn^2: (cn^2, 1, dn^2)
   double xc = J.cn * J.cn, zc = J.dn * J.dn;
   double rho = zc - n * (ys * ys);
   double rj, rd, rf;
   carlson_set<1>(xc, 1.0, zc, &rho, &rj, &rd, &rf);
   double ys3 = ys * ys * ys;
-  double pi0 = ys * rf + (n / 3.0) * ys3 * rj;
-  double Pi = pi_assemble(n, Phi, nr, pi0, f[T_PIC], kk);
-  out.Gph = f[T_PREF] * Pi - s * f[T_GPH];
-  if (th == TH_ORD) {
+  st.pi = pi_assemble(n, st.Phi, nr, ys * rf + (n / 3.0) * ys3 * rj, f[T_PIC], kk);
+  if (code_th(code) == TH_ORD) {
+    double emf = -(kk / 3.0) * ys3 * rd;  // (E - F)(phi0 | kk)
+    if (nr != 0.0) emf += 2.0 * nr * (f[T_EC] - f[T_KC]);
+    st.e = emf;
+  } else {
+    double E = ys * rf - (kk / 3.0) * ys3 * rd;
+    if (nr != 0.0) E += 2.0 * nr * f[T_EC];
+    st.e = E;
+  }
+  return st;
+}
+
+template <class FV>
+KG_HD double theta_snarg(const FV& f, double tau) {
+  return f[T_SCALE] * (-tau + f[F_S] * f[T_GTH]);
+}
+
+// theta, G_phi, G_t from the state (kgeo/kerr_raytracing_ana.py:280-296, 355-363).
+template <class FV>
+KG_HD ThetaOut theta_assemble(const FV& f, int code, const ThetaState& st) {
+  ThetaOut out;
+  const double s = f[F_S];
+  out.Gph = f[T_PREF] * st.pi - s * f[T_GPH];
+  if (code_th(code) == TH_ORD) {
     const double up = f[T_UP];
-    out.th = acos(-s * sqrt(up) * sinPhi);
+    out.th = acos(-s * sqrt(up) * st.sn);
     double gt;
-    if (code_kk0(code)) {
-      gt = -2 * up * f[T_PREF] * 0.125 * (-2 * Phi + sin(2 * Phi));
-    } else {
-      // (E - F)(Phi | kk) = 2 nr (E(kk) - K(kk)) - (kk/3) sin^3(phi0) R_D
-      double emf = -(kk / 3.0) * ys3 * rd;
-      if (nr != 0.0) emf += 2.0 * nr * (f[T_EC] - f[T_KC]);
-      gt = -(2 * up * f[T_PREF] * emf) / (2 * kk);
-    }
+    if (code_kk0(code)) gt = -2 * up * f[T_PREF] * 0.125 * (-2 * st.Phi + sin(2 * st.Phi));
+    else gt = -(2 * up * f[T_PREF] * st.e) / (2 * f[T_KK]);
     out.Gt = gt - s * f[T_GT];
   } else {
     const double up = f[T_UP], um = f[T_UM];
-    out.th = acos(f[T_H] * sqrt(um + (up - um) * (sinPhi * sinPhi)));
-    double E = ys * rf - (kk / 3.0) * ys3 * rd;
-    if (nr != 0.0) E += 2.0 * nr * f[T_EC];
-    out.Gt = f[T_PREFC] * E - s * f[T_GT];
+    out.th = acos(f[T_H] * sqrt(um + (up - um) * (st.sn * st.sn)));
+    out.Gt = f[T_PREFC] * st.e - s * f[T_GT];
   }
   return out;
 }
+
+// One step snarg -> snarg - dth (the next sample of the even Mino grid).
+// Returns false (state untouched) when the step passes too close to a pole of Pi.
+template <class FV>
+KG_HD bool theta_step(const FV& f, ThetaState* st) {
+  const double kk = f[T_KK], n = f[T_N];
+  const double snv = -f[S_TSN], cnv = f[S_TCN], dnv = f[S_TDN];
+  JacobiW w = jacobi_add(st->sn, st->cn, st->dn, snv, cnv, dnv, kk);
+  double S3 = st->sn * snv * w.sn;
+  if (near_pi_pole(n, st->sn) || near_pi_pole(n, w.sn)) return false;
+  double pi = st->pi - f[S_TPI] + pi_add_term(n, f[S_TC], st->sn, snv, w);
+  st->e = st->e - f[S_TE] - kk * S3;
+  st->pi = pi;
+  st->sn = w.sn;
+  st->cn = w.cn;
+  st->dn = w.dn;
+  return true;
+}
+
+// ---- r ---------------------------------------------------------------------
+
+struct RadialState {
+  double X;           // Jacobi argument (F(am X | k) = X)
+  double sn, cn, dn;  // of X
+  double E;           // E(am X | k)
+  double P[3];        // Pi(n_i; am X | k)
+  double am;          // amplitude (direct evaluations only)
+};
 
 struct RadialOut {
   double r, Ip, Im, I1, I2;
 };
 
 template <class FV>
-KG_HD RadialOut sample_radial(const FV& f, int code, double tau, bool want_phi_t) {
-  RadialOut o{0.0, 0.0, 0.0, 0.0, 0.0};
-  int rc = code_rcase(code);
-  if (rc == RCASE_NONE) return o;
-  double X = f[R_XS] * (-tau + f[R_IRO]);
+KG_HD double radial_X(const FV& f, double tau) {
+  return f[R_XS] * (-tau + f[R_IRO]);
+}
+
+// Direct evaluation at X (kgeo/kerr_raytracing_ana.py:434-440, 510-515, 584-591 and the
+// elliptic integrals of S1_S2 / R1_R2 / case 2 at am X).
+template <class FV>
+KG_HD RadialState radial_state_direct(const FV& f, int code, double X, bool want_integrals) {
+  RadialState st;
+  st.X = X;
   double v;
   double nr = reduce_half_period(X, f[R_K2], &v);
   const double k = f[R_M];
   Jacobi J = jacobi_landen(v, k);
   double odd = fmod(fabs(nr), 2.0) == 1.0 ? -1.0 : 1.0;
-  double snX = odd * J.sn, cnX = odd * J.cn, dnX = J.dn;
-  double amX = nr * PI + atan2(J.sn, J.cn);
+  st.sn = odd * J.sn;
+  st.cn = odd * J.cn;
+  st.dn = J.dn;
+  st.am = nr * PI + atan2(J.sn, J.cn);
+  st.E = 0.0;
+  st.P[0] = st.P[1] = st.P[2] = 0.0;
+  if (!want_integrals) return st;
+  double s2r = J.sn * J.sn;
+  double rho[3] = {1.0 - f[R_N0] * s2r, 1.0 - f[R_N1] * s2r, 1.0 - f[R_N2] * s2r};
+  double rj[3], rd, rf;
+  carlson_set<3>(J.cn * J.cn, J.dn * J.dn, 1.0, rho, rj, &rd, &rf);
   double sn3 = J.sn * J.sn * J.sn;
+  double Finc = J.sn * rf;
+  double Einc = Finc - (k / 3.0) * sn3 * rd;
+  st.E = nr == 0.0 ? Einc : Einc + 2.0 * nr * f[R_EC];
+  const double nn[3] = {f[R_N0], f[R_N1], f[R_N2]};
+  const double pic[3] = {f[R_PIC0], f[R_PIC1], f[R_PIC2]};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) st.P[i] = pi_assemble(nn[i], st.am, nr, Finc + (nn[i] / 3.0) * sn3 * rj[i], pic[i], k);
+  return st;
+}
+
+// One step X -> X - dX. Returns false (state untouched) when the step passes too close to a
+// pole of one of the Pi's.
+template <class FV>
+KG_HD bool radial_step(const FV& f, RadialState* st, double Xnew) {
+  const double k = f[R_M];
+  const double snv = -f[S_RSN], cnv = f[S_RCN], dnv = f[S_RDN];
+  JacobiW w = jacobi_add(st->sn, st->cn, st->dn, snv, cnv, dnv, k);
+  double S3 = st->sn * snv * w.sn;
+  const double n0 = f[R_N0], n1 = f[R_N1], n2 = f[R_N2];
+  // reject when the previous sample or this one is next to a pole of a Pi integrand
+  if (near_pi_pole(n0, st->sn) || near_pi_pole(n1, st->sn) || near_pi_pole(n2, st->sn) ||
+      near_pi_pole(n0, w.sn) || near_pi_pole(n1, w.sn) || near_pi_pole(n2, w.sn))
+    return false;
+  double p0 = st->P[0] - f[S_RP0] + pi_add_term(n0, f[S_RC0], st->sn, snv, w);
+  double p1 = st->P[1] - f[S_RP1] + pi_add_term(n1, f[S_RC1], st->sn, snv, w);
+  double p2 = st->P[2] - f[S_RP2] + pi_add_term(n2, f[S_RC2], st->sn, snv, w);
+  st->E = st->E - f[S_RE] - k * S3;
+  st->P[0] = p0;
+  st->P[1] = p1;
+  st->P[2] = p2;
+  st->sn = w.sn;
+  st->cn = w.cn;
+  st->dn = w.dn;
+  st->X = Xnew;
+  return true;
+}
+
+// r, I_+, I_-, I_1, I_2 from the state (kgeo/kerr_raytracing_ana.py:441-471, 516-552, 592-624).
+template <class FV>
+KG_HD RadialOut radial_assemble(const FV& f, int code, double tau, const RadialState& st, bool want_phi_t) {
+  RadialOut o{0.0, 0.0, 0.0, 0.0, 0.0};
+  const int rc = code_rcase(code);
+  const double k = f[R_M];
+  const double snX = st.sn, cnX = st.cn, dnX = st.dn;
   if (rc == RCASE_2) {
     const double rr1 = f[R_C0], rr2 = f[R_C1], rr3 = f[R_C2], rr4 = f[R_C3];
     const double rr31 = f[R_C16], rr41 = f[R_C17], rr43 = f[R_C18];
+    (void)rr1;
+    (void)rr2;
     double sn2 = snX * snX;
     double rs = (rr4 * rr31 - rr3 * rr41 * sn2) / (rr31 - rr41 * sn2);
     o.r = rs;
@@ -685,23 +862,10 @@ KG_HD RadialOut sample_radial(const FV& f, int code, double tau, bool want_phi_t
     double den = rr31 - rr41 * sn2;
     double drs = -(rr31 * rr43 * rr41 * dsn2 / (den * den));
     double H = drs / (rs - rr3) - f[R_C8];
-    double rho[3];
-    double s2r = J.sn * J.sn;
-    rho[0] = 1.0 - f[R_N0] * s2r;
-    rho[1] = 1.0 - f[R_N1] * s2r;
-    rho[2] = 1.0 - f[R_N2] * s2r;
-    double rj[3], rd, rf;
-    carlson_set<3>(J.cn * J.cn, J.dn * J.dn, 1.0, rho, rj, &rd, &rf);
-    double Finc = J.sn * rf;
-    double Einc = Finc - (k / 3.0) * sn3 * rd;
-    double E = nr == 0.0 ? Einc : Einc + 2.0 * nr * f[R_EC];
-    double Eterm = f[R_C12] * (E - f[R_C4]);
-    double P1 = pi_assemble(f[R_N0], amX, nr, Finc + (f[R_N0] / 3.0) * sn3 * rj[0], f[R_PIC0], k);
-    double Pp = pi_assemble(f[R_N1], amX, nr, Finc + (f[R_N1] / 3.0) * sn3 * rj[1], f[R_PIC1], k);
-    double Pm = pi_assemble(f[R_N2], amX, nr, Finc + (f[R_N2] / 3.0) * sn3 * rj[2], f[R_PIC2], k);
-    double Pi_1 = f[R_C9] * (P1 - f[R_C5]);
-    double Pi_p = f[R_C10] * (Pp - f[R_C6]);
-    double Pi_m = f[R_C11] * (Pm - f[R_C7]);
+    double Eterm = f[R_C12] * (st.E - f[R_C4]);
+    double Pi_1 = f[R_C9] * (st.P[0] - f[R_C5]);
+    double Pi_p = f[R_C10] * (st.P[1] - f[R_C6]);
+    double Pi_m = f[R_C11] * (st.P[2] - f[R_C7]);
     o.I1 = rr3 * (-tau) + rr43 * Pi_1;
     o.I2 = H - f[R_C15] * (-tau) - Eterm;
     o.Ip = tau / f[R_C13] - Pi_p;
@@ -713,34 +877,22 @@ KG_HD RadialOut sample_radial(const FV& f, int code, double tau, bool want_phi_t
     o.r = ((BB * rr2 - AA * rr1) + (BB * rr2 + AA * rr1) * cnX) / ((BB - AA) + (BB + AA) * cnX);
     if (!want_phi_t) return o;
     const double al[3] = {f[R_C4], f[R_C5], f[R_C6]};
-    double s2r = J.sn * J.sn;
-    double rho[3];
-    rho[0] = 1.0 - f[R_N0] * s2r;
-    rho[1] = 1.0 - f[R_N1] * s2r;
-    rho[2] = 1.0 - f[R_N2] * s2r;
-    double rj[3], rd, rf;
-    carlson_set<3>(J.cn * J.cn, J.dn * J.dn, 1.0, rho, rj, &rd, &rf);
-    double Finc = J.sn * rf;
-    double F = nr == 0.0 ? Finc : Finc + 2.0 * nr * f[R_KC];
-    double Einc = Finc - (k / 3.0) * sn3 * rd;
-    double E = nr == 0.0 ? Einc : Einc + 2.0 * nr * f[R_EC];
     const double nn[3] = {f[R_N0], f[R_N1], f[R_N2]};
-    const double pic[3] = {f[R_PIC0], f[R_PIC1], f[R_PIC2]};
     double R1[3];
-    const bool use_m = !code_minspin(code);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       double a_ = al[i];
       double al2 = a_ * a_;
       double p1 = (i == 0) ? f[R_C18] : (i == 1 ? f[R_C19] : sqrt((al2 - 1) / (k + (1 - k) * al2)));
       double f1 = 0.5 * p1 * log(fabs((p1 * dnX + snX) / (p1 * dnX - snX)));
-      double P = pi_assemble(nn[i], amX, nr, Finc + (nn[i] / 3.0) * sn3 * rj[i], pic[i], k);
-      R1[i] = (P - a_ * f1) / (1 - al2);
+      R1[i] = (st.P[i] - a_ * f1) / (1 - al2);
+      (void)nn;
     }
     double al2 = al[0] * al[0];
     double jd = k + (1 - k) * al2;
-    double R2 = (F - (al2 / jd) * (E - al[0] * snX * dnX / (1 + al[0] * cnX))) / (al2 - 1);
+    double R2 = (st.X - (al2 / jd) * (st.E - al[0] * snX * dnX / (1 + al[0] * cnX))) / (al2 - 1);
     R2 = R2 + (2 * k - nn[0]) * R1[0] / jd;
+    const bool use_m = !code_minspin(code);
     double R1m = use_m ? R1[2] : 0.0;
     double R1bm = use_m ? f[R_C10] : 0.0;
     double c0 = f[R_C11];
@@ -755,26 +907,12 @@ KG_HD RadialOut sample_radial(const FV& f, int code, double tau, bool want_phi_t
     o.Im = -((BB + AA) * (-tau) + Pi_m) / f[R_C17];
     return o;
   }
-  // RCASE_4
-  {
+  if (rc == RCASE_4) {
     const double a2i = f[R_C0], b1 = f[R_C1], g0 = f[R_C2];
     double sc = snX / cnX;
     o.r = -a2i * (g0 - sc) / (1 + g0 * sc) - b1;
     if (!want_phi_t) return o;
-    double s2r = J.sn * J.sn;
-    double rho[3];
-    rho[0] = 1.0 - f[R_N0] * s2r;
-    rho[1] = 1.0 - f[R_N1] * s2r;
-    rho[2] = 1.0 - f[R_N2] * s2r;
-    double rj[3], rd, rf;
-    carlson_set<3>(J.cn * J.cn, J.dn * J.dn, 1.0, rho, rj, &rd, &rf);
-    double Finc = J.sn * rf;
-    double F = nr == 0.0 ? Finc : Finc + 2.0 * nr * f[R_KC];
-    double Einc = Finc - (k / 3.0) * sn3 * rd;
-    double E = nr == 0.0 ? Einc : Einc + 2.0 * nr * f[R_EC];
     const double gs[3] = {g0, f[R_C3], f[R_C4]};
-    const double nn[3] = {f[R_N0], f[R_N1], f[R_N2]};
-    const double pic[3] = {f[R_PIC0], f[R_PIC1], f[R_PIC2]};
     double S1[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -784,11 +922,10 @@ KG_HD RadialOut sample_radial(const FV& f, int code, double tau, bool want_phi_t
       double al2j = 1 - k + al2;
       double p2 = sqrt(al2p1 / al2j);
       double f2 = 0.5 * p2 * log(fabs(((1 - p2) * (1 + p2 * dnX)) / ((1 + p2) * (1 - p2 * dnX))));
-      double P = pi_assemble(nn[i], amX, nr, Finc + (nn[i] / 3.0) * sn3 * rj[i], pic[i], k);
-      S1[i] = (F + al2 * P - al * f2) / al2p1;
+      S1[i] = (st.X + al2 * st.P[i] - al * f2) / al2p1;
     }
     double al2 = g0 * g0, al2p1 = 1 + al2, al2j = 1 - k + al2;
-    double S2a = (1 - k) * F + al2 * E + al2 * dnX * (g0 - sc) / (1 + g0 * sc) - al2 * g0;
+    double S2a = (1 - k) * st.X + al2 * st.E + al2 * dnX * (g0 - sc) / (1 + g0 * sc) - al2 * g0;
     S2a = -S2a / (al2p1 * al2j);
     double S2b = S1[0] * (1. / al2p1 + (1 - k) / al2j);
     double S2 = S2a + S2b;
@@ -803,6 +940,47 @@ KG_HD RadialOut sample_radial(const FV& f, int code, double tau, bool want_phi_t
     o.Im = f[R_C15] * (-tau - Pi_m);
     return o;
   }
+  return o;
+}
+
+// ---- combination -------------------------------------------------------------
+
+// t, phi, sigma from the theta and r parts (kgeo/kerr_raytracing_ana.py:186-188, 626-633).
+template <class FV>
+KG_HD Sample combine(const Observer& ob, const FV& f, double tau, const ThetaOut& T, const RadialOut& R) {
+  const double a = ob.a, rp = ob.rplus, rm = ob.rminus, lam = f[F_LAM];
+  double I_0 = -tau;
+  double I_phi = (2 * a / (rp - rm)) * ((rp - 0.5 * a * lam) * R.Ip - (rm - 0.5 * a * lam) * R.Im);
+  double I_tA = (4 / (rp - rm)) * ((rp * rp - 0.5 * a * lam * rp) * R.Ip - (rm * rm - 0.5 * a * lam * rm) * R.Im);
+  double I_t = I_tA + 4 * I_0 + 2 * R.I1 + R.I2;
+  Sample S;
+  S.sig = 0 + R.I2 + ob.a2 * T.Gt;
+  S.t = 0 + I_t + ob.a2 * T.Gt;
+  S.ph = 0 + I_phi + lam * T.Gph;
+  S.r = R.r;
+  S.th = T.th;
+  return S;
+}
+
+template <class FV>
+KG_HD bool theta_active(const FV& f, int code, bool ordinary_active) {
+  int th = code_th(code);
+  return th == TH_VORT || (th == TH_ORD && ordinary_active);
+}
+
+// Direct evaluation of the theta part at tau (zeros where the reference leaves them zero).
+template <class FV>
+KG_HD ThetaOut sample_theta(const FV& f, int code, double tau, bool ordinary_active) {
+  if (!theta_active(f, code, ordinary_active)) return ThetaOut{0.0, 0.0, 0.0};
+  ThetaState st = theta_state_direct(f, code, theta_snarg(f, tau));
+  return theta_assemble(f, code, st);
+}
+
+template <class FV>
+KG_HD RadialOut sample_radial(const FV& f, int code, double tau, bool want_phi_t) {
+  if (code_rcase(code) == RCASE_NONE) return RadialOut{0.0, 0.0, 0.0, 0.0, 0.0};
+  RadialState st = radial_state_direct(f, code, radial_X(f, tau), want_phi_t);
+  return radial_assemble(f, code, tau, st, want_phi_t);
 }
 
 // Element g of numpy.linspace(0, stop, G) for an array stop (numpy's arithmetic:
@@ -816,23 +994,80 @@ KG_HD double linspace_at(int64_t g, int64_t G, double stop, bool any_step_zero) 
   return (double)g * (stop / div) + 0.0;
 }
 
-// All five coordinates at Mino time tau (kgeo/kerr_raytracing_ana.py:186-188, 626-633).
+// All five coordinates at Mino time tau by direct evaluation.
 template <class FV>
 KG_HD Sample sample_all(const Observer& ob, const FV& f, int code, double tau, bool ordinary_active) {
   ThetaOut T = sample_theta(f, code, tau, ordinary_active);
   RadialOut R = sample_radial(f, code, tau, true);
-  const double a = ob.a, rp = ob.rplus, rm = ob.rminus, lam = f[F_LAM];
-  double I_0 = -tau;
-  double I_phi = (2 * a / (rp - rm)) * ((rp - 0.5 * a * lam) * R.Ip - (rm - 0.5 * a * lam) * R.Im);
-  double I_tA = (4 / (rp - rm)) * ((rp * rp - 0.5 * a * lam * rp) * R.Ip - (rm * rm - 0.5 * a * lam * rm) * R.Im);
-  double I_t = I_tA + 4 * I_0 + 2 * R.I1 + R.I2;
-  Sample S;
-  S.sig = 0 + R.I2 + ob.a2 * T.Gt;
-  S.t = 0 + I_t + ob.a2 * T.Gt;
-  S.ph = 0 + I_phi + lam * T.Gph;
-  S.r = R.r;
-  S.th = T.th;
-  return S;
+  return combine(ob, f, tau, T, R);
+}
+
+// Samples g0 .. g1-1 of one ray on the even Mino grid (G samples, last one = taumax):
+// a direct evaluation at g0 and at the final sample, the addition-theorem recurrence in
+// between (direct everywhere for rays without CODE_STEP). emit(g, tau, Sample) stores.
+template <class FV, class Emit>
+KG_HD void ray_chunk(const Observer& ob, const FV& f, int code, int64_t g0, int64_t g1, int64_t G,
+                     bool ordinary_active, bool step_zero, Emit emit) {
+  const double taumax = f[F_TAUMAX];
+  const bool thact = theta_active(f, code, ordinary_active);
+  const bool stepping = code_step(code);
+  const bool rdo = code_rcase(code) != RCASE_NONE;
+  ThetaState ts;
+  RadialState rs;
+  ts.sn = ts.cn = ts.dn = ts.e = ts.pi = ts.Phi = 0.0;
+  rs.X = rs.sn = rs.cn = rs.dn = rs.E = rs.am = 0.0;
+  rs.P[0] = rs.P[1] = rs.P[2] = 0.0;
+  for (int64_t g = g0; g < g1; ++g) {
+    const double tau = linspace_at(g, G, taumax, step_zero);
+    const double X = radial_X(f, tau);
+    if (g == g0 || g == G - 1 || !stepping) {
+      if (thact) ts = theta_state_direct(f, code, theta_snarg(f, tau));
+      if (rdo) rs = radial_state_direct(f, code, X, true);
+    } else {
+      if (thact && !theta_step(f, &ts)) ts = theta_state_direct(f, code, theta_snarg(f, tau));
+      if (rdo && !radial_step(f, &rs, X)) rs = radial_state_direct(f, code, X, true);
+    }
+    ThetaOut T = thact ? theta_assemble(f, code, ts) : ThetaOut{0.0, 0.0, 0.0};
+    RadialOut R = rdo ? radial_assemble(f, code, tau, rs, true) : RadialOut{0.0, 0.0, 0.0, 0.0, 0.0};
+    emit(g, tau, combine(ob, f, tau, T, R));
+  }
+}
+
+// Per-ray constants of one step of the even Mino grid (Mino step dtau): the Jacobi
+// functions and the integrals at the step itself. Sets CODE_STEP when the ray can be
+// stepped (finite constants, no n = 1 theta characteristic, not the a < MINSPIN limit).
+template <class FV>
+KG_HD int step_constants(FV f, int code, double dtau, double* out /* f itself, writable */) {
+  bool ok = dtau > 0 && std::isfinite(dtau) && code_rcase(code) != RCASE_NONE && code_th(code) != TH_ZERO &&
+            !code_kk0(code) && f[T_KK] >= M_NEG_INF;
+  if (ok) {
+    double dth = f[T_SCALE] * dtau;
+    ThetaState ts = theta_state_direct(f, code, dth);
+    out[S_TSN] = ts.sn;
+    out[S_TCN] = ts.cn;
+    out[S_TDN] = ts.dn;
+    out[S_TE] = ts.e;
+    out[S_TPI] = ts.pi;
+    const double n = f[T_N], kk = f[T_KK];
+    out[S_TC] = n * (kk - n) * (1 - n);
+    double dX = f[R_XS] * dtau;
+    RadialState rs = radial_state_direct(f, code, dX, true);
+    out[S_RSN] = rs.sn;
+    out[S_RCN] = rs.cn;
+    out[S_RDN] = rs.dn;
+    out[S_RE] = rs.E;
+    out[S_RP0] = rs.P[0];
+    out[S_RP1] = rs.P[1];
+    out[S_RP2] = rs.P[2];
+    const double k = f[R_M];
+    const double nn[3] = {f[R_N0], f[R_N1], f[R_N2]};
+    out[S_RC0] = nn[0] * (k - nn[0]) * (1 - nn[0]);
+    out[S_RC1] = nn[1] * (k - nn[1]) * (1 - nn[1]);
+    out[S_RC2] = nn[2] * (k - nn[2]) * (1 - nn[2]);
+    ok = n != 1.0 && std::isfinite(f[T_PIC]);
+    for (int i = S_TSN; i <= S_RC2; ++i) ok = ok && std::isfinite(out[i]);
+  }
+  return ok ? (code | CODE_STEP) : (code & ~CODE_STEP);
 }
 
 }  // namespace kg

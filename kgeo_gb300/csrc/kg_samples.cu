@@ -39,12 +39,55 @@ __global__ void __launch_bounds__(256) samples_kernel(SampleArgs a) {
   }
 }
 
+// Even Mino grid: one thread per (pixel, chunk of `chunk` consecutive samples), items
+// chunk-major over the class-sorted pixels. Each thread evaluates its first sample (and the
+// grid's last) directly and the others by the addition-theorem recurrence (kg::ray_chunk).
+__global__ void __launch_bounds__(256) stepped_kernel(SampleArgs a) {
+  const uint32_t fl = *a.flags;
+  const bool ordinary_active = (fl & FLAG_ANY_ETA_POS) != 0;
+  const bool step_zero = (fl & FLAG_ANY_STEP_ZERO) != 0;
+  const int64_t chunk = a.chunk;
+  const int64_t nch = (a.nsamp + chunk - 1) / chunk;
+  const int64_t total = a.npix * nch;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+    // lanes take consecutive rays of the class-sorted order at the same chunk: uniform
+    // branches across the warp and (mostly) contiguous stores
+    const int64_t c = i / a.npix;
+    const int64_t p = __ldg(a.perm + (i - c * a.npix));
+    RecView f{a.rec + p, a.npix};
+    const int code = __ldg(a.code + p);
+    const int64_t g0 = c * chunk;
+    const int64_t g1 = g0 + chunk < a.nsamp ? g0 + chunk : a.nsamp;
+    ray_chunk(a.obs, f, code, g0, g1, a.nsamp, ordinary_active, step_zero,
+              [&](int64_t g, double tau, const Sample& S) {
+                const int64_t o = g * a.npix + p;
+                if (a.t) a.t[o] = S.t;
+                if (a.r) a.r[o] = S.r;
+                if (a.th) a.th[o] = S.th;
+                if (a.ph) a.ph[o] = S.ph;
+                if (a.sig) a.sig[o] = S.sig;
+                if (a.mino) a.mino[o] = tau;
+              });
+  }
+}
+
 cudaError_t launch_samples(const SampleArgs& a, cudaStream_t s) {
-  const int64_t total = a.npix * a.nsamp;
-  if (total <= 0) return cudaSuccess;
+  const int64_t total0 = a.npix * a.nsamp;
+  if (total0 <= 0) return cudaSuccess;
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (a.tau == nullptr && a.do_phi_t && a.chunk > 0) {
+    const int block = 256;
+    const int64_t nch = (a.nsamp + a.chunk - 1) / a.chunk;
+    int64_t grid = (a.npix * nch + block - 1) / block;
+    const int64_t cap = (int64_t)sms * 64;
+    if (grid > cap) grid = cap;
+    stepped_kernel<<<(unsigned)grid, block, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  const int64_t total = total0;
   const int block = 256;
   int64_t grid = (total + block - 1) / block;
   const int64_t cap = (int64_t)sms * 16;  // grid-stride beyond 16 resident-ish blocks per SM

@@ -11,6 +11,8 @@ __global__ void __launch_bounds__(128) ray_setup_kernel(SetupArgs a) {
     RayRec R;
     int rc = 0, tc = 0;
     fl = ray_setup(a.obs, a.alpha[i], a.beta[i], a.maxtaufrac, &R, &rc, &tc);
+    if (a.ngeo > 1)
+      R.code = step_constants<const double*>(R.f, R.code, R.f[F_TAUMAX] / (double)(a.ngeo - 1), R.f);
 #pragma unroll
     for (int k = 0; k < NUM_FIELDS; ++k) a.rec[(int64_t)k * a.npix + i] = R.f[k];
     a.code[i] = R.code;
@@ -21,6 +23,36 @@ __global__ void __launch_bounds__(128) ray_setup_kernel(SetupArgs a) {
   }
   fl = __reduce_or_sync(0xffffffffu, fl);
   if ((threadIdx.x & 31) == 0 && fl) atomicOr(a.flags, fl);
+  // class-bucket counts, one atomic per distinct bucket of the warp
+  const int key = i < a.npix ? ray_bucket(a.code[i]) : -1;
+  const unsigned grp = __match_any_sync(0xffffffffu, key);
+  if (key >= 0 && (threadIdx.x & 31) == (unsigned)(__ffs(grp) - 1)) atomicAdd(a.counts + key, (uint32_t)__popc(grp));
+}
+
+// Exclusive scan of the bucket counts into the cursors (one warp).
+__global__ void bucket_scan_kernel(uint32_t* counts) {
+  const int lane = threadIdx.x;
+  uint32_t c = counts[lane];
+  uint32_t v = c;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += u;
+  }
+  counts[NBUCKET + lane] = v - c;
+}
+
+// Scatter rays into their buckets (order inside a bucket follows warp arrival; the
+// computation of a ray does not depend on its position).
+__global__ void __launch_bounds__(128) bucket_scatter_kernel(const int* code, int64_t npix, uint32_t* counts, int* perm) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int key = i < npix ? ray_bucket(code[i]) : -1;
+  const unsigned grp = __match_any_sync(0xffffffffu, key);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(grp) - 1;
+  uint32_t base = 0;
+  if (key >= 0 && lane == leader) base = atomicAdd(counts + NBUCKET + key, (uint32_t)__popc(grp));
+  base = __shfl_sync(grp, base, leader);
+  if (key >= 0) perm[base + __popc(grp & ((1u << lane) - 1u))] = (int)i;
 }
 
 cudaError_t launch_ray_setup(const SetupArgs& a, cudaStream_t s) {
@@ -28,6 +60,8 @@ cudaError_t launch_ray_setup(const SetupArgs& a, cudaStream_t s) {
   const int block = 128;
   const int64_t grid = (a.npix + block - 1) / block;
   ray_setup_kernel<<<(unsigned)grid, block, 0, s>>>(a);
+  bucket_scan_kernel<<<1, 32, 0, s>>>(a.counts);
+  bucket_scatter_kernel<<<(unsigned)grid, block, 0, s>>>(a.code, a.npix, a.counts, a.perm);
   return cudaGetLastError();
 }
 

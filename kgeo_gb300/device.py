@@ -116,16 +116,18 @@ class PreparedRays:
                                            self.ngeo, self.maxtaufrac, _ptr(self.ws), self.ws_bytes,
                                            ctypes.byref(per), self._stream(stream)))
 
-    def alloc(self, nsamp=None, keys=('t', 'r', 'th', 'ph', 'sig', 'mino')):
+    def alloc(self, nsamp=None, keys=('t', 'r', 'th', 'ph', 'sig', 'mino'), fill=None):
         n = self.ngeo if nsamp is None else nsamp
-        return {k: torch.empty((n, self.npix), dtype=torch.float64, device=self.dev) for k in keys}
+        if fill is None:
+            return {k: torch.empty((n, self.npix), dtype=torch.float64, device=self.dev) for k in keys}
+        return {k: torch.full((n, self.npix), fill, dtype=torch.float64, device=self.dev) for k in keys}
 
-    def samples(self, out, tau=None, do_phi_and_t=True, flags=None, stream=None):
+    def samples(self, out, tau=None, do_phi_and_t=True, flags=None, stream=None, chunk=-1):
         nsamp = tau.shape[0] if tau is not None else self.ngeo
         g = _lib.GeodesicsOut(*[_ptr(out.get(k)) for k in ('t', 'r', 'th', 'ph', 'sig', 'mino')],
                               None, None, None, _ptr(flags))
         _lib.check(self.lib.kgeo_ray_samples(ctypes.byref(self.obs), _ptr(self.ws), self.ws_bytes, self.npix,
-                                             _ptr(tau), nsamp, 1 if do_phi_and_t else 0, ctypes.byref(g),
+                                             _ptr(tau), nsamp, 1 if do_phi_and_t else 0, int(chunk), ctypes.byref(g),
                                              self._stream(stream)))
         return out
 

@@ -934,3 +934,93 @@ def image_grid(alpha_min, alpha_max, beta_min, beta_max, psize):
     betas = np.linspace(beta_min, beta_min + n_b * psize, n_b)
     A, B = np.meshgrid(alphas, betas)
     return A.flatten(), B.flatten()
+
+
+# ----------------------------------------------------------------------------
+# conditioning helper for the parity tests
+# ----------------------------------------------------------------------------
+
+
+def pole_distance(a, r_o, th_o, alpha, beta, tau):
+    """Smallest |1 - n sin^2(amplitude)| over the elliptic-Pi characteristics n > 0 that the
+    reference evaluates at each sample (the r-part Pi's of kgeo/kerr_raytracing_ana.py:447-612
+    and the theta-part Pi of :243-285, 326-360). Near 0 the reference's Pi, and the R1/S1
+    combinations that cancel its pole, carry rounding amplified by ~1/rho.
+    """
+    if tau.ndim == 1:
+        tau = tau.reshape(1, tau.shape[0])
+    lam, eta = conserved(a, th_o, alpha, beta)
+    s_o = beta_sign(beta)
+    up, um, _, _, _ = theta_turning(a, th_o, lam, eta)
+    r1, r2, r3, r4, _ = quartic_roots(a, lam, eta)
+    rplus = 1 + np.sqrt(1 - a ** 2)
+    rminus = 1 - np.sqrt(1 - a ** 2)
+    out = np.full(tau.shape, np.inf)
+
+    def upd(cols, ns, amp):
+        s2 = np.sin(amp) ** 2
+        for nn in ns:
+            rho = np.where(nn > 0, np.abs(1 - nn * s2), np.inf)
+            out[:, cols] = np.minimum(out[:, cols], rho)
+
+    m4 = np.imag(r1) != 0
+    if np.any(m4):
+        a1, b1, a2, b2, CC, DD, k4, g0 = _case4_params(a, r_o, r2[m4], r4[m4])
+        x_p = (rplus + b1) / a2
+        x_m = (rminus + b1) / a2
+        x_o = np.inf if r_o == np.inf else (r_o + b1) / a2
+        gp = (g0 * x_p - 1.) / (g0 + x_p)
+        gm = (g0 * x_m - 1.) / (g0 + x_m)
+        Ir_o = 2. / (CC + DD) * sp.ellipkinc(np.arctan(x_o) + np.arctan(g0), k4)
+        X = ((CC + DD) / 2.) * (-tau[:, m4] + Ir_o)
+        am = sp.ellipj(X, k4)[3]
+        upd(m4, [1 + g0 ** 2, 1 + gp ** 2, 1 + gm ** 2], am)
+    m3 = (np.imag(r3) != 0) * (~m4)
+    if np.any(m3):
+        a1, b1, rr1, rr2, rr21, AA, BB, k3 = _case3_params(r1[m3], r2[m3], r4[m3])
+        rrp1, rrp2, rrm1, rrm2 = rplus - rr1, rplus - rr2, rminus - rr1, rminus - rr2
+        x_p = (AA * rrp1 - BB * rrp2) / (AA * rrp1 + BB * rrp2)
+        x_m = (AA * rrm1 - BB * rrm2) / (AA * rrm1 + BB * rrm2)
+        x_o = (AA - BB) / (AA + BB) if r_o == np.inf else \
+            (AA * (r_o - rr1) - BB * (r_o - rr2)) / (AA * (r_o - rr1) + BB * (r_o - rr2))
+        als = [(BB + AA) / (BB - AA), -1. / x_p, -1. / x_m]
+        pref = 1. / np.sqrt(AA * BB)
+        X = (1. / pref) * (-tau[:, m3] + pref * sp.ellipkinc(np.arccos(x_o), k3))
+        am = sp.ellipj(X, k3)[3]
+        upd(m3, [al ** 2 / (al ** 2 - 1) for al in als], am)
+    m2 = (np.imag(r3) == 0.) * (~m3)
+    if np.any(m2):
+        rr1, rr2, rr3, rr4 = (np.real(r)[m2] for r in (r1, r2, r3, r4))
+        rr31, rr32, rr41, rr42 = rr3 - rr1, rr3 - rr2, rr4 - rr1, rr4 - rr2
+        k2 = (rr32 * rr41) / (rr31 * rr42)
+        x_o = np.sqrt(rr31 / rr41) if r_o == np.inf else np.sqrt((rr31 * (r_o - rr4)) / (rr41 * (r_o - rr3)))
+        Ir_o = 2 * sp.ellipkinc(np.arcsin(x_o), k2) / np.sqrt(rr31 * rr42)
+        X = 0.5 * np.sqrt(rr31 * rr42) * (-tau[:, m2] + Ir_o)
+        am = sp.ellipj(X, k2)[3]
+        ns = [rr41 / rr31, ((rplus - rr3) * rr41) / ((rplus - rr4) * rr31),
+              ((rminus - rr3) * rr41) / ((rminus - rr4) * rr31)]
+        upd(m2, ns, am)
+    # theta part
+    if np.any(eta > 0.):
+        sel = eta >= 0.
+        if np.abs(a) >= MINSPIN:
+            kk = up[sel] / um[sel]
+            a2um = a ** 2 * um[sel]
+            pref = 1 / np.sqrt(-a2um)
+            arg = np.arcsin(np.cos(th_o) / np.sqrt(up[sel]))
+            Gth_o = -pref * sp.ellipkinc(arg, kk)
+            snarg = np.sqrt(-a2um) * (-tau[:, sel] + s_o[sel] * Gth_o)
+            _, amp = _am_beyond_quarter(snarg, kk)
+            upd(sel, [up[sel]], amp)
+    if np.any(eta < 0.) and np.abs(a) >= MINSPIN:
+        sel = eta < 0.
+        u_p, u_m = up[sel], um[sel]
+        a2um = a ** 2 * u_m
+        h = 1. if th_o <= np.pi / 2 else -1
+        kk = 1 - u_p / u_m
+        nu_o = np.arcsin(np.sqrt((np.cos(th_o) ** 2 - u_m) / (u_p - u_m)))
+        Gth_o = -h * (1 / np.sqrt(a2um)) * sp.ellipkinc(nu_o, kk)
+        snarg = np.sqrt(a2um) * (-tau[:, sel] + s_o[sel] * Gth_o)
+        _, amp = _am_beyond_quarter(snarg, kk)
+        upd(sel, [(u_p - u_m) / (1. - u_m)], amp)
+    return out

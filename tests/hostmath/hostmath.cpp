@@ -32,12 +32,13 @@ void hm_roots(const double* ob, double lam, double eta, double* out, int* rclass
   *rclass = R.rclass;
 }
 unsigned hm_setup(const double* ob, const double* alpha, const double* beta, long n, double maxtaufrac,
-                  double* rec, int* code, int* rclass, int* thclass) {
+                  double* rec, int* code, int* rclass, int* thclass, long ngeo) {
   Observer o = make_obs(ob);
   unsigned flags = 0;
   for (long i = 0; i < n; ++i) {
     RayRec R;
     flags |= ray_setup(o, alpha[i], beta[i], maxtaufrac, &R, rclass + i, thclass + i);
+    if (ngeo > 1) R.code = step_constants<const double*>(R.f, R.code, R.f[F_TAUMAX] / (double)(ngeo - 1), R.f);
     for (int k = 0; k < NUM_FIELDS; ++k) rec[k * n + i] = R.f[k];
     code[i] = R.code;
   }
@@ -52,6 +53,48 @@ void hm_samples(const double* ob, const double* rec, const int* code, long n, co
       Sample S = sample_all(o, f, code[i], tau[g * n + i], ordinary_active != 0);
       t[g * n + i] = S.t; r[g * n + i] = S.r; th[g * n + i] = S.th; ph[g * n + i] = S.ph; sig[g * n + i] = S.sig;
     }
+  }
+}
+void hm_samples_stepped(const double* ob, const double* rec, const int* code, long n, long G, long chunk,
+                        int ordinary_active, double* t, double* r, double* th, double* ph, double* sig, double* mino) {
+  Observer o = make_obs(ob);
+  for (long i = 0; i < n; ++i) {
+    RecView f{rec + i, n};
+    for (long g0 = 0; g0 < G; g0 += chunk) {
+      long g1 = g0 + chunk < G ? g0 + chunk : G;
+      ray_chunk(o, f, code[i], g0, g1, G, ordinary_active != 0, false, [&](long g, double tau, const Sample& S) {
+        t[g * n + i] = S.t; r[g * n + i] = S.r; th[g * n + i] = S.th; ph[g * n + i] = S.ph; sig[g * n + i] = S.sig;
+        mino[g * n + i] = tau;
+      });
+    }
+  }
+}
+void hm_theta_debug(const double* ob, const double* rec, const int* code, long n, long i, long G, double* out) {
+  Observer o = make_obs(ob);
+  RecView f{rec + i, n};
+  double taumax = f[F_TAUMAX];
+  ThetaState ts;
+  for (long g = 0; g < G; ++g) {
+    double tau = linspace_at(g, G, taumax, false);
+    ThetaState d = theta_state_direct(f, code[i], theta_snarg(f, tau));
+    if (g == 0 || !theta_step(f, &ts)) ts = d;
+    double* q = out + g * 10;
+    q[0] = ts.sn; q[1] = ts.cn; q[2] = ts.dn; q[3] = ts.pi; q[4] = ts.e;
+    q[5] = d.sn; q[6] = d.cn; q[7] = d.dn; q[8] = d.pi; q[9] = d.e;
+  }
+}
+void hm_radial_debug(const double* ob, const double* rec, const int* code, long n, long i, long G, double* out) {
+  RecView f{rec + i, n};
+  double taumax = f[F_TAUMAX];
+  RadialState rs;
+  for (long g = 0; g < G; ++g) {
+    double tau = linspace_at(g, G, taumax, false);
+    double X = radial_X(f, tau);
+    RadialState d = radial_state_direct(f, code[i], X, true);
+    if (g == 0 || !radial_step(f, &rs, X)) rs = d;
+    double* q = out + g * 14;
+    q[0] = rs.sn; q[1] = rs.cn; q[2] = rs.dn; q[3] = rs.E; q[4] = rs.P[0]; q[5] = rs.P[1]; q[6] = rs.P[2];
+    q[7] = d.sn; q[8] = d.cn; q[9] = d.dn; q[10] = d.E; q[11] = d.P[0]; q[12] = d.P[1]; q[13] = d.P[2];
   }
 }
 void hm_requatorial(const double* ob, const double* alpha, const double* beta, long n, int mbar_lo, int nord,

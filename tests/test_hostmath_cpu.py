@@ -60,13 +60,30 @@ def host_trace(L, a, r_o, th_o, alpha, beta, ngeo, maxtaufrac=1 - 1e-10):
     code, rc, tc = (np.zeros(n, np.int32) for _ in range(3))
     alpha = np.ascontiguousarray(alpha, float)
     beta = np.ascontiguousarray(beta, float)
-    flags = L.hm_setup(dp(ob), dp(alpha), dp(beta), ctypes.c_long(n), D(maxtaufrac), dp(rec), ip(code), ip(rc), ip(tc))
+    flags = L.hm_setup(dp(ob), dp(alpha), dp(beta), ctypes.c_long(n), D(maxtaufrac), dp(rec), ip(code), ip(rc), ip(tc), ctypes.c_long(ngeo))
     tau = np.ascontiguousarray(np.linspace(0, rec.reshape(nf, n)[2], ngeo))
     outs = [np.zeros((ngeo, n)) for _ in range(5)]
     L.hm_samples(dp(ob), dp(rec), ip(code), ctypes.c_long(n), dp(tau), ctypes.c_long(ngeo), ctypes.c_int(flags & 1),
                  *[dp(o) for o in outs])
     t, r, th, ph, sig = outs
     return dict(t=t, r=r, th=th, ph=ph, sig=sig, rclass=rc, thclass=tc)
+
+
+def host_trace_stepped(L, a, r_o, th_o, alpha, beta, ngeo, chunk, maxtaufrac=1 - 1e-10):
+    n = len(alpha)
+    nf = L.hm_num_fields()
+    ob = observer(a, r_o, th_o)
+    rec = np.zeros(nf * n)
+    code, rc, tc = (np.zeros(n, np.int32) for _ in range(3))
+    alpha = np.ascontiguousarray(alpha, float)
+    beta = np.ascontiguousarray(beta, float)
+    flags = L.hm_setup(dp(ob), dp(alpha), dp(beta), ctypes.c_long(n), D(maxtaufrac), dp(rec), ip(code), ip(rc), ip(tc),
+                       ctypes.c_long(ngeo))
+    outs = [np.zeros((ngeo, n)) for _ in range(6)]
+    L.hm_samples_stepped(dp(ob), dp(rec), ip(code), ctypes.c_long(n), ctypes.c_long(ngeo), ctypes.c_long(chunk),
+                         ctypes.c_int(flags & 1), *[dp(o) for o in outs])
+    t, r, th, ph, sig, mino = outs
+    return dict(t=t, r=r, th=th, ph=ph, sig=sig, mino=mino)
 
 
 def rel(a, b):
@@ -125,4 +142,9 @@ def test_host_trace_vs_reference_fixture(hm, golden, name):
     assert np.array_equal(out['rclass'], g['rclass'])
     assert np.array_equal(out['thclass'], g['thclass'])
     if np.isfinite(r_o):
-        check_trace(out, dict(t=g['t'], r=g['r'], th=g['th'], ph=g['ph'], sig=g['sig']), r_o, g['rclass'], name)
+        from oracle import kgeo_oracle as ko
+        rho = ko.pole_distance(a, r_o, th_o, g['alpha'], g['beta'], g['mino'])
+        check_trace(out, dict(t=g['t'], r=g['r'], th=g['th'], ph=g['ph'], sig=g['sig']), r_o, g['rclass'], name, rho=rho)
+        st = host_trace_stepped(hm, a, r_o, th_o, g['alpha'], g['beta'], int(g['ngeo']), 50)
+        check_trace(st, dict(t=g['t'], r=g['r'], th=g['th'], ph=g['ph'], sig=g['sig']), r_o, g['rclass'],
+                    name + '-recurrence', rho=rho)

@@ -49,7 +49,9 @@ def test_trace_vs_reference_fixture(kg, golden, name):
                 fin = np.isfinite(y)
                 assert np.all(np.abs(x[fin] - y[fin]) <= tol * np.maximum(np.abs(y[fin]), 1.0))
         return
-    check_trace(got, ref, r_o, g['rclass'], name)
+    from oracle import kgeo_oracle as ko
+    rho = ko.pole_distance(a, r_o, th_o, g['alpha'], g['beta'], g['mino'])
+    check_trace(got, ref, r_o, g['rclass'], name, rho=rho)
 
 
 def test_config1_full_vs_oracle(kg):
@@ -62,7 +64,8 @@ def test_config1_full_vs_oracle(kg):
     ref = ko.raytrace(a, r_o, th_o, A, B, 100)
     got = _run(kg, a, r_o, th_o, A, B, 100)
     refd = dict(t=ref['t'], r=ref['r'], th=ref['th'], ph=ref['ph'], sig=ref['affine_times'])
-    check_trace(got, refd, r_o, ref['rclass'], 'config1')
+    rho = ko.pole_distance(a, r_o, th_o, A, B, ref['mino_times'])
+    check_trace(got, refd, r_o, ref['rclass'], 'config1', rho=rho)
 
 
 def test_classes_bit_exact_config2_grids(kg):
@@ -99,7 +102,7 @@ def test_coords_at_tau_vs_oracle(kg):
     sig, (t, r, th, ph) = ko.coords_at_tau(a, r_o, th_o, A, B, tau)
     gs, (gt, gr, gth, gph) = kg.coords_at_tau(a, [0, r_o, th_o, 0], [A, B], tau)
     check_trace(dict(t=gt, r=gr, th=gth, ph=gph, sig=gs), dict(t=t, r=r, th=th, ph=ph, sig=sig), r_o,
-                np.zeros(300, int), 'coords_at_tau')
+                np.zeros(300, int), 'coords_at_tau', rho=ko.pole_distance(a, r_o, th_o, A, B, tau))
     gs0, (gt0, gr0, gth0, gph0) = kg.coords_at_tau(a, [0, r_o, th_o, 0], [A, B], tau, do_phi_and_t=False)
     s0, (t0, r0, th0, ph0) = ko.coords_at_tau(a, r_o, th_o, A, B, tau, do_phi_and_t=False)
     assert np.allclose(gr0, r0, rtol=1e-10, atol=0) and np.allclose(gth0, th0, rtol=1e-10, atol=1e-10)
@@ -202,3 +205,43 @@ def test_r_equatorial_config2_grid_vs_oracle(kg):
         assert np.array_equal(r_s[m] == 0, rr == 0)
         np.testing.assert_allclose(r_s[m], rr, rtol=1e-10, atol=0)
         np.testing.assert_allclose(Ir[m], ir, rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.parametrize('seed', [11, 12, 13])
+def test_config2_draws_vs_oracle(kg, seed):
+    """Seeded configuration-2 geometries (a ~ U[0, 0.998), theta_o ~ U[1, 89] deg, one mirrored
+    below the equator), 40x40 over [-10, 10], ngeo = 400, through the default (recurrence) path."""
+    from oracle import kgeo_oracle as ko
+    rng = np.random.default_rng(seed)
+    a = float(rng.uniform(0, 0.998))
+    th_o = float(rng.uniform(1, 89)) * np.pi / 180
+    if seed == 13:
+        th_o = np.pi - th_o
+    x = np.linspace(-10, 10, 40)
+    A, B = (v.flatten() for v in np.meshgrid(x, x))
+    ref = ko.raytrace(a, 1.e4, th_o, A, B, 400)
+    got = _run(kg, a, 1.e4, th_o, A, B, 400)
+    rho = ko.pole_distance(a, 1.e4, th_o, A, B, ref['mino_times'])
+    check_trace(got, dict(t=ref['t'], r=ref['r'], th=ref['th'], ph=ref['ph'], sig=ref['affine_times']), 1.e4,
+                ref['rclass'], 'config2-%d' % seed, rho=rho)
+
+
+@pytest.mark.parametrize('chunk', [1, 7, 50, 64])
+def test_recurrence_matches_independent_samples(kg, chunk):
+    """The addition-theorem recurrence (chunk > 1) against independent per-sample evaluation
+    (chunk 0) on the same prepared rays: same classes, agreement within the parity bars."""
+    import torch
+    from oracle import kgeo_oracle as ko
+    from kgeo_gb300 import device as dev
+    x = np.linspace(-9, 9, 48)
+    A, B = (v.flatten() for v in np.meshgrid(x, x))
+    a, th_o = 0.8, 35 * np.pi / 180
+    prep = dev.PreparedRays(a, 1.e4, th_o, dev.as_device(A), dev.as_device(B), ngeo=200)
+    o0 = prep.samples(prep.alloc(fill=float('nan')), chunk=0)
+    o1 = prep.samples(prep.alloc(fill=float('nan')), chunk=chunk)
+    torch.cuda.synchronize()
+    h0 = {k: v.cpu().numpy() for k, v in o0.items()}
+    h1 = {k: v.cpu().numpy() for k, v in o1.items()}
+    assert np.array_equal(h0['mino'], h1['mino'])
+    rho = ko.pole_distance(a, 1.e4, th_o, A, B, h0['mino'])
+    check_trace(h1, h0, 1.e4, prep.rclass.cpu().numpy(), 'chunk%d' % chunk, rho=rho)
