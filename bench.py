@@ -336,17 +336,146 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------
+# configuration 3: mixed precision (2048^2 grid + polar band near the critical curve)
+# ---------------------------------------------------------------------------
+
+def mixed_workload(small=False):
+    from kgeo_gb300.equatorial_lensing import critical_band
+    a, th_o = 0.94, 17 * np.pi / 180
+    n = 256 if small else 2048
+    x = np.linspace(-LIM, LIM, n)
+    A, B = (v.flatten() for v in np.meshgrid(x, x))
+    bA, bB = critical_band(a, th_o, n_angles=512 if small else 4096, n_radii=32 if small else 256)
+    return a, th_o, np.concatenate([A, bA]), np.concatenate([B, bB]), A.size
+
+
+def _oracle_chunk(args):
+    a, th_o, A, B, ngeo = args
+    from oracle import kgeo_oracle as ko
+    import warnings
+    warnings.filterwarnings('ignore')
+    out = ko.raytrace(a, R_O, th_o, A, B, ngeo)
+    return np.stack([out['r'], out['th'], out['ph'], out['t'], out['affine_times']]), out['rclass']
+
+
+def error_stats(got, ref, rclass, torch):
+    """Per output max / RMS relative error with the parity scales; the horizon-adjacent last
+    sample of rclass 2-4 rays is reported separately."""
+    res = {}
+    G = ref['r'].shape[0]
+    horizon = torch.isin(rclass, torch.tensor([2, 3, 4], device=rclass.device))
+    for k, scale in (('r', None), ('th', 1.0), ('ph', 1.0), ('t', R_O), ('sig', R_O)):
+        x, y = got[k], ref[k]
+        den = y.abs() if scale is None else torch.clamp(y.abs(), min=scale)
+        e = (x - y).abs() / den
+        fin = torch.isfinite(e)
+        e = torch.where(fin, e, torch.zeros_like(e))
+        body = e[:G - 1]
+        last = e[G - 1][horizon]
+        e_rest = e[G - 1][~horizon]
+        mx = max(float(body.max()), float(e_rest.max()) if e_rest.numel() else 0.0)
+        rms = float(torch.sqrt((body.double() ** 2).mean()))
+        res[k] = {'max': mx, 'rms': rms, 'horizon_sample_max': float(last.max()) if last.numel() else 0.0,
+                  'nonfinite_mismatch': int((torch.isfinite(x) != torch.isfinite(y)).sum())}
+    return res
+
+
+def run_mixed(args):
+    small = args.case == 'mixed-small'
+    pool = cores = None
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()
+    import torch
+    from kgeo_gb300 import device as dev
+    a, th_o, A, B, ngrid = mixed_workload(small)
+    npix = A.size
+    G = 256
+    al, be = dev.as_device(A), dev.as_device(B)
+    prep = dev.PreparedRays(a, R_O, th_o, al, be, ngeo=G)
+    out_m = prep.alloc()
+    out_d = prep.alloc()
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / steps
+
+    def step_mixed():
+        prep.setup()
+        prep.samples(out_m, mixed=True)
+
+    def step_fp64():
+        prep.setup()
+        prep.samples(out_d)
+
+    def step_plain():
+        prep.setup()
+        prep.samples(out_d, chunk=0)
+
+    clocks = Clocks(0)
+    clocks.start()
+    t_mixed = timed(step_mixed, args.steps, args.warmup)
+    ck = clocks.stop()
+    t_plain = timed(step_plain, 1, 0)
+    t_fp64 = timed(step_fp64, max(1, args.steps // 2), 1)
+    errs = error_stats(out_m, out_d, prep.rclass, torch)
+    # FP64 kernel against the oracle on a seeded 1/64 subsample of the same rays
+    orc = None
+    if pool is not None:
+        rng = np.random.default_rng(0)
+        sub = np.sort(rng.choice(npix, npix // 64, replace=False))
+        chunks = np.array_split(sub, cores * 4)
+        parts = pool.map(_oracle_chunk, [(a, th_o, A[c], B[c], G) for c in chunks if c.size])
+        pool.close()
+        ref = np.concatenate([p_[0] for p_ in parts], axis=2)
+        rc = np.concatenate([p_[1] for p_ in parts])
+        idx = torch.from_numpy(sub).to(al.device)
+        got = {k: out_d[k][:, idx] for k in ('r', 'th', 'ph', 't', 'sig')}
+        refd = {k: torch.from_numpy(ref[i]).to(al.device) for i, k in enumerate(('r', 'th', 'ph', 't', 'sig'))}
+        orc = error_stats(got, refd, torch.from_numpy(rc).to(al.device), torch)
+        orc['rays'] = int(sub.size)
+    points = npix * G
+    line = {
+        'metric': 'Kerr rays/s: mixed-precision raytrace (ngeo=256), 2048^2 grid + 256x4096 critical-curve band',
+        'value': npix / t_mixed, 'unit': 'rays/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': t_mixed * 1e3, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32+f64', 'data': 'synthetic: uniform grid + polar band from critical_curve(0.94, 17 deg)',
+        'config': {'workload': 'configuration 3: a=0.94, theta_o=17 deg, r_o=1e4, ngeo=256, '
+                               '%d grid + %d band rays' % (ngrid, npix - ngrid), 'npix': npix, 'ngeo': G,
+                   'precision': 'mixed', 'case': args.case},
+        'points_per_s': points / t_mixed,
+        'fp64_recurrence': {'value': npix / t_fp64, 'ms_per_step': t_fp64 * 1e3},
+        'fp64_plain': {'value': npix / t_plain, 'ms_per_step': t_plain * 1e3},
+        'speedup_vs_fp64_recurrence': t_fp64 / t_mixed, 'speedup_vs_fp64_plain': t_plain / t_mixed,
+        'mixed_vs_fp64_error': errs, 'fp64_vs_oracle_error': orc, 'clocks': ck,
+        'gpu_launches': 4 * args.steps,
+    }
+    print(json.dumps(line))
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument('--gpus', type=int, default=1)
     p.add_argument('--steps', type=int, default=5)
     p.add_argument('--warmup', type=int, default=3)
     p.add_argument('--impl', choices=('ours', 'reference'), default='ours')
-    p.add_argument('--case', choices=('full', 'small'), default='full')
+    p.add_argument('--case', choices=('full', 'small', 'mixed', 'mixed-small'), default='full')
     p.add_argument('--no-cpu-baseline', action='store_true')
     args = p.parse_args()
     if args.impl == 'reference':
         run_reference(args)
+    elif args.case.startswith('mixed'):
+        run_mixed(args)
     else:
         run_ours(args)
 

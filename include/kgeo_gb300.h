@@ -41,6 +41,13 @@ typedef enum {
   KGEO_ERR_NOALLOC_SIZE = 11 /* npix above KGEO_NOALLOC_MAX_PIXELS for kgeo_raytrace_noalloc */
 } kgeo_status;
 
+/* Arithmetic of the sample kernels. FP64: every output within the FP64 parity bars.
+ * MIXED: FP32 for the elliptic-integral increments, the chunk-start integrals and theta, FP64
+ * for the Jacobi state, r and the final sums; samples next to an elliptic-Pi pole and the
+ * final horizon-adjacent sample stay FP64 (error bars: bench.py --case mixed / DESIGN). */
+#define KGEO_PRECISION_FP64 0
+#define KGEO_PRECISION_MIXED 1
+
 /* Bits of the device flags word written by the tracing entry points. */
 #define KGEO_FLAG_ANY_ETA_POS 1u
 #define KGEO_FLAG_ANY_ETA_NONPOS 2u
@@ -83,6 +90,12 @@ int kgeo_raytrace(const kgeo_observer* obs, const double* alpha, const double* b
                   int32_t ngeo, double maxtaufrac, kgeo_geodesics* out, void* workspace,
                   size_t workspace_bytes, void* stream);
 
+/* kgeo_raytrace with the mixed-precision sample kernel (KGEO_PRECISION_MIXED); same
+ * arguments and outputs. */
+int kgeo_raytrace_mixed(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                        int32_t ngeo, double maxtaufrac, kgeo_geodesics* out, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
 /* coords_at_tau(a, observer_coords, image_coords, tau, do_phi_and_t)
  * (kgeo/kerr_raytracing_ana.py:126-193): coordinates at caller-given Mino times
  * tau (ntau, npix). With do_phi_and_t == 0 only r and theta are meaningful
@@ -106,13 +119,14 @@ int kgeo_coords_at_tau(const kgeo_observer* obs, const double* alpha, const doub
  * every sample independently (Landen + Carlson per sample); k > 0 gives each thread k
  * consecutive samples, the first (and the grid's last) evaluated directly and the rest by
  * the addition theorems of sn/cn/dn, E and Pi from the previous sample (k is capped at 64);
- * < 0 picks the library default. Caller-given tau always uses independent evaluation. */
+ * < 0 picks the library default. Caller-given tau always uses independent evaluation.
+ * precision: KGEO_PRECISION_FP64 or KGEO_PRECISION_MIXED (the latter for the recurrence). */
 int kgeo_ray_setup(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix, int32_t ngeo,
                    double maxtaufrac, void* workspace, size_t workspace_bytes, kgeo_geodesics* per_ray,
                    void* stream);
 int kgeo_ray_samples(const kgeo_observer* obs, const void* workspace, size_t workspace_bytes, int64_t npix,
-                     const double* tau, int32_t nsamp, int32_t do_phi_and_t, int32_t chunk, kgeo_geodesics* out,
-                     void* stream);
+                     const double* tau, int32_t nsamp, int32_t do_phi_and_t, int32_t chunk, int32_t precision,
+                     kgeo_geodesics* out, void* stream);
 
 /* r_equatorial(a, r_o, th_o, mbar, alpha, beta) (kgeo/equatorial_lensing.py:85-196) for the
  * orders mbar = mbar_lo .. mbar_lo + n_orders - 1 in one pass: r_s and Ir are (n_orders, npix),

@@ -36,7 +36,9 @@ SIGNATURES = {
     'kgeo_ray_setup': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_int32, c_double, c_void_p,
                                c_size_t, ctypes.POINTER(GeodesicsOut), c_void_p]),
     'kgeo_ray_samples': (c_int, [ctypes.POINTER(Observer), c_void_p, c_size_t, c_int64, c_void_p, c_int32, c_int32,
-                                 c_int32, ctypes.POINTER(GeodesicsOut), c_void_p]),
+                                 c_int32, c_int32, ctypes.POINTER(GeodesicsOut), c_void_p]),
+    'kgeo_raytrace_mixed': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_int32, c_double,
+                                    ctypes.POINTER(GeodesicsOut), c_void_p, c_size_t, c_void_p]),
     'kgeo_raytrace_noalloc': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_int32, c_double,
                                       ctypes.POINTER(GeodesicsOut), c_void_p]),
     'kgeo_measure_fp64_peak': (c_int, [ctypes.POINTER(c_double), c_void_p]),
@@ -48,6 +50,8 @@ SIGNATURES = {
     'kgeo_abi_version': (c_int, []),
 }
 
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
 FLAG_ANY_ETA_POS = 1
 FLAG_ANY_ETA_NONPOS = 2
 FLAG_ANY_STEP_ZERO = 4

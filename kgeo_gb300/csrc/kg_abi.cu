@@ -82,7 +82,7 @@ int setup_common(const kgeo_observer* obs, const double* alpha, const double* be
 }
 
 int samples_common(const kgeo_observer* obs, const Workspace& w, int64_t npix, int64_t nsamp, const double* tau,
-                   int do_phi_t, int chunk, kgeo_geodesics* out, cudaStream_t s) {
+                   int do_phi_t, int chunk, int mixed, kgeo_geodesics* out, cudaStream_t s) {
   if (npix > 0) {
     SampleArgs pa;
     pa.obs = make_observer(obs);
@@ -94,6 +94,7 @@ int samples_common(const kgeo_observer* obs, const Workspace& w, int64_t npix, i
     pa.do_phi_t = do_phi_t;
     pa.chunk = chunk < 0 ? DEFAULT_CHUNK : (chunk > MAX_CHUNK ? MAX_CHUNK : chunk);
     pa.perm = w.perm;
+    pa.mixed = mixed;
     pa.flags = w.flags;
     pa.t = out->t;
     pa.r = out->r;
@@ -111,7 +112,7 @@ int samples_common(const kgeo_observer* obs, const Workspace& w, int64_t npix, i
 
 int trace_common(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
                  int64_t nsamp, const double* tau, int do_phi_t, double maxtaufrac, kgeo_geodesics* out,
-                 void* workspace, size_t workspace_bytes_, void* stream) {
+                 void* workspace, size_t workspace_bytes_, void* stream, int mixed = 0) {
   int st = check_observer(obs);
   if (st) return st;
   if (npix < 0) return KGEO_ERR_LENGTHS;
@@ -125,7 +126,7 @@ int trace_common(const kgeo_observer* obs, const double* alpha, const double* be
   Workspace w = carve_workspace(sc.ptr, npix);
   st = setup_common(obs, alpha, beta, npix, tau ? 0 : nsamp, maxtaufrac, w, out, s);
   if (st) return st;
-  return samples_common(obs, w, npix, nsamp, tau, do_phi_t, -1, out, s);
+  return samples_common(obs, w, npix, nsamp, tau, do_phi_t, -1, mixed, out, s);
 }
 
 }  // namespace
@@ -139,6 +140,13 @@ int kgeo_raytrace(const kgeo_observer* obs, const double* alpha, const double* b
                   size_t workspace_bytes_, void* stream) {
   return trace_common(obs, alpha, beta, npix, ngeo, nullptr, 1, maxtaufrac, out, workspace, workspace_bytes_,
                       stream);
+}
+
+int kgeo_raytrace_mixed(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                        int32_t ngeo, double maxtaufrac, kgeo_geodesics* out, void* workspace,
+                        size_t workspace_bytes_, void* stream) {
+  return trace_common(obs, alpha, beta, npix, ngeo, nullptr, 1, maxtaufrac, out, workspace, workspace_bytes_,
+                      stream, 1);
 }
 
 int kgeo_coords_at_tau(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
@@ -208,8 +216,9 @@ int kgeo_ray_setup(const kgeo_observer* obs, const double* alpha, const double* 
 }
 
 int kgeo_ray_samples(const kgeo_observer* obs, const void* workspace, size_t workspace_bytes_, int64_t npix,
-                     const double* tau, int32_t nsamp, int32_t do_phi_and_t, int32_t chunk, kgeo_geodesics* out,
-                     void* stream) {
+                     const double* tau, int32_t nsamp, int32_t do_phi_and_t, int32_t chunk, int32_t precision,
+                     kgeo_geodesics* out, void* stream) {
+  if (precision != KGEO_PRECISION_FP64 && precision != KGEO_PRECISION_MIXED) return KGEO_ERR_MODEL;
   int st = check_observer(obs);
   if (st) return st;
   if (npix < 0) return KGEO_ERR_LENGTHS;
@@ -217,7 +226,8 @@ int kgeo_ray_samples(const kgeo_observer* obs, const void* workspace, size_t wor
   if (!workspace || !out) return KGEO_ERR_NULL;
   if (workspace_bytes_ < workspace_bytes(npix)) return KGEO_ERR_WORKSPACE;
   Workspace w = carve_workspace(const_cast<void*>(workspace), npix);
-  return samples_common(obs, w, npix, nsamp, tau, do_phi_and_t ? 1 : 0, chunk, out, static_cast<cudaStream_t>(stream));
+  return samples_common(obs, w, npix, nsamp, tau, do_phi_and_t ? 1 : 0, chunk, precision == KGEO_PRECISION_MIXED,
+                        out, static_cast<cudaStream_t>(stream));
 }
 
 const char* kgeo_status_string(int status) {

@@ -28,6 +28,14 @@ KG_HD double kg_nan() { return __builtin_nan(""); }
 
 KG_HD double sq(double x) { return x * x; }
 
+KG_HD float rsqrt_f(float x) {
+#if defined(__CUDA_ARCH__)
+  return rsqrtf(x);
+#else
+  return 1.0f / sqrtf(x);
+#endif
+}
+
 // x**3 as numpy evaluates it (a correctly rounded pow): product of a double-double
 // square with x, rounded once.
 KG_HD double cube_rn(double x) {

@@ -75,6 +75,7 @@ struct SampleArgs {
   int do_phi_t;
   int chunk;            // > 0: even grid by the addition-theorem recurrence, chunk samples per thread
   const int* perm;      // class-sorted rays for the recurrence kernel
+  int mixed;            // 1: mixed-precision recurrence (kg_mixed.cuh)
   const uint32_t* flags;
   double* t;
   double* r;

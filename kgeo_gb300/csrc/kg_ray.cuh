@@ -61,11 +61,17 @@ enum RecField : int {
   // one step of the even Mino grid: theta Jacobi values / integrals at the step, r ditto
   S_TSN, S_TCN, S_TDN, S_TE, S_TPI, S_TC,
   S_RSN, S_RCN, S_RDN, S_RE, S_RP0, S_RP1, S_RP2, S_RC0, S_RC1, S_RC2,
+  // observer constants the gain estimate needs
+  G_A, G_RP, G_RM, G_RO,
   NUM_FIELDS
 };
 
 // code bit: the ray's samples may be produced by the addition-theorem recurrence
 constexpr int CODE_STEP = 1 << 10;
+// code bits 11..15: the mixed-precision recurrence keeps the increments of this integral in
+// FP64 (theta Pi, r Pi_0, Pi_1, Pi_2, r E) because its errors reach phi or t / r_o amplified
+constexpr int CODE_F64_SHIFT = 11;
+constexpr double MIXED_GAIN_MAX = 2.0;
 
 // Strided view of one ray's record inside the structure-of-arrays buffer.
 struct RecView {
@@ -90,6 +96,7 @@ KG_HD int code_th(int code) { return (code >> 4) & 15; }
 KG_HD bool code_kk0(int code) { return (code >> 8) & 1; }
 KG_HD bool code_minspin(int code) { return (code >> 9) & 1; }
 KG_HD bool code_step(int code) { return (code >> 10) & 1; }
+KG_HD bool code_f64(int code, int i) { return (code >> (CODE_F64_SHIFT + i)) & 1; }
 
 // ---------------------------------------------------------------------------
 // building blocks at a generic amplitude (ray constants)
@@ -295,6 +302,10 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
   double s = beta >= 0 ? 1.0 : -1.0;  // my_sign, kgeo/kerr_raytracing_utils.py:857-864
   f[F_LAM] = lam;
   f[F_S] = s;
+  f[G_A] = a;
+  f[G_RP] = o.rplus;
+  f[G_RM] = o.rminus;
+  f[G_RO] = o.r_o;
 
   // u_+, u_- with clamps, kgeo/kerr_raytracing_utils.py:290-326
   Turning U = u_turning(o, lam, eta);
@@ -1033,6 +1044,57 @@ KG_HD void ray_chunk(const Observer& ob, const FV& f, int code, int64_t g0, int6
   }
 }
 
+struct GainArgs {
+  double a, rp, rm, r_o;
+};
+
+template <class FV>
+KG_HD GainArgs ob_gain_args(const FV& f) {
+  return GainArgs{f[G_A], f[G_RP], f[G_RM], f[G_RO]};
+}
+
+// Amplification of an absolute error in each elliptic integral into phi and into t / r_o,
+// following the combinations of radial_assemble / theta_assemble / combine. gain[0]: theta Pi,
+// gain[1..3]: r Pi_0..2, gain[4]: r E.
+template <class FV>
+KG_HD void mixed_gains(const GainArgs& g, const FV& f, int code, double* gain) {
+  const double lam = f[F_LAM];
+  const double tsc = 1.0 / (g.r_o > 0 && g.r_o < 1e300 ? g.r_o : 1.0);
+  const double cphi_p = fabs(2 * g.a / (g.rp - g.rm) * (g.rp - 0.5 * g.a * lam));
+  const double cphi_m = fabs(2 * g.a / (g.rp - g.rm) * (g.rm - 0.5 * g.a * lam));
+  const double ct_p = fabs(4 / (g.rp - g.rm) * (g.rp * g.rp - 0.5 * g.a * lam * g.rp)) * tsc;
+  const double ct_m = fabs(4 / (g.rp - g.rm) * (g.rm * g.rm - 0.5 * g.a * lam * g.rm)) * tsc;
+  const double wp = fmax(cphi_p, ct_p), wm = fmax(cphi_m, ct_m);
+  gain[0] = fabs(lam * f[T_PREF]);
+  gain[1] = gain[2] = gain[3] = gain[4] = 0.0;
+  const int rc = code_rcase(code);
+  const double k = f[R_M];
+  if (rc == RCASE_2) {
+    gain[1] = fabs(f[R_C9] * f[R_C18]) * 3 * tsc;
+    gain[2] = fabs(f[R_C10]) * wp;
+    gain[3] = fabs(f[R_C11]) * wm;
+    gain[4] = fabs(f[R_C12]) * tsc;
+  } else if (rc == RCASE_3) {
+    const double al0 = f[R_C4], alp = f[R_C5], alm = f[R_C6];
+    const double c0 = f[R_C11], pr = f[R_C14], sAB = f[R_C15];
+    const double a02 = al0 * al0, jd = k + (1 - k) * a02;
+    const double r2f = fabs(sAB * c0 * c0);
+    gain[1] = fabs(c0 / (1 - a02)) * (3 + 2 * fabs(pr) + r2f * fabs((2 * k - f[R_N0]) / jd)) * tsc;
+    gain[2] = fabs(f[R_C12] / ((1 - alp * alp) * f[R_C16])) * wp;
+    gain[3] = code_minspin(code) ? 0.0 : fabs(f[R_C13] / ((1 - alm * alm) * f[R_C17])) * wm;
+    gain[4] = r2f * fabs(a02 / (jd * (a02 - 1))) * tsc;
+  } else if (rc == RCASE_4) {
+    const double g0 = f[R_C2], gp = f[R_C3], gm = f[R_C4];
+    const double aa1 = f[R_C13];
+    const double a02 = g0 * g0, a02p1 = 1 + a02, a02j = 1 - k + a02;
+    const double s2w = fabs(f[R_C10] / f[R_C9]) * (1. / a02p1 + (1 - k) / a02j);
+    gain[1] = (a02 / a02p1) * fabs(f[R_C9]) * (3 + 2 * fabs(aa1) + s2w) * tsc;
+    gain[2] = (gp * gp / (1 + gp * gp)) * fabs(f[R_C11] * f[R_C14]) * wp;
+    gain[3] = (gm * gm / (1 + gm * gm)) * fabs(f[R_C12] * f[R_C15]) * wm;
+    gain[4] = fabs(f[R_C10]) * a02 / (a02p1 * a02j) * tsc;
+  }
+}
+
 // Per-ray constants of one step of the even Mino grid (Mino step dtau): the Jacobi
 // functions and the integrals at the step itself. Sets CODE_STEP when the ray can be
 // stepped (finite constants, no n = 1 theta characteristic, not the a < MINSPIN limit).
@@ -1067,7 +1129,15 @@ KG_HD int step_constants(FV f, int code, double dtau, double* out /* f itself, w
     ok = n != 1.0 && std::isfinite(f[T_PIC]);
     for (int i = S_TSN; i <= S_RC2; ++i) ok = ok && std::isfinite(out[i]);
   }
-  return ok ? (code | CODE_STEP) : (code & ~CODE_STEP);
+  code = ok ? (code | CODE_STEP) : (code & ~CODE_STEP);
+  // gains by which an error in each integral's increments reaches phi (scale 1) or t (scale r_o)
+  double gain[5];
+  mixed_gains(ob_gain_args(f), f, code, gain);
+  for (int i = 0; i < 5; ++i) {
+    if (!(gain[i] <= MIXED_GAIN_MAX)) code |= 1 << (CODE_F64_SHIFT + i);
+    else code &= ~(1 << (CODE_F64_SHIFT + i));
+  }
+  return code;
 }
 
 }  // namespace kg

@@ -2,6 +2,7 @@
 // that the lanes of a warp walk consecutive samples of the same ray and take the same
 // branches; stores go to the (nsamp, npix) row-major outputs.
 #include "kg_launch.h"
+#include "kg_mixed.cuh"
 
 namespace kg {
 
@@ -42,6 +43,7 @@ __global__ void __launch_bounds__(256) samples_kernel(SampleArgs a) {
 // Even Mino grid: one thread per (pixel, chunk of `chunk` consecutive samples), items
 // chunk-major over the class-sorted pixels. Each thread evaluates its first sample (and the
 // grid's last) directly and the others by the addition-theorem recurrence (kg::ray_chunk).
+template <bool MIXED>
 __global__ void __launch_bounds__(256) stepped_kernel(SampleArgs a) {
   const uint32_t fl = *a.flags;
   const bool ordinary_active = (fl & FLAG_ANY_ETA_POS) != 0;
@@ -59,16 +61,17 @@ __global__ void __launch_bounds__(256) stepped_kernel(SampleArgs a) {
     const int code = __ldg(a.code + p);
     const int64_t g0 = c * chunk;
     const int64_t g1 = g0 + chunk < a.nsamp ? g0 + chunk : a.nsamp;
-    ray_chunk(a.obs, f, code, g0, g1, a.nsamp, ordinary_active, step_zero,
-              [&](int64_t g, double tau, const Sample& S) {
-                const int64_t o = g * a.npix + p;
-                if (a.t) a.t[o] = S.t;
-                if (a.r) a.r[o] = S.r;
-                if (a.th) a.th[o] = S.th;
-                if (a.ph) a.ph[o] = S.ph;
-                if (a.sig) a.sig[o] = S.sig;
-                if (a.mino) a.mino[o] = tau;
-              });
+    auto emit = [&](int64_t g, double tau, const Sample& S) {
+      const int64_t o = g * a.npix + p;
+      if (a.t) a.t[o] = S.t;
+      if (a.r) a.r[o] = S.r;
+      if (a.th) a.th[o] = S.th;
+      if (a.ph) a.ph[o] = S.ph;
+      if (a.sig) a.sig[o] = S.sig;
+      if (a.mino) a.mino[o] = tau;
+    };
+    if (MIXED) ray_chunk_mixed(a.obs, f, code, g0, g1, a.nsamp, ordinary_active, step_zero, emit);
+    else ray_chunk(a.obs, f, code, g0, g1, a.nsamp, ordinary_active, step_zero, emit);
   }
 }
 
@@ -84,7 +87,8 @@ cudaError_t launch_samples(const SampleArgs& a, cudaStream_t s) {
     int64_t grid = (a.npix * nch + block - 1) / block;
     const int64_t cap = (int64_t)sms * 64;
     if (grid > cap) grid = cap;
-    stepped_kernel<<<(unsigned)grid, block, 0, s>>>(a);
+    if (a.mixed) stepped_kernel<true><<<(unsigned)grid, block, 0, s>>>(a);
+    else stepped_kernel<false><<<(unsigned)grid, block, 0, s>>>(a);
     return cudaGetLastError();
   }
   const int64_t total = total0;

@@ -122,12 +122,13 @@ class PreparedRays:
             return {k: torch.empty((n, self.npix), dtype=torch.float64, device=self.dev) for k in keys}
         return {k: torch.full((n, self.npix), fill, dtype=torch.float64, device=self.dev) for k in keys}
 
-    def samples(self, out, tau=None, do_phi_and_t=True, flags=None, stream=None, chunk=-1):
+    def samples(self, out, tau=None, do_phi_and_t=True, flags=None, stream=None, chunk=-1, mixed=False):
         nsamp = tau.shape[0] if tau is not None else self.ngeo
         g = _lib.GeodesicsOut(*[_ptr(out.get(k)) for k in ('t', 'r', 'th', 'ph', 'sig', 'mino')],
                               None, None, None, _ptr(flags))
         _lib.check(self.lib.kgeo_ray_samples(ctypes.byref(self.obs), _ptr(self.ws), self.ws_bytes, self.npix,
-                                             _ptr(tau), nsamp, 1 if do_phi_and_t else 0, int(chunk), ctypes.byref(g),
+                                             _ptr(tau), nsamp, 1 if do_phi_and_t else 0, int(chunk),
+                                             _lib.PRECISION_MIXED if mixed else _lib.PRECISION_FP64, ctypes.byref(g),
                                              self._stream(stream)))
         return out
 

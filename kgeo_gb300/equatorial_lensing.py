@@ -144,3 +144,40 @@ def _imax_counts(a, r_o, th_o, alpha, beta, key):
     res = _dev.trace(a, r_o, th_o, _dev.as_device(alpha), _dev.as_device(beta), ngeo=1, outputs=(),
                      per_ray=('tau_tot',))
     return _crossings(a, th_o, alpha, beta, res['tau_tot'], (key,))[key]
+
+
+def critical_curve(a, th0, n=100000):
+    """Parametrised critical curve (alpha, beta), 2 x (valid points) long.
+
+    GL19b eqs. 38-40 as kgeo/equatorial_lensing.py:264-293 evaluates them: photon-orbit radii
+    between the retrograde and prograde circular orbits, their conserved quantities, the
+    screen coordinates, NaN points dropped, the lower half mirrored. Host-side numpy: it is a
+    closed form evaluated once per image, not part of the traced path.
+    """
+    rminus = 2 * (1 + np.cos(2. * np.arccos(-a) / 3.))
+    rplus = 2 * (1 + np.cos(2. * np.arccos(a) / 3.))
+    r = np.linspace(rminus, rplus, n)
+    lam = -(r ** 3 + a ** 2 + r * (a ** 2) - 3 * r ** 2) / (a * r - a)
+    eta = (r ** 2) * (3 * r ** 2 + a ** 2 - lam ** 2) / (r ** 2 - a ** 2)
+    with np.errstate(invalid='ignore'):
+        alpha = -lam / np.sin(th0)
+        beta = np.sqrt(eta + (a * np.cos(th0)) ** 2 - (lam / np.tan(th0)) ** 2)
+    bad = np.isnan(alpha) + np.isnan(beta)
+    alpha = alpha[~bad]
+    beta = beta[~bad]
+    return np.hstack((alpha, np.flip(alpha))), np.hstack((beta, -np.flip(beta)))
+
+
+def critical_band(a, th0, n_angles=4096, n_radii=256, half_width=0.05, n_curve=100000):
+    """Polar band of pixels around the critical curve: n_radii offsets in
+    [-half_width, half_width] M around the curve's radius at n_angles screen angles."""
+    al, be = critical_curve(a, th0, n_curve)
+    ang = np.arctan2(be, al)
+    rad = np.hypot(al, be)
+    order = np.argsort(ang)
+    ang, rad = ang[order], rad[order]
+    phis = np.linspace(-np.pi, np.pi, n_angles, endpoint=False)
+    rc = np.interp(phis, ang, rad, period=2 * np.pi)
+    offs = np.linspace(-half_width, half_width, n_radii)
+    R = rc[None, :] + offs[:, None]
+    return (R * np.cos(phis)[None, :]).flatten(), (R * np.sin(phis)[None, :]).flatten()

@@ -1,6 +1,7 @@
 // Host (g++) build of the device arithmetic headers, for CPU unit checks of the
 // same code the CUDA kernels compile. Test-only: never loaded by the product.
 #include "../../kgeo_gb300/csrc/kg_equatorial.cuh"
+#include "../../kgeo_gb300/csrc/kg_mixed.cuh"
 
 using namespace kg;
 
@@ -63,6 +64,20 @@ void hm_samples_stepped(const double* ob, const double* rec, const int* code, lo
     for (long g0 = 0; g0 < G; g0 += chunk) {
       long g1 = g0 + chunk < G ? g0 + chunk : G;
       ray_chunk(o, f, code[i], g0, g1, G, ordinary_active != 0, false, [&](long g, double tau, const Sample& S) {
+        t[g * n + i] = S.t; r[g * n + i] = S.r; th[g * n + i] = S.th; ph[g * n + i] = S.ph; sig[g * n + i] = S.sig;
+        mino[g * n + i] = tau;
+      });
+    }
+  }
+}
+void hm_samples_mixed(const double* ob, const double* rec, const int* code, long n, long G, long chunk,
+                      int ordinary_active, double* t, double* r, double* th, double* ph, double* sig, double* mino) {
+  Observer o = make_obs(ob);
+  for (long i = 0; i < n; ++i) {
+    RecView f{rec + i, n};
+    for (long g0 = 0; g0 < G; g0 += chunk) {
+      long g1 = g0 + chunk < G ? g0 + chunk : G;
+      ray_chunk_mixed(o, f, code[i], g0, g1, G, ordinary_active != 0, false, [&](long g, double tau, const Sample& S) {
         t[g * n + i] = S.t; r[g * n + i] = S.r; th[g * n + i] = S.th; ph[g * n + i] = S.ph; sig[g * n + i] = S.sig;
         mino[g * n + i] = tau;
       });

@@ -245,3 +245,29 @@ def test_recurrence_matches_independent_samples(kg, chunk):
     assert np.array_equal(h0['mino'], h1['mino'])
     rho = ko.pole_distance(a, 1.e4, th_o, A, B, h0['mino'])
     check_trace(h1, h0, 1.e4, prep.rclass.cpu().numpy(), 'chunk%d' % chunk, rho=rho)
+
+
+@pytest.mark.parametrize('geom', [(0.94, 17.0), (0.3, 70.0), (0.7, 5.0)])
+def test_mixed_precision_error_bars(kg, geom):
+    """Mixed-precision recurrence against the FP64 oracle: r 1e-9, theta 1e-6, phi 2e-6
+    (relative, floor 1), t and sigma 1e-7 of r_o; the horizon-adjacent last sample is
+    checked at the FP64 path's bar (it is evaluated in FP64)."""
+    import torch
+    from oracle import kgeo_oracle as ko
+    from kgeo_gb300 import device as dev
+    from parity import rel_err
+    a, th = geom[0], geom[1] * np.pi / 180
+    x = np.linspace(-10, 10, 40)
+    A, B = (v.flatten() for v in np.meshgrid(x, x))
+    ref = ko.raytrace(a, 1.e4, th, A, B, 256)
+    prep = dev.PreparedRays(a, 1.e4, th, dev.as_device(A), dev.as_device(B), ngeo=256)
+    out = prep.samples(prep.alloc(fill=float('nan')), mixed=True)
+    torch.cuda.synchronize()
+    got = {k: v.cpu().numpy() for k, v in out.items()}
+    assert np.array_equal(np.isfinite(got['ph']), np.isfinite(ref['ph']))
+    last = np.zeros(ref['r'].shape, bool)
+    last[-1] = np.isin(ref['rclass'], (2, 3, 4))
+    for k, rk, scale, bar in (('r', 'r', 1e-300, 1e-9), ('th', 'th', 1.0, 1e-6), ('ph', 'ph', 1.0, 2e-6),
+                              ('t', 't', 1.e4, 1e-7), ('sig', 'affine_times', 1.e4, 1e-7)):
+        e = rel_err(got[k], ref[rk], scale)
+        assert e[~last].max() <= bar, (k, e[~last].max())
