@@ -118,7 +118,8 @@ int kgeo_coords_at_tau(const kgeo_observer* obs, const double* alpha, const doub
  * modified between the two calls. chunk selects the evaluation of the even grid: 0 evaluates
  * every sample independently (Landen + Carlson per sample); k > 0 gives each thread k
  * consecutive samples, the first (and the grid's last) evaluated directly and the rest by
- * the addition theorems of sn/cn/dn, E and Pi from the previous sample (k is capped at 64);
+ * the addition theorems of sn/cn/dn, E and Pi from the previous sample (k is capped at 64,
+ * 256 for KGEO_PRECISION_MIXED);
  * < 0 picks the library default. Caller-given tau always uses independent evaluation.
  * precision: KGEO_PRECISION_FP64 or KGEO_PRECISION_MIXED (the latter for the recurrence). */
 int kgeo_ray_setup(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix, int32_t ngeo,

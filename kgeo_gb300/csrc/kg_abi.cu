@@ -92,7 +92,10 @@ int samples_common(const kgeo_observer* obs, const Workspace& w, int64_t npix, i
     pa.nsamp = nsamp;
     pa.tau = tau;
     pa.do_phi_t = do_phi_t;
-    pa.chunk = chunk < 0 ? DEFAULT_CHUNK : (chunk > MAX_CHUNK ? MAX_CHUNK : chunk);
+    if (mixed)
+      pa.chunk = chunk < 0 ? DEFAULT_CHUNK_MIXED : (chunk > MAX_CHUNK_MIXED ? MAX_CHUNK_MIXED : chunk);
+    else
+      pa.chunk = chunk < 0 ? DEFAULT_CHUNK : (chunk > MAX_CHUNK ? MAX_CHUNK : chunk);
     pa.perm = w.perm;
     pa.mixed = mixed;
     pa.flags = w.flags;

@@ -28,6 +28,22 @@ KG_HD double kg_nan() { return __builtin_nan(""); }
 
 KG_HD double sq(double x) { return x * x; }
 
+// 1/x to FP64 working accuracy (not correctly rounded): the hardware reciprocal
+// approximation refined by two Newton steps. For the recurrence's normalisations, where the
+// last-bit rounding of an IEEE divide carries no meaning; |x| must be a normal number.
+KG_HD double rcp_fast(double x) {
+#if defined(__CUDA_ARCH__)
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+#else
+  return 1.0 / x;
+#endif
+}
+
 KG_HD float rsqrt_f(float x) {
 #if defined(__CUDA_ARCH__)
   return rsqrtf(x);

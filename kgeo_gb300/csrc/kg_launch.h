@@ -114,6 +114,10 @@ struct CrossingArgs {
 // accumulate more rounding: 64 keeps every output within the FP64 parity bars).
 constexpr int DEFAULT_CHUNK = 50;
 constexpr int MAX_CHUNK = 64;
+// The mixed recurrence accumulates FP32 increments into FP64 sums, so its chains may be
+// longer: the chunk-start evaluation is amortised over more samples.
+constexpr int DEFAULT_CHUNK_MIXED = 128;
+constexpr int MAX_CHUNK_MIXED = 256;
 
 cudaError_t launch_ray_setup(const SetupArgs& a, cudaStream_t s);
 cudaError_t launch_equatorial(const EquatorialArgs& a, cudaStream_t s);

@@ -15,10 +15,18 @@
 
 namespace kg {
 
+KG_HD float __frcp_rn_compat(float x) {
+#if defined(__CUDA_ARCH__)
+  return __frcp_rn(x);
+#else
+  return 1.0f / x;
+#endif
+}
+
 // Pi increment of one step in FP32 (see pi_add_term for the formula); X is formed in FP64
 // by the caller (it cancels near a pole) and handed over rounded.
 KG_HD float pi_add_term_f(float n, float c, float X, float S3) {
-  float iX = 1.0f / X;
+  float iX = __frcp_rn_compat(X);
   float t = S3 * iX;
   float z2 = c * (t * t);
   if (X > 0.0f && fabsf(z2) < 2.0e-2f) return n * t * rc_one_f(-z2);
@@ -90,7 +98,8 @@ KG_HD ThetaState theta_state_direct_mixed(const FV& f, int code, double snarg) {
   return st;
 }
 
-// Direct r state with FP64 Jacobi functions and FP32 integrals.
+// Direct r state with FP64 Jacobi functions; the integrals in FP32 except those the ray's
+// error budget flags (code bits), which get an FP64 Carlson evaluation of their own.
 template <class FV>
 KG_HD RadialState radial_state_direct_mixed(const FV& f, int code, double X) {
   RadialState st;
@@ -104,23 +113,44 @@ KG_HD RadialState radial_state_direct_mixed(const FV& f, int code, double X) {
   st.cn = odd * J.cn;
   st.dn = J.dn;
   st.am = 0.0;
-  double s2r = J.sn * J.sn;
+  const double s2r = J.sn * J.sn, c2r = J.cn * J.cn, d2r = J.dn * J.dn;
   const double nn[3] = {f[R_N0], f[R_N1], f[R_N2]};
-  float rho[3];
+  double rho[3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) rho[i] = (float)(nn[i] < 1.0 ? (1.0 - nn[i]) + nn[i] * (J.cn * J.cn) : 1.0 - nn[i] * s2r);
-  float rj[3], rd, rf;
-  carlson_set_f<3>((float)(J.cn * J.cn), (float)(J.dn * J.dn), 1.0f, rho, rj, &rd, &rf);
-  double sn3 = J.sn * J.sn * J.sn;
-  double Finc = J.sn * (double)rf;
-  double Einc = Finc - (k / 3.0) * sn3 * (double)rd;
-  st.E = nr == 0.0 ? Einc : Einc + 2.0 * nr * f[R_EC];
+  for (int i = 0; i < 3; ++i) rho[i] = nn[i] < 1.0 ? (1.0 - nn[i]) + nn[i] * c2r : 1.0 - nn[i] * s2r;
+  const double sn3 = J.sn * J.sn * J.sn;
   const double pic[3] = {f[R_PIC0], f[R_PIC1], f[R_PIC2]};
+  int nflag = 0, which = 0;
 #pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    double inc = Finc + (nn[i] / 3.0) * sn3 * (double)rj[i];
-    st.P[i] = nr == 0.0 ? inc : 2.0 * nr * pic[i] + inc;
+  for (int i = 0; i < 3; ++i)
+    if (code_f64(code, 1 + i)) ++nflag, which = i;
+  double P[3], E;
+  if (nflag >= 2) {
+    double rj[3], rd, rf;
+    carlson_set<3>(c2r, d2r, 1.0, rho, rj, &rd, &rf);
+    double Finc = J.sn * rf;
+    E = Finc - (k / 3.0) * sn3 * rd;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) P[i] = Finc + (nn[i] / 3.0) * sn3 * rj[i];
+  } else {
+    float rho32[3] = {(float)rho[0], (float)rho[1], (float)rho[2]};
+    float rj[3], rd, rf;
+    carlson_set_f<3>((float)c2r, (float)d2r, 1.0f, rho32, rj, &rd, &rf);
+    double Finc = J.sn * (double)rf;
+    E = Finc - (k / 3.0) * sn3 * (double)rd;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) P[i] = Finc + (nn[i] / 3.0) * sn3 * (double)rj[i];
+    if (nflag == 1 || code_f64(code, 4)) {
+      double rj1, rd1, rf1;
+      carlson_set<1>(c2r, d2r, 1.0, &rho[which], &rj1, &rd1, &rf1);
+      double F64 = J.sn * rf1;
+      if (nflag == 1) P[which] = F64 + (nn[which] / 3.0) * sn3 * rj1;
+      if (code_f64(code, 4)) E = F64 - (k / 3.0) * sn3 * rd1;
+    }
   }
+  st.E = nr == 0.0 ? E : E + 2.0 * nr * f[R_EC];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) st.P[i] = nr == 0.0 ? P[i] : 2.0 * nr * pic[i] + P[i];
   return st;
 }
 
@@ -311,7 +341,7 @@ KG_HD void ray_chunk_mixed(const Observer& ob, const FV& f, int code, int64_t g0
     ray_chunk(ob, f, code, g0, g1, G, ordinary_active, step_zero, emit);
     return;
   }
-  const double taumax = f[F_TAUMAX];
+  const EvenGrid grid(f[F_TAUMAX], G, step_zero);
   const bool thact = theta_active(f, code, ordinary_active);
   ThetaState ts;
   RadialState rs;
@@ -319,7 +349,7 @@ KG_HD void ray_chunk_mixed(const Observer& ob, const FV& f, int code, int64_t g0
   rs.X = rs.sn = rs.cn = rs.dn = rs.E = rs.am = 0.0;
   rs.P[0] = rs.P[1] = rs.P[2] = 0.0;
   for (int64_t g = g0; g < g1; ++g) {
-    const double tau = linspace_at(g, G, taumax, step_zero);
+    const double tau = grid.at(g);
     const double X = radial_X(f, tau);
     bool fp64 = (g == G - 1);  // the horizon-adjacent sample
     ThetaOut T{0.0, 0.0, 0.0};
@@ -328,10 +358,15 @@ KG_HD void ray_chunk_mixed(const Observer& ob, const FV& f, int code, int64_t g0
       if (thact) ts = theta_state_direct(f, code, theta_snarg(f, tau));
       rs = radial_state_direct(f, code, X, true);
     } else if (g == g0) {
-      // chunk start: FP64 direct evaluation (its integrals seed the FP64 accumulators)
-      if (thact) ts = theta_state_direct(f, code, theta_snarg(f, tau));
-      rs = radial_state_direct(f, code, X, true);
-      fp64 = (thact && theta_near_pole(f, ts.sn)) || radial_near_pole(f, rs.sn);
+      // chunk start: FP64 Jacobi functions; integrals in FP32 unless the error budget or a
+      // nearby Pi pole asks for FP64
+      if (thact) {
+        ts = code_f64(code, 0) ? theta_state_direct(f, code, theta_snarg(f, tau))
+                               : theta_state_direct_mixed(f, code, theta_snarg(f, tau));
+        if (theta_near_pole(f, ts.sn)) ts = theta_state_direct(f, code, theta_snarg(f, tau)), fp64 = true;
+      }
+      rs = radial_state_direct_mixed(f, code, X);
+      if (radial_near_pole(f, rs.sn)) rs = radial_state_direct(f, code, X, true), fp64 = true;
     } else {
       if (thact && !theta_step_mixed(f, code, &ts)) ts = theta_state_direct(f, code, theta_snarg(f, tau)), fp64 = true;
       if (!radial_step_mixed(f, code, &rs, X)) rs = radial_state_direct(f, code, X, true), fp64 = true;

@@ -638,7 +638,7 @@ struct JacobiW {
 
 // sn, cn, dn(u + v | m) from the values at u and v (DLMF 22.8.1-3), any real m.
 KG_HD JacobiW jacobi_add(double snu, double cnu, double dnu, double snv, double cnv, double dnv, double m) {
-  double inv = 1.0 / (1.0 - m * (snu * snu) * (snv * snv));
+  double inv = rcp_fast(1.0 - m * (snu * snu) * (snv * snv));
   JacobiW w;
   w.sn = (snu * cnv * dnv + snv * cnu * dnu) * inv;
   w.cn = (cnu * cnv - snu * snv * dnu * dnv) * inv;
@@ -664,7 +664,7 @@ KG_HD bool near_pi_pole(double n, double sn) { return n > 0.0 && fabs(1.0 - n * 
 KG_HD double pi_add_term(double n, double c, double snu, double snv, const JacobiW& w) {
   double S3 = snu * snv * w.sn;
   double X = 1.0 - n * (w.sn * w.sn) + n * snu * snv * w.cn * w.dn;
-  double iX = 1.0 / X;
+  double iX = rcp_fast(X);
   double t = S3 * iX;
   double z2 = c * (t * t);
   if (X > 0.0 && fabs(z2) < 2.0e-3) return n * t * rc_one(-z2);
@@ -1005,6 +1005,22 @@ KG_HD double linspace_at(int64_t g, int64_t G, double stop, bool any_step_zero) 
   return (double)g * (stop / div) + 0.0;
 }
 
+// The even grid with its step computed once (same arithmetic as linspace_at).
+struct EvenGrid {
+  double stop, step, div;
+  int64_t G;
+  bool step_zero;
+  KG_HD EvenGrid(double stop_, int64_t G_, bool step_zero_)
+      : stop(stop_), step(G_ > 1 ? stop_ / (double)(G_ - 1) : 0.0), div((double)(G_ - 1)), G(G_),
+        step_zero(step_zero_) {}
+  KG_HD double at(int64_t g) const {
+    if (G == 1) return 0.0 * stop + 0.0;
+    if (g == G - 1) return stop;
+    if (step_zero) return ((double)g / div) * stop + 0.0;
+    return (double)g * step + 0.0;
+  }
+};
+
 // All five coordinates at Mino time tau by direct evaluation.
 template <class FV>
 KG_HD Sample sample_all(const Observer& ob, const FV& f, int code, double tau, bool ordinary_active) {
@@ -1019,7 +1035,7 @@ KG_HD Sample sample_all(const Observer& ob, const FV& f, int code, double tau, b
 template <class FV, class Emit>
 KG_HD void ray_chunk(const Observer& ob, const FV& f, int code, int64_t g0, int64_t g1, int64_t G,
                      bool ordinary_active, bool step_zero, Emit emit) {
-  const double taumax = f[F_TAUMAX];
+  const EvenGrid grid(f[F_TAUMAX], G, step_zero);
   const bool thact = theta_active(f, code, ordinary_active);
   const bool stepping = code_step(code);
   const bool rdo = code_rcase(code) != RCASE_NONE;
@@ -1029,7 +1045,7 @@ KG_HD void ray_chunk(const Observer& ob, const FV& f, int code, int64_t g0, int6
   rs.X = rs.sn = rs.cn = rs.dn = rs.E = rs.am = 0.0;
   rs.P[0] = rs.P[1] = rs.P[2] = 0.0;
   for (int64_t g = g0; g < g1; ++g) {
-    const double tau = linspace_at(g, G, taumax, step_zero);
+    const double tau = grid.at(g);
     const double X = radial_X(f, tau);
     if (g == g0 || g == G - 1 || !stepping) {
       if (thact) ts = theta_state_direct(f, code, theta_snarg(f, tau));
