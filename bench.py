@@ -463,19 +463,189 @@ def run_mixed(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------
+# configuration 5: differentiable equatorial image (image + gradient per step)
+# ---------------------------------------------------------------------------
+
+IMG_GRID = 512
+IMG_LIM = 8.0
+IMG_PHYS = (0.5, 60 * np.pi / 180, 2.0, 0.8, 0.5)   # a, theta_o, p, xi, beta_r
+IMG_MBAR = 2
+# FP64 FLOP per pixel of the adjoint kernel on this workload (all three orders), from the
+# ncu capture summarised in profiles/image_adjoint_config5.md: (dadd + dmul + 2 dfma
+# thread instructions) / pixels. Used for roofline.achieved.
+ADJ_FLOP_PER_PIXEL = 29170
+CPU_IMG_SAMPLE = 65536       # pixels of the bounded CPU sample (every 4th pixel)
+
+
+def image_workload(grid=IMG_GRID):
+    x = np.linspace(-IMG_LIM, IMG_LIM, grid)
+    A, B = np.meshgrid(x, x)
+    eps = np.random.default_rng(0).choice([-1.0, 1.0], size=5)
+    return A.flatten(), B.flatten(), np.array(IMG_PHYS), np.array(IMG_PHYS) * (1 + 0.02 * eps)
+
+
+def _cpu_image_chunk(args):
+    """Oracle image at the parameters and at +-1e-6 in each of the five (the central
+    differences a CPU user of the reference computes for the gradient), and the loss."""
+    A, B, phys, tgt = args
+    from oracle import kgeo_oracle as ko
+    import warnings
+    warnings.filterwarnings('ignore')
+
+    def img(ph):
+        return ko.make_image_px(float(ph[0]), R_O, float(ph[1]), IMG_MBAR, A, B,
+                                emis=('bpl', {'p1': -ph[2], 'p2': 0.0}),
+                                vel=('general', {'fac_subkep': ph[3], 'beta_r': ph[4]}))['I']
+    target = img(tgt)
+    L = ((img(phys) - target) ** 2).sum()
+    for k in range(5):
+        for sgn in (1, -1):
+            q = phys.copy()
+            q[k] += sgn * 1e-6
+            ((img(q) - target) ** 2).sum()
+    return L
+
+
+def cpu_image_run(pool, cores):
+    A, B, phys, tgt = image_workload()
+    idx = np.arange(0, A.size, A.size // CPU_IMG_SAMPLE)[:CPU_IMG_SAMPLE]
+    chunks = np.array_split(idx, cores * 2)
+    t0 = time.time()
+    pool.map(_cpu_image_chunk, [(A[c], B[c], phys, tgt) for c in chunks])
+    dt = time.time() - t0
+    return {'value': (idx.size / A.size) / dt, 'unit': 'image+grad/s', 'cores': cores, 'kind': 'port',
+            'sample': '%d pixels (every %dth of the 512x512 image), 3 orders, image + 10 central-difference '
+                      'images + target; oracle/kgeo_oracle.py on a %d-process pool, %.1f s wall, scaled to the '
+                      'full image' % (idx.size, A.size // CPU_IMG_SAMPLE, cores, dt)}
+
+
+def run_image(args):
+    small = args.case == 'image-small'
+    pool = cores = None
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()
+    import torch
+    from kgeo_gb300.image_grad import config_params, equatorial_image
+    grid = 128 if small else IMG_GRID
+    A, B, phys, tgt = image_workload(grid)
+    npix = A.size
+    al = torch.from_numpy(A).cuda()
+    be = torch.from_numpy(B).cuda()
+    with torch.no_grad():
+        target = equatorial_image(config_params(*tgt), al, be, mbar_max=IMG_MBAR)
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def step(al_, be_):
+        xs = [torch.tensor(v, dtype=torch.float64, requires_grad=True) for v in phys]
+        I = equatorial_image(config_params(*xs), al_, be_, mbar_max=IMG_MBAR)
+        L = ((I - target) ** 2).sum()
+        L.backward()
+        return L, xs
+
+    for _ in range(args.warmup):
+        step(al, be)
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(args.steps):
+        L, xs = step(al, be)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    t_step = e0.elapsed_time(e1) / 1e3 / args.steps
+    grad = [float(x.grad) for x in xs]
+    # per-kernel times on the launching stream
+    from kgeo_gb300.equatorial_images import emission_model, image_adjoint_device, image_device
+    from kgeo_gb300.emissivities import Emissivity
+    from kgeo_gb300.velocities import Velocity
+    model = emission_model(Emissivity('bpl', p1=-phys[2], p2=0.0),
+                           Velocity('general', fac_subkep=phys[3], beta_r=phys[4]))
+    gI = torch.ones((npix, IMG_MBAR + 1), dtype=torch.float64, device=al.device)
+
+    def kt(fn, n=5):
+        fn()
+        torch.cuda.synchronize()
+        a0, a1 = ev(), ev()
+        a0.record(stream)
+        for _ in range(n):
+            fn()
+        a1.record(stream)
+        torch.cuda.synchronize()
+        return a0.elapsed_time(a1) / 1e3 / n
+    t_fwd = kt(lambda: image_device(phys[0], R_O, phys[1], 0, IMG_MBAR + 1, al, be, model))
+    t_adj = kt(lambda: image_adjoint_device(phys[0], R_O, phys[1], 0, IMG_MBAR + 1, al, be, model, gI))
+    # end to end: host pixel arrays in, loss and gradient out, through the public API
+    Ah = torch.from_numpy(A).pin_memory()
+    Bh = torch.from_numpy(B).pin_memory()
+    for _ in range(2):
+        step(Ah.cuda(non_blocking=True), Bh.cuda(non_blocking=True))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L, xs = step(Ah.cuda(non_blocking=True), Bh.cuda(non_blocking=True))
+        out = (float(L.detach()), [float(x.grad) for x in xs])
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    pk = peaks()
+    fp64_peak = None
+    try:
+        from kgeo_gb300 import device as dev
+        fp64_peak = dev.fp64_peak_tflops()
+    except Exception:
+        pass
+    roof = {'bound': 'fp64', 'unit': 'TFLOP/s', 'kernel': 'image_adjoint_kernel', 'launch_ms': t_adj * 1e3,
+            'peak': fp64_peak, 'peak_source': 'FP64 FMA loop measured live by bench.py (kgeo_measure_fp64_peak)',
+            'achieved': None, 'frac': None, 'fp64_flop_per_pixel': ADJ_FLOP_PER_PIXEL,
+            # ncu dram__bytes_read + write of the 128x128 capture scaled by pixels (inputs and
+            # grad_I are read once; the per-block partial sums are the only writes)
+            'traffic': (3.674e6 + 4.1e3) * npix / 16384}
+    if ADJ_FLOP_PER_PIXEL and fp64_peak:
+        roof['achieved'] = ADJ_FLOP_PER_PIXEL * npix / t_adj / 1e12
+        roof['frac'] = roof['achieved'] / fp64_peak
+    cpu = cpu_image_run(pool, cores) if pool is not None else None
+    if pool is not None:
+        pool.close()
+    line = {
+        'metric': 'image+grad/s: configuration-5 equatorial image (512x512, n=0..2) + adjoint gradient wrt '
+                  '(a, theta_o, p, xi, beta_r)',
+        'value': 1.0 / t_step, 'unit': 'image+grad/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': t_step * 1e3, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f64', 'data': 'synthetic: uniform image-plane grid; target image at parameters x (1 + 0.02 eps), '
+                                'eps = +-1 from default_rng(0)',
+        'config': {'workload': 'configuration 5: a=0.5, theta_o=60 deg, r_o=1e4, %dx%d over [-8, 8] M, orders '
+                               '0..2, bpl j ~ r^-2, general velocity xi=0.8 beta_r=0.5' % (grid, grid),
+                   'npix': npix, 'orders': IMG_MBAR + 1, 'case': args.case,
+                   'l2': 'inputs 4 MB (compute-bound kernels; not flushed)'},
+        'loss': out[0], 'grad': out[1], 'pixels_per_s': npix / t_step,
+        'kernel_ms': {'image': t_fwd * 1e3, 'image_adjoint': t_adj * 1e3},
+        'roofline': roof, 'cpu_baseline': cpu,
+        'e2e': {'value': 1.0 / t_e2e, 'unit': 'image+grad/s', 'h2d_bytes_per_step': 2 * 8 * npix,
+                'd2h_bytes_per_step': 8 * 6, 'ms_per_step': t_e2e * 1e3,
+                'path': 'kgeo_gb300.image_grad.equatorial_image (torch.autograd.Function) from pinned host arrays'},
+        'gpu_launches': 3 * args.steps, 'clocks': ck,
+    }
+    print(json.dumps(line))
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument('--gpus', type=int, default=1)
     p.add_argument('--steps', type=int, default=5)
     p.add_argument('--warmup', type=int, default=3)
     p.add_argument('--impl', choices=('ours', 'reference'), default='ours')
-    p.add_argument('--case', choices=('full', 'small', 'mixed', 'mixed-small'), default='full')
+    p.add_argument('--case', choices=('full', 'small', 'mixed', 'mixed-small', 'image', 'image-small'),
+                   default='full')
     p.add_argument('--no-cpu-baseline', action='store_true')
     args = p.parse_args()
     if args.impl == 'reference':
         run_reference(args)
     elif args.case.startswith('mixed'):
         run_mixed(args)
+    elif args.case.startswith('image'):
+        run_image(args)
     else:
         run_ours(args)
 

@@ -146,6 +146,65 @@ int kgeo_equatorial_crossings(const kgeo_observer* obs, const double* alpha, con
                               const double* tau, int32_t ntau, double* n_eq, double* n_pol,
                               double* outside_crit, void* stream);
 
+/* Emission model of an unpolarised equatorial image: Emissivity(emistype, **kwargs)
+ * (kgeo/emissivities.py:38-72) and Velocity(veltype, **kwargs) (kgeo/velocities.py:23-67)
+ * restricted to the models below, plus Iobs' specind and sin(theta_B)
+ * (kgeo/equatorial_images.py:17-20). */
+#define KGEO_EMIS_BPL 0        /* emisBPL: exp(p1 ln(r/r_h) + p2 ln^2(r/r_h)) */
+#define KGEO_EMIS_CONSTANT 1   /* 1 */
+#define KGEO_EMIS_GLM 2        /* emisGLM with mu = 1 - sqrt(1 - a^2) */
+#define KGEO_EMIS_RING 3       /* emisGLM with mu = mu_ring (0: as GLM) */
+#define KGEO_VEL_ZAMO 0
+#define KGEO_VEL_INFALL 1
+#define KGEO_VEL_KEP 2         /* 'kep' / 'cunningham' */
+#define KGEO_VEL_SUBKEP 3      /* 'subkep' / 'cunningham_subkep' */
+#define KGEO_VEL_GENERAL 4
+typedef struct {
+  int32_t emissivity;   /* KGEO_EMIS_* */
+  int32_t velocity;     /* KGEO_VEL_* */
+  int32_t retrograde;   /* kep / subkep / general */
+  int32_t reserved;
+  double emis_p[2];     /* bpl: (p1, p2); glm / ring: (gamma_off, sigma) */
+  double mu_ring;       /* ring: r_ring */
+  double vel_p[3];      /* subkep: (fac_subkep); general: (fac_subkep, beta_phi, beta_r), each in [0, 1] */
+  double emiscut_in;    /* pixels with r_s < emiscut_in are dark when emiscut_in > 0 */
+  double emiscut_out;   /* pixels with r_s > emiscut_out are dark when emiscut_out > 0 */
+  double specind;       /* spectral index (1 in make_image) */
+  double sinthb;        /* sin(theta_B) of the unpolarised image (pi/4 in the reference) */
+} kgeo_emission;
+
+/* Outputs of kgeo_image. Per-order arrays are (npix, n_orders) row-major, the layout of
+ * make_image's outarr_*; I is required, every other pointer may be NULL. */
+typedef struct {
+  double* I;        /* observed intensity g^2 j g^specind sin(theta_B)^(1 + specind), 0 where masked */
+  double* g;        /* redshift factor, 0 where masked */
+  double* r_s;      /* emission radius (r_equatorial's r_s) */
+  double* Ir;       /* Mino time of the crossing (make_image's outarr_t) */
+  double* sinthb;   /* sin(theta_B) where lit, else 0 */
+  double* imax;     /* (npix) Imax, the total Mino time (Iobs' Imax) */
+  double* nmax;     /* (npix) Nmax, make_image's outarr_n */
+  double* npol;     /* (npix) nmax_poloidal, make_image's outarr_np */
+} kgeo_image_out;
+
+/* make_image(a, r_o, th_o, mbar_max, ...) with polarization=False, pathlength=False
+ * (kgeo/equatorial_images.py:23-122; per order Iobs, :124-264) on the caller's pixels
+ * (alpha, beta), for the orders mbar = mbar_lo .. mbar_lo + n_orders - 1 in one pass over the
+ * pixels (make_image: mbar_lo = 0, n_orders = mbar_max + 1; Iobs: one order). Q and U of the
+ * reference are zero in this mode and are not produced. */
+int kgeo_image(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha, const double* beta,
+               int64_t npix, const kgeo_emission* model, kgeo_image_out* out, void* stream);
+
+/* Adjoint of kgeo_image's I (no counterpart in the reference): given grad_I = dL/dI
+ * (npix, n_orders) for the orders mbar_lo .. mbar_lo + n_orders - 1, writes grad[7] = dL/dq for q = (a, th_o, emis_p[0], emis_p[1],
+ * vel_p[0], vel_p[1], vel_p[2]) to device memory. Masks, the momentum signs and Nmax are
+ * held fixed (they are piecewise constant); the geodesic is recomputed, not stored.
+ * workspace: device scratch of kgeo_image_adjoint_workspace_size(npix) bytes. Deterministic:
+ * per-block partial sums are added in a fixed order. */
+size_t kgeo_image_adjoint_workspace_size(int64_t npix);
+int kgeo_image_adjoint(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha,
+                       const double* beta, int64_t npix, const kgeo_emission* model, const double* grad_I, double* grad,
+                       void* workspace, size_t workspace_bytes, void* stream);
+
 /* Allocation-free kgeo_raytrace. No counterpart in the reference: it exists for callers
  * that may not allocate device memory when they call in — an application that owns all
  * device memory under a fixed budget, a latency-critical loop that cannot afford an

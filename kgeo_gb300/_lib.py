@@ -26,6 +26,23 @@ class GeodesicsOut(ctypes.Structure):
                 ('flags', c_void_p)]
 
 
+class Emission(ctypes.Structure):
+    """kgeo_emission."""
+    _fields_ = [('emissivity', c_int32), ('velocity', c_int32), ('retrograde', c_int32), ('reserved', c_int32),
+                ('emis_p', c_double * 2), ('mu_ring', c_double), ('vel_p', c_double * 3),
+                ('emiscut_in', c_double), ('emiscut_out', c_double), ('specind', c_double), ('sinthb', c_double)]
+
+
+class ImageOut(ctypes.Structure):
+    """kgeo_image_out."""
+    _fields_ = [('I', c_void_p), ('g', c_void_p), ('r_s', c_void_p), ('Ir', c_void_p), ('sinthb', c_void_p),
+                ('imax', c_void_p), ('nmax', c_void_p), ('npol', c_void_p)]
+
+
+EMIS = {'bpl': 0, 'constant': 1, 'glm': 2, 'ring': 3}
+VEL = {'zamo': 0, 'infall': 1, 'kep': 2, 'cunningham': 2, 'subkep': 3, 'cunningham_subkep': 3, 'general': 4}
+N_IMAGE_PARAMS = 7  # a, th_o, emis_p[0..1], vel_p[0..2]
+
 # name -> (restype, argtypes); kept in step with include/kgeo_gb300.h
 SIGNATURES = {
     'kgeo_workspace_size': (c_size_t, [c_int64]),
@@ -46,6 +63,11 @@ SIGNATURES = {
                                   c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     'kgeo_equatorial_crossings': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_void_p, c_int32,
                                           c_void_p, c_void_p, c_void_p, c_void_p]),
+    'kgeo_image': (c_int, [ctypes.POINTER(Observer), c_int32, c_int32, c_void_p, c_void_p, c_int64,
+                           ctypes.POINTER(Emission), ctypes.POINTER(ImageOut), c_void_p]),
+    'kgeo_image_adjoint_workspace_size': (c_size_t, [c_int64]),
+    'kgeo_image_adjoint': (c_int, [ctypes.POINTER(Observer), c_int32, c_int32, c_void_p, c_void_p, c_int64,
+                                   ctypes.POINTER(Emission), c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     'kgeo_status_string': (ctypes.c_char_p, [c_int]),
     'kgeo_abi_version': (c_int, []),
 }

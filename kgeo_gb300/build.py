@@ -22,6 +22,7 @@ COMMON = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-I', os.path
 # follow numpy's one-operation-at-a-time arithmetic.
 UNITS = [
     ('kg_setup.cu', ['-fmad=false']),
+    ('kg_image.cu', ['-fmad=false']),
     ('kg_samples.cu', []),
     ('kg_abi.cu', []),
     ('kg_peak.cu', []),

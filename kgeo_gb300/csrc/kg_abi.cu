@@ -132,6 +132,29 @@ int trace_common(const kgeo_observer* obs, const double* alpha, const double* be
   return samples_common(obs, w, npix, nsamp, tau, do_phi_t, -1, mixed, out, s);
 }
 
+// Emission model with the reference's parameter checks (kgeo/velocities.py:315-317,
+// 446-451: fac_subkep, beta_phi, beta_r in [0, 1]).
+int make_model(const kgeo_emission* m, EmissionModel* out) {
+  if (!m) return KGEO_ERR_NULL;
+  if (m->emissivity < KGEO_EMIS_BPL || m->emissivity > KGEO_EMIS_RING) return KGEO_ERR_MODEL;
+  if (m->velocity < KGEO_VEL_ZAMO || m->velocity > KGEO_VEL_GENERAL) return KGEO_ERR_MODEL;
+  const int nv = m->velocity == KGEO_VEL_SUBKEP ? 1 : (m->velocity == KGEO_VEL_GENERAL ? 3 : 0);
+  for (int k = 0; k < nv; ++k)
+    if (!(m->vel_p[k] >= 0 && m->vel_p[k] <= 1)) return KGEO_ERR_MODEL;
+  out->emis = m->emissivity;
+  out->vel = m->velocity;
+  out->retrograde = m->retrograde != 0;
+  for (int k = 0; k < 2; ++k) out->emis_p[k] = m->emis_p[k];
+  for (int k = 0; k < 3; ++k) out->vel_p[k] = m->vel_p[k];
+  out->mu_ring = m->mu_ring;
+  out->emiscut_in = m->emiscut_in;
+  out->emiscut_out = m->emiscut_out;
+  out->specind = m->specind;
+  out->sinthb = m->sinthb;
+  out->sinthb_pow = std::pow(m->sinthb, 1 + m->specind);
+  return KGEO_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -180,6 +203,63 @@ int kgeo_r_equatorial(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_order
   ea.Imax = Imax;
   ea.Nmax = Nmax;
   return launch_equatorial(ea, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
+}
+
+int kgeo_image(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha, const double* beta,
+               int64_t npix, const kgeo_emission* model, kgeo_image_out* out, void* stream) {
+  int st = check_observer(obs);
+  if (st) return st;
+  if (mbar_lo < 0 || n_orders < 1) return KGEO_ERR_MBAR;
+  if (npix < 0) return KGEO_ERR_LENGTHS;
+  ImageArgs ia;
+  st = make_model(model, &ia.model);
+  if (st) return st;
+  if (!out) return KGEO_ERR_NULL;
+  if (npix > 0 && (!alpha || !beta || !out->I)) return KGEO_ERR_NULL;
+  ia.obs = make_observer(obs);
+  ia.alpha = alpha;
+  ia.beta = beta;
+  ia.npix = npix;
+  ia.mbar_lo = mbar_lo;
+  ia.nord = n_orders;
+  ia.I = out->I;
+  ia.g = out->g;
+  ia.r_s = out->r_s;
+  ia.Ir = out->Ir;
+  ia.sinthb = out->sinthb;
+  ia.imax = out->imax;
+  ia.nmax = out->nmax;
+  ia.npol = out->npol;
+  return launch_image(ia, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
+}
+
+size_t kgeo_image_adjoint_workspace_size(int64_t npix) {
+  return (size_t)(npix > 0 ? image_adjoint_blocks(npix) : 0) * NQ * sizeof(double);
+}
+
+int kgeo_image_adjoint(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha,
+                       const double* beta, int64_t npix, const kgeo_emission* model, const double* grad_I,
+                       double* grad, void* workspace, size_t workspace_bytes_, void* stream) {
+  int st = check_observer(obs);
+  if (st) return st;
+  if (mbar_lo < 0 || n_orders < 1) return KGEO_ERR_MBAR;
+  if (npix < 0) return KGEO_ERR_LENGTHS;
+  ImageAdjointArgs aa;
+  st = make_model(model, &aa.model);
+  if (st) return st;
+  if (!grad) return KGEO_ERR_NULL;
+  if (npix > 0 && (!alpha || !beta || !grad_I || !workspace)) return KGEO_ERR_NULL;
+  if (workspace_bytes_ < kgeo_image_adjoint_workspace_size(npix)) return KGEO_ERR_WORKSPACE;
+  aa.obs = make_observer(obs);
+  aa.alpha = alpha;
+  aa.beta = beta;
+  aa.npix = npix;
+  aa.mbar_lo = mbar_lo;
+  aa.nord = n_orders;
+  aa.grad_I = grad_I;
+  aa.partial = static_cast<double*>(workspace);
+  aa.grad = grad;
+  return launch_image_adjoint(aa, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
 }
 
 int kgeo_equatorial_crossings(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,

@@ -4,7 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
-#include "kg_equatorial.cuh"
+#include "kg_image.cuh"
 
 namespace kg {
 
@@ -119,7 +119,46 @@ constexpr int MAX_CHUNK = 64;
 constexpr int DEFAULT_CHUNK_MIXED = 128;
 constexpr int MAX_CHUNK_MIXED = 256;
 
+// Equatorial image of orders mbar_lo .. mbar_lo + nord - 1 (kg_image.cuh); outputs are
+// (npix, nord) row-major.
+struct ImageArgs {
+  Observer obs;
+  EmissionModel model;
+  const double* alpha;
+  const double* beta;
+  int64_t npix;
+  int mbar_lo;
+  int nord;
+  double* I;
+  double* g;
+  double* r_s;
+  double* Ir;
+  double* sinthb;
+  double* imax;   // (npix)
+  double* nmax;   // (npix)
+  double* npol;   // (npix)
+};
+
+// Adjoint of the image: sum over pixels and orders of grad_I * dI/dq for the NQ parameters.
+struct ImageAdjointArgs {
+  Observer obs;
+  EmissionModel model;
+  const double* alpha;
+  const double* beta;
+  int64_t npix;
+  int mbar_lo;
+  int nord;
+  const double* grad_I;  // (npix, nord)
+  double* partial;       // (blocks, NQ) per-block sums
+  double* grad;          // (NQ)
+};
+
+constexpr int IMAGE_BLOCK = 128;
+KG_HD constexpr int64_t image_adjoint_blocks(int64_t npix) { return (npix + IMAGE_BLOCK - 1) / IMAGE_BLOCK; }
+
 cudaError_t launch_ray_setup(const SetupArgs& a, cudaStream_t s);
+cudaError_t launch_image(const ImageArgs& a, cudaStream_t s);
+cudaError_t launch_image_adjoint(const ImageAdjointArgs& a, cudaStream_t s);
 cudaError_t launch_equatorial(const EquatorialArgs& a, cudaStream_t s);
 cudaError_t launch_crossings(const CrossingArgs& a, cudaStream_t s);
 cudaError_t launch_samples(const SampleArgs& a, cudaStream_t s);

@@ -804,6 +804,46 @@ def r_isco(a, s=1):
     return 3 + z2 - s * np.sqrt((3 - z1) * (3 + z1 + 2 * z2))
 
 
+def u_zamo(a, r):
+    """Zero-angular-momentum observer at th = pi/2; kgeo/velocities.py:180-206."""
+    th = np.pi / 2.
+    Delta = r ** 2 - 2 * r + a ** 2
+    Sigma = r ** 2 + a ** 2 * np.cos(th) ** 2
+    g00 = -(1 - 2 * r / Sigma)
+    g33 = (r ** 2 + a ** 2 + 2 * r * (a * np.sin(th)) ** 2 / Sigma) * np.sin(th) ** 2
+    g03 = -2 * r * a * np.sin(th) ** 2 / Sigma
+    v3 = -g03 / g33
+    u0 = np.sqrt(-1. / (g00 + 2 * g03 * v3 + g33 * v3 * v3))
+    return u0, 0 * r, 0, u0 * v3
+
+
+def u_kep(a, r, retrograde=False):
+    """Cunningham: Keplerian outside the ISCO, plunging inside; kgeo/velocities.py:229-281."""
+    s = -1 if retrograde else 1
+    ri = r_isco(a, s)
+    u0 = np.zeros(r.shape)
+    u1 = np.zeros(r.shape)
+    u3 = np.zeros(r.shape)
+    out = r >= ri
+    spin = np.abs(a)
+    asign = np.sign(a)
+    if np.any(out):
+        rr = r[out]
+        Omega = asign * s / (rr ** 1.5 + s * spin)
+        u0[out] = (rr ** 1.5 + s * spin) / np.sqrt(rr ** 3 - 3 * rr ** 2 + 2 * s * spin * rr ** 1.5)
+        u3[out] = Omega * u0[out]
+    if np.any(~out):
+        rr = r[~out]
+        Delta = (rr ** 2 - 2 * rr + a ** 2)
+        ell_i = s * asign * (ri ** 2 + a ** 2 - s * 2 * spin * np.sqrt(ri)) / (ri ** 1.5 - 2 * np.sqrt(ri) + s * spin)
+        gam_i = np.sqrt(1 - 2. / (3. * ri))
+        H = (2 * rr - a * ell_i) / Delta
+        u0[~out] = gam_i * (1 + (2 / rr) * (1 + H))
+        u1[~out] = -np.sqrt(2. / (3 * ri)) * (ri / rr - 1) ** 1.5
+        u3[~out] = gam_i * (ell_i + a * H) / (rr ** 2)
+    return u0, u1, 0, u3
+
+
 def u_infall(a, r):
     """Geodesic infall from rest at infinity; kgeo/velocities.py:211-226."""
     Delta = r ** 2 + a ** 2 - 2 * r
@@ -874,6 +914,96 @@ def emis_bpl(a, r, p1=-2.0, p2=-0.5):
     """Broken power law; kgeo/emissivities.py:121-127."""
     rh = 1 + np.sqrt(1 - a ** 2)
     return np.exp(p1 * np.log(r / rh) + p2 * np.log(r / rh) ** 2)
+
+
+def emis_glm(a, r, gamma_off=-1.5, sigma=0.5, mu_ring=False):
+    """GLM / ring profile; kgeo/emissivities.py:130-139."""
+    mu = mu_ring if mu_ring else 1 - np.sqrt(1 - a ** 2)
+    return np.exp(-0.5 * (gamma_off + np.arcsinh((r - mu) / sigma)) ** 2) / np.sqrt((r - mu) ** 2 + sigma ** 2)
+
+
+def velocity(a, r, veltype, kw):
+    """Velocity(veltype, **kw).u_lab(a, r) for the supported models; kgeo/velocities.py:69-95."""
+    retro = kw.get('retrograde', False)
+    if veltype == 'zamo':
+        return u_zamo(a, r)
+    if veltype == 'infall':
+        return u_infall(a, r)
+    if veltype in ('kep', 'cunningham'):
+        return u_kep(a, r, retrograde=retro)
+    if veltype in ('subkep', 'cunningham_subkep'):
+        return u_subkep(a, r, fac_subkep=kw.get('fac_subkep', 1), retrograde=retro)
+    if veltype == 'general':
+        return u_general(a, r, fac_subkep=kw.get('fac_subkep', 1), beta_phi=kw.get('beta_phi', 1),
+                         beta_r=kw.get('beta_r', 1), retrograde=retro)
+    raise ValueError(veltype)
+
+
+def emissivity(a, r, emistype, kw):
+    """Emissivity(emistype, **kw).jrest(a, r) without the spectral factors; kgeo/emissivities.py:38-127."""
+    if emistype == 'constant':
+        return np.ones(r.shape)
+    if emistype == 'bpl':
+        return emis_bpl(a, r, p1=kw.get('p1', -2.0), p2=kw.get('p2', -0.5))
+    if emistype == 'glm':
+        return emis_glm(a, r, gamma_off=kw.get('gamma_off', -1.5), sigma=kw.get('sigma', 0.5), mu_ring=False)
+    if emistype == 'ring':
+        return emis_glm(a, r, gamma_off=kw.get('gamma_off', 0), sigma=kw.get('sigma', 0.3),
+                        mu_ring=kw.get('r_ring', 4.5))
+    raise ValueError(emistype)
+
+
+def make_image_px(a, r_o, th_o, mbar_max, alpha, beta, emis=('bpl', {}), vel=('zamo', {}), specind=1,
+                  sinthb=np.pi / 4.):
+    """make_image's (I, Q, U, r, t, g, sinthb, n, np) on given pixels, unpolarised.
+
+    kgeo/equatorial_images.py:23-122 (the pixel grid is image_grid's) with Iobs :124-264.
+    """
+    emistype, ekw = emis
+    veltype, vkw = vel
+    cut_in = ekw.get('emiscut_in', 0)
+    cut_out = ekw.get('emiscut_out', 1.e10)
+    rh = 1 + np.sqrt(1 - a ** 2)
+    lam = -alpha * np.sin(th_o)
+    eta = (alpha ** 2 - a ** 2) * np.cos(th_o) ** 2 + beta ** 2
+    n_pix = len(alpha)
+    out = {k: np.zeros((n_pix, mbar_max + 1)) for k in ('I', 'Q', 'U', 'r', 't', 'g', 'sinthb')}
+    nmax_out = None
+    for mbar in range(mbar_max + 1):
+        r_s, Ir, Imax, Nmax = r_equatorial(a, r_o, th_o, mbar, alpha, beta)
+        zero = (Nmax < mbar) + (Nmax == -1) + (r_s <= rh)
+        if cut_in > 0:
+            zero = zero + (r_s < cut_in)
+        if cut_out > 0:
+            zero = zero + (r_s > cut_out)
+        g = np.zeros(n_pix)
+        I = np.zeros(n_pix)
+        sb = np.zeros(n_pix)
+        if np.any(~zero):
+            live = ~zero
+            inside = ~outside_critical(a, th_o, alpha[live], beta[live]).astype(bool)
+            kr = np.where(inside + (Ir[live] <= 0.5 * Imax[live]), 1., -1.)
+            kth = -1 * np.power(-1, np.mod(mbar, 2)) if th_o < 0.5 * np.pi else 1 * np.power(-1, np.mod(mbar, 2))
+            u0, u1, u2, u3 = velocity(a, r_s[live], veltype, vkw)
+            gg = redshift(a, r_s[live], lam[live], eta[live], kr, kth, u0, u1, u2, u3)
+            j = emissivity(a, r_s[live], emistype, ekw)
+            j = j * gg ** specind
+            j = j * sinthb ** (1 + specind)
+            g[live] = gg
+            I[live] = (gg ** 2) * j
+            sb[live] = sinthb
+        out['I'][:, mbar] = I
+        out['g'][:, mbar] = g
+        out['r'][:, mbar] = r_s
+        out['t'][:, mbar] = Ir
+        out['sinthb'][:, mbar] = sb
+        nmax_out = Nmax
+    tau_tot = np.zeros(n_pix)
+    r1, r2, r3, r4, _ = quartic_roots(a, lam, eta)
+    tau_tot = mino_total(a, r_o, eta, r1, r2, r3, r4)
+    out['n'] = nmax_out
+    out['np'] = n_poloidal_orbits(a, th_o, alpha, beta, tau_tot)
+    return out
 
 
 def redshift(a, r, lam, eta, kr_sign, kth_sign, u0, u1, u2, u3, th=np.pi / 2):

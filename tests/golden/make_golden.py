@@ -198,6 +198,32 @@ def main(path):
                                I=res[0], r=res[3], g=res[5], n=res[7], np_=res[8],
                                p1=-2.0, p2=0.0, fac_subkep=0.8, beta_r=0.5, beta_phi=1.0))
 
+    # make_image across the other velocity / emissivity models, both hemispheres, cuts
+    cases = [
+        (0.3, 40, 1, ('constant', {}), ('zamo', {})),
+        (0.9, 25, 2, ('bpl', {}), ('kep', {})),
+        (0.7, 110, 1, ('glm', {}), ('kep', {'retrograde': True})),
+        (0.2, 75, 1, ('ring', {'r_ring': 5.0, 'gamma_off': 0.3, 'sigma': 0.4, 'emiscut_in': 3.0}),
+         ('subkep', {'fac_subkep': 0.6, 'retrograde': True})),
+        (0.94, 17, 2, ('bpl', {'p1': -1.5, 'p2': -0.3}), ('infall', {})),
+        (0.9375, 135, 1, ('bpl', {'p1': -2.5, 'p2': 0.1}),
+         ('general', {'fac_subkep': 0.3, 'beta_phi': 0.1, 'beta_r': 0.4, 'retrograde': True})),
+    ]
+    psize = 18. / 20
+    n_side = int(np.floor(9. - -9.) / psize)
+    side = np.linspace(-9., -9. + n_side * psize, n_side)
+    Ai, Bi = np.meshgrid(side, side)
+    out = dict(alpha=Ai.flatten(), beta=Bi.flatten(), psize=psize, ncase=len(cases))
+    for i, (a, th, mbar_max, (et, ek), (vt, vk)) in enumerate(cases):
+        em = ref.emis.Emissivity(et, **ek)
+        ve = ref.vel.Velocity(vt, **vk)
+        res = quiet(ref.images.make_image, a, 1.e4, th * deg, mbar_max, -9., 9., -9., 9., psize,
+                    emissivity=em, velocity=ve)
+        out.update({'case%d' % i: repr((a, th, mbar_max, et, ek, vt, vk))})
+        for k, v in zip(['I', 'Q', 'U', 'r', 't', 'g', 'sinthb', 'n', 'np'], res):
+            out['%s%d' % (k, i)] = v
+    save('image_models', out)
+
     # elliptic Pi adapter: random in-domain points plus every special-case mask
     rng = np.random.default_rng(2)
     n = np.concatenate([rng.uniform(-3, 0.95, 400), rng.uniform(1.05, 6, 200),

@@ -1,6 +1,7 @@
 // Host (g++) build of the device arithmetic headers, for CPU unit checks of the
 // same code the CUDA kernels compile. Test-only: never loaded by the product.
 #include "../../kgeo_gb300/csrc/kg_equatorial.cuh"
+#include "../../kgeo_gb300/csrc/kg_image.cuh"
 #include "../../kgeo_gb300/csrc/kg_mixed.cuh"
 
 using namespace kg;
@@ -10,6 +11,18 @@ static Observer make_obs(const double* ob) {
   o.a = ob[0]; o.a2 = ob[1]; o.r_o = ob[2]; o.th_o = ob[3]; o.sin_th = ob[4]; o.cos_th = ob[5];
   o.cos2 = ob[6]; o.rplus = ob[7]; o.rminus = ob[8]; o.minspin = (int)ob[9]; o.r_o_inf = (int)ob[10];
   return o;
+}
+
+// mi = (emissivity, velocity, retrograde); md = (emis_p0, emis_p1, mu_ring, vel_p0, vel_p1,
+// vel_p2, emiscut_in, emiscut_out, specind, sinthb)
+static EmissionModel make_model(const int* mi, const double* md) {
+  EmissionModel M;
+  M.emis = mi[0]; M.vel = mi[1]; M.retrograde = mi[2];
+  M.emis_p[0] = md[0]; M.emis_p[1] = md[1]; M.mu_ring = md[2];
+  M.vel_p[0] = md[3]; M.vel_p[1] = md[4]; M.vel_p[2] = md[5];
+  M.emiscut_in = md[6]; M.emiscut_out = md[7]; M.specind = md[8]; M.sinthb = md[9];
+  M.sinthb_pow = std::pow(md[9], 1 + md[8]);
+  return M;
 }
 
 extern "C" {
@@ -133,6 +146,55 @@ void hm_crossings(const double* ob, const double* alpha, const double* beta, lon
     for (long g = 0; g < ntau; ++g) {
       n_eq[g * n + i] = n_eq_at(o, c, beta[i], tau[g * n + i]);
       n_pol[g * n + i] = n_pol_at(c, Kc, tau[g * n + i]);
+    }
+  }
+}
+// image (npix, nord) outputs as kgeo_image
+void hm_image(const double* ob, const int* mi, const double* md, const double* alpha, const double* beta, long n,
+              int nord, double* I, double* g, double* r_s, double* Ir, double* sinthb, double* nmax, double* npol) {
+  Observer o = make_obs(ob);
+  EmissionModel M = make_model(mi, md);
+  for (long i = 0; i < n; ++i) {
+    PixelGeo p;
+    for (int m0 = 0; m0 < nord; m0 += ORDER_GROUP) {
+      const int k = std::min(ORDER_GROUP, nord - m0);
+      pixel_geo(o, alpha[i], beta[i], m0, k, &p);
+      for (int j = 0; j < k; ++j) {
+        long q = i * nord + m0 + j;
+        double II = 0, gg = 0, sb = 0;
+        if (!image_zero(M, o, p, j)) {
+          emission_px(M, o, p, j, &II, &gg);
+          sb = M.sinthb;
+        }
+        I[q] = II; g[q] = gg; r_s[q] = p.r_s[j]; Ir[q] = p.Ir[j]; sinthb[q] = sb;
+      }
+    }
+    nmax[i] = p.Nmax;
+    npol[i] = p.npol;
+  }
+}
+// per pixel and order dI/dq (npix, nord, NQ); rs_d (npix, nord, 2) = d r_s / d(a, th_o)
+void hm_image_jac(const double* ob, const int* mi, const double* md, const double* alpha, const double* beta,
+                  long n, int nord, double* jac, double* rs_d) {
+  Observer o = make_obs(ob);
+  EmissionModel M = make_model(mi, md);
+  for (long i = 0; i < n; ++i) {
+    for (int m0 = 0; m0 < nord; m0 += ORDER_GROUP) {
+      const int k = std::min(ORDER_GROUP, nord - m0);
+      PixelGeo p;
+      pixel_geo(o, alpha[i], beta[i], m0, k, &p);
+      D2 rs[ORDER_GROUP];
+      bool live = p.eta > 0;
+      if (live) rs_tangents(o, alpha[i], beta[i], p, k, rs);
+      for (int j = 0; j < k; ++j) {
+        long q = i * nord + m0 + j;
+        rs_d[q * 2] = live ? rs[j].d[0] : 0.0;
+        rs_d[q * 2 + 1] = live ? rs[j].d[1] : 0.0;
+        for (int c = 0; c < NQ; ++c) jac[q * NQ + c] = 0.0;
+        if (image_zero(M, o, p, j)) continue;
+        Dual<NQ> I = emission_dual(M, o, p, j, alpha[i], beta[i], rs[j]);
+        for (int c = 0; c < NQ; ++c) jac[q * NQ + c] = I.d[c];
+      }
     }
   }
 }
