@@ -630,14 +630,169 @@ def run_image(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------
+# configuration 4: batched images (64 images, one persistent launch, CUDA graph)
+# ---------------------------------------------------------------------------
+
+BATCH_IMAGES = 64
+
+
+def batch_workload(n_img=BATCH_IMAGES, small=False):
+    """64 images from default_rng(0): side ~ U{128..768} (uniform integer), a ~ U[0, 0.998),
+    theta_o ~ U[1, 89] deg, ngeo ~ U{64, 128, 256}, grids over [-12, 12] M."""
+    rng = np.random.default_rng(0)
+    ims, A, B = [], [], []
+    for _ in range(n_img):
+        side = int(rng.integers(128, 769))
+        if small:
+            side = max(8, side // 8)
+        a = float(rng.uniform(0, 0.998))
+        th = float(rng.uniform(1, 89)) * np.pi / 180
+        ng = int(rng.choice([64, 128, 256]))
+        x = np.linspace(-12, 12, side)
+        Ai, Bi = np.meshgrid(x, x)
+        ims.append(dict(a=a, th_o=th, npix=side * side, ngeo=ng, side=side))
+        A.append(Ai.flatten())
+        B.append(Bi.flatten())
+    return ims, np.concatenate(A), np.concatenate(B)
+
+
+def _oracle_batch_chunk(args):
+    a, th_o, A, B, G = args
+    from oracle import kgeo_oracle as ko
+    import warnings
+    warnings.filterwarnings('ignore')
+    ko.raytrace(a, R_O, th_o, A, B, G)
+    return len(A)
+
+
+def run_batch(args):
+    small = args.case == 'batch-small'
+    pool = cores = None
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()
+    import torch
+    from kgeo_gb300 import device as dev
+    from kgeo_gb300.batch import BatchPlan
+    ims, A, B = batch_workload(small=small)
+    n_rays = A.size
+    keys = ('t', 'r', 'th', 'ph', 'sig')
+    plan = BatchPlan(ims, precision='mixed', keys=keys)
+    al, be = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    plan.bind(al, be)
+    t0 = time.perf_counter()
+    cfg = plan.autotune(budget_ms=3000)
+    t_tune = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    for _ in range(args.warmup):
+        plan.graph_launch()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.graph_launch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    t_mixed = e0.elapsed_time(e1) / 1e3 / args.steps
+    n_points = plan.n_samples
+    # FP64 recurrence on the same batch (same plan shape, own outputs after the mixed ones
+    # are checked) and the plain FP64 kernel (independent evaluation per sample) on every 8th
+    # image, scaled by points
+    sub = list(range(0, len(ims), 8))
+    off = np.cumsum([0] + [im['npix'] for im in ims])
+    errs = {k: {'max': 0.0, 'rms_sum': 0.0, 'n': 0} for k in keys}
+    t_plain, pts_plain = 0.0, 0
+    for i in sub:
+        im = ims[i]
+        sl = slice(int(off[i]), int(off[i + 1]))
+        prep = dev.PreparedRays(im['a'], R_O, im['th_o'], al[sl], be[sl], ngeo=im['ngeo'])
+        out = prep.alloc(keys=keys)
+        prep.samples(out, chunk=cfg['chunk'])
+        got = plan.image(i)
+        for k in keys:
+            # the scales of the configuration-3 statistics: relative, with a floor of 1 rad for
+            # the angles and of r_o for t and sigma
+            x, y = got[k], out[k]
+            floor = {'r': 1e-300, 'th': 1.0, 'ph': 1.0, 't': R_O, 'sig': R_O}[k]
+            d = (x - y).abs() / y.abs().clamp_min(floor)
+            d = d[torch.isfinite(d)]
+            if d.numel():
+                errs[k]['max'] = max(errs[k]['max'], float(d.max()))
+                errs[k]['rms_sum'] += float((d * d).sum())
+                errs[k]['n'] += int(d.numel())
+        torch.cuda.synchronize()
+        a0, a1 = ev(), ev()
+        a0.record(stream)
+        prep.samples(out, chunk=0)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        t_plain += a0.elapsed_time(a1) / 1e3
+        pts_plain += im['npix'] * im['ngeo']
+        del out, prep
+    mixed_err = {k: {'max': v['max'], 'rms': float(np.sqrt(v['rms_sum'] / max(v['n'], 1)))} for k, v in errs.items()}
+    plain_pts_per_s = pts_plain / t_plain
+    pts_per_ray = n_points / n_rays
+    plan_d = BatchPlan(ims, precision='fp64', keys=('r',))
+    plan_d.bind(al, be)
+    plan_d.run()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    plan_d.run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_fp64 = e0.elapsed_time(e1) / 1e3
+    plan_d.close()
+    cpu = None
+    if pool is not None:
+        rng = np.random.default_rng(0)
+        idx = np.sort(rng.choice(n_rays, n_rays // 256, replace=False))
+        img_of = np.searchsorted(off, idx, side='right') - 1
+        jobs = []
+        for i in np.unique(img_of):
+            sel = idx[img_of == i]
+            for c in np.array_split(sel, max(1, sel.size // 512)):
+                jobs.append((ims[i]['a'], ims[i]['th_o'], A[c], B[c], ims[i]['ngeo']))
+        tc0 = time.time()
+        pool.map(_oracle_batch_chunk, jobs)
+        dt = time.time() - tc0
+        pool.close()
+        cpu = {'value': idx.size / dt, 'unit': 'rays/s', 'cores': cores, 'kind': 'port',
+               'sample': '%d rays (seeded 1/256 of the batch, every image proportionally, its own ngeo); '
+                         'oracle/kgeo_oracle.py raytrace on a %d-process pool, %.1f s wall' % (idx.size, cores, dt)}
+    line = {
+        'metric': 'Kerr rays/s: 64 batched images, mixed precision, one persistent launch in a CUDA graph',
+        'value': n_rays / t_mixed, 'unit': 'rays/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': t_mixed * 1e3, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32+f64', 'data': 'synthetic: 64 image-plane grids from default_rng(0)',
+        'config': {'workload': 'configuration 4: 64 images, side ~ U{128..768}, a ~ U[0, 0.998), theta_o ~ '
+                               'U[1, 89] deg, ngeo ~ U{64, 128, 256}, grids over [-12, 12] M, r_o = 1e4',
+                   'rays': n_rays, 'samples': n_points, 'precision': 'mixed', 'case': args.case,
+                   'tuned': cfg, 'tune_s': t_tune, 'l2': 'outputs %.0f GB per step' % (n_points * 40 / 1e9)},
+        'points_per_s': n_points / t_mixed,
+        'fp64_batched_recurrence': {'value': n_rays / t_fp64, 'ms_per_step': t_fp64 * 1e3},
+        'fp64_plain': {'value': plain_pts_per_s / pts_per_ray, 'points_per_s': plain_pts_per_s,
+                       'sample': 'images %s, independent evaluation per sample, scaled by points' % sub},
+        'speedup_vs_fp64_plain': (n_rays / t_mixed) / (plain_pts_per_s / pts_per_ray),
+        'speedup_vs_fp64_recurrence': t_fp64 / t_mixed,
+        'mixed_vs_fp64_error': mixed_err,
+        'cpu_baseline': cpu, 'clocks': ck, 'gpu_launches': 6 * args.steps,
+    }
+    plan.close()
+    print(json.dumps(line))
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument('--gpus', type=int, default=1)
     p.add_argument('--steps', type=int, default=5)
     p.add_argument('--warmup', type=int, default=3)
     p.add_argument('--impl', choices=('ours', 'reference'), default='ours')
-    p.add_argument('--case', choices=('full', 'small', 'mixed', 'mixed-small', 'image', 'image-small'),
-                   default='full')
+    p.add_argument('--case', choices=('full', 'small', 'mixed', 'mixed-small', 'image', 'image-small', 'batch',
+                                      'batch-small'), default='full')
     p.add_argument('--no-cpu-baseline', action='store_true')
     args = p.parse_args()
     if args.impl == 'reference':
@@ -646,6 +801,8 @@ def main():
         run_mixed(args)
     elif args.case.startswith('image'):
         run_image(args)
+    elif args.case.startswith('batch'):
+        run_batch(args)
     else:
         run_ours(args)
 

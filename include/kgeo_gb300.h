@@ -205,6 +205,49 @@ int kgeo_image_adjoint(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orde
                        const double* beta, int64_t npix, const kgeo_emission* model, const double* grad_I, double* grad,
                        void* workspace, size_t workspace_bytes, void* stream);
 
+/* Batched tracing: many images of different size, spin, inclination and ngeo traced as one
+ * job (no counterpart in the reference, whose raytrace_ana takes one image per call:
+ * kgeo/kerr_raytracing_ana.py:46). A plan describes the images; kgeo_batch_bind attaches the
+ * device buffers: alpha, beta are every image's pixels concatenated (image i owns rays
+ * [sum_{j<i} npix_j, ... + npix_i)); per-ray outputs (tau_tot, rclass, thclass) follow the
+ * same concatenation; each sample output (t, r, th, ph, sig, mino) holds image i's
+ * (ngeo_i, npix_i) row-major block at offset sum_{j<i} ngeo_j npix_j. A run is one setup pass
+ * over all rays (per-image class sort) and one persistent sample kernel whose blocks pull
+ * tiles of work items from a device counter. Results equal kgeo_raytrace(_mixed) of each image
+ * with the same chunk length. A plan and its bound buffers are used by one stream at a time.
+ *
+ * kgeo_batch_autotune times the sample kernel's launch shapes (block size, CTAs per SM, tile
+ * length, samples per work item) on a subset of the bound batch's tiles within about budget_ms
+ * and keeps the fastest; results are cached per device, precision and image sizes (the cache
+ * is the library's only global state, mutex-guarded), so a new plan for the same batch shape
+ * starts tuned. kgeo_batch_graph_launch captures the whole run into a CUDA graph on first use
+ * (and again after a bind or a configuration change) and replays it on `stream`. */
+#define KGEO_BATCH_MAX_IMAGES 4096
+typedef struct {
+  double a, r_o, th_o;    /* observer of this image (the kgeo_observer rules apply) */
+  int64_t npix;
+  int32_t ngeo;
+  int32_t reserved;
+  double maxtaufrac;
+} kgeo_batch_image;
+typedef struct {
+  int32_t block;          /* threads per block of the sample kernel: 128 or 256 */
+  int32_t ctas_per_sm;    /* resident blocks per SM of the persistent grid (1..4) */
+  int32_t tile;           /* work items per tile taken from the counter (multiple of block) */
+  int32_t chunk;          /* samples per work item (<= 64 FP64, <= 256 mixed) */
+} kgeo_batch_config;
+typedef struct kgeo_batch_plan kgeo_batch_plan;
+int kgeo_batch_create(const kgeo_batch_image* images, int32_t nimg, int32_t precision, kgeo_batch_plan** plan);
+void kgeo_batch_destroy(kgeo_batch_plan* plan);
+int kgeo_batch_sizes(const kgeo_batch_plan* plan, int64_t* n_rays, int64_t* n_samples, size_t* workspace_bytes);
+int kgeo_batch_bind(kgeo_batch_plan* plan, const double* alpha, const double* beta, kgeo_geodesics* out,
+                    void* workspace, size_t workspace_bytes);
+int kgeo_batch_get_config(const kgeo_batch_plan* plan, kgeo_batch_config* cfg, int32_t* tuned);
+int kgeo_batch_set_config(kgeo_batch_plan* plan, const kgeo_batch_config* cfg);
+int kgeo_batch_autotune(kgeo_batch_plan* plan, int32_t budget_ms, void* stream, kgeo_batch_config* best);
+int kgeo_batch_run(kgeo_batch_plan* plan, void* stream);
+int kgeo_batch_graph_launch(kgeo_batch_plan* plan, void* stream);
+
 /* Allocation-free kgeo_raytrace. No counterpart in the reference: it exists for callers
  * that may not allocate device memory when they call in — an application that owns all
  * device memory under a fixed budget, a latency-critical loop that cannot afford an

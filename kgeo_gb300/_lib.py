@@ -39,6 +39,17 @@ class ImageOut(ctypes.Structure):
                 ('imax', c_void_p), ('nmax', c_void_p), ('npol', c_void_p)]
 
 
+class BatchImage(ctypes.Structure):
+    """kgeo_batch_image."""
+    _fields_ = [('a', c_double), ('r_o', c_double), ('th_o', c_double), ('npix', c_int64), ('ngeo', c_int32),
+                ('reserved', c_int32), ('maxtaufrac', c_double)]
+
+
+class BatchConfig(ctypes.Structure):
+    """kgeo_batch_config."""
+    _fields_ = [('block', c_int32), ('ctas_per_sm', c_int32), ('tile', c_int32), ('chunk', c_int32)]
+
+
 EMIS = {'bpl': 0, 'constant': 1, 'glm': 2, 'ring': 3}
 VEL = {'zamo': 0, 'infall': 1, 'kep': 2, 'cunningham': 2, 'subkep': 3, 'cunningham_subkep': 3, 'general': 4}
 N_IMAGE_PARAMS = 7  # a, th_o, emis_p[0..1], vel_p[0..2]
@@ -68,6 +79,16 @@ SIGNATURES = {
     'kgeo_image_adjoint_workspace_size': (c_size_t, [c_int64]),
     'kgeo_image_adjoint': (c_int, [ctypes.POINTER(Observer), c_int32, c_int32, c_void_p, c_void_p, c_int64,
                                    ctypes.POINTER(Emission), c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    'kgeo_batch_create': (c_int, [ctypes.POINTER(BatchImage), c_int32, c_int32, ctypes.POINTER(c_void_p)]),
+    'kgeo_batch_destroy': (None, [c_void_p]),
+    'kgeo_batch_sizes': (c_int, [c_void_p, ctypes.POINTER(c_int64), ctypes.POINTER(c_int64),
+                                 ctypes.POINTER(c_size_t)]),
+    'kgeo_batch_bind': (c_int, [c_void_p, c_void_p, c_void_p, ctypes.POINTER(GeodesicsOut), c_void_p, c_size_t]),
+    'kgeo_batch_get_config': (c_int, [c_void_p, ctypes.POINTER(BatchConfig), ctypes.POINTER(c_int32)]),
+    'kgeo_batch_set_config': (c_int, [c_void_p, ctypes.POINTER(BatchConfig)]),
+    'kgeo_batch_autotune': (c_int, [c_void_p, c_int32, c_void_p, ctypes.POINTER(BatchConfig)]),
+    'kgeo_batch_run': (c_int, [c_void_p, c_void_p]),
+    'kgeo_batch_graph_launch': (c_int, [c_void_p, c_void_p]),
     'kgeo_status_string': (ctypes.c_char_p, [c_int]),
     'kgeo_abi_version': (c_int, []),
 }

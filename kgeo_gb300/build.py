@@ -27,6 +27,7 @@ UNITS = [
     ('kg_abi.cu', []),
     ('kg_peak.cu', []),
     ('kg_noalloc.cu', []),
+    ('kg_batch.cu', []),
 ]
 
 

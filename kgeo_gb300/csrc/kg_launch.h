@@ -153,6 +153,58 @@ struct ImageAdjointArgs {
   double* grad;          // (NQ)
 };
 
+// ---------------------------------------------------------------------------
+// batched images (kg_batch.cu): many images of different size, spin, inclination and ngeo in
+// one setup pass and one persistent sample kernel. Rays of all images are concatenated
+// (image i owns rays [pix_off, pix_off + npix)); the per-ray records are one
+// structure-of-arrays buffer with stride ntot; image i's samples are the (ngeo, npix)
+// row-major block at out_off of each output.
+struct BatchImage {
+  Observer obs;
+  int64_t pix_off, npix, ngeo, out_off;
+  double maxtaufrac;
+};
+
+struct BatchArgs {
+  const BatchImage* img;   // (nimg)
+  const int64_t* pix_off;  // (nimg + 1) ray offsets, for the image lookup
+  int64_t* item_off;       // (nimg + 1) work-item offsets of the sample kernel (chunk dependent)
+  int nimg;
+  int64_t ntot;
+  const double* alpha;     // (ntot)
+  const double* beta;      // (ntot)
+  double* rec;             // NUM_FIELDS x ntot
+  int* code;               // (ntot)
+  int* perm;               // (ntot) rays of each image sorted by class bucket (global ray indices)
+  uint32_t* counts;        // (nimg * NBUCKET) bucket counts, then (nimg * NBUCKET) cursors
+  uint32_t* flags;         // (nimg) launch flags per image
+  unsigned long long* work;  // work counter of the persistent kernel
+  int32_t* rclass;         // per-ray outputs (ntot), may be NULL
+  int32_t* thclass;
+  double* tau_tot;
+  double *t, *r, *th, *ph, *sig, *mino;  // concatenated sample outputs
+  int chunk;               // samples per work item
+  int tile;                // work items per tile (multiple of the block size)
+  int tile_skip;           // 1: every tile; S > 1: every S-th tile (autotuner timing runs)
+  int mixed;
+};
+
+constexpr int BATCH_MAX_IMAGES = 4096;
+
+// Image containing global index x of a prefix-offset table off (nimg + 1 entries).
+KG_HD int batch_find(const int64_t* off, int nimg, int64_t x) {
+  int lo = 0, hi = nimg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= x) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+cudaError_t launch_batch_setup(const BatchArgs& a, cudaStream_t s);
+cudaError_t launch_batch_samples(const BatchArgs& a, int block, int grid, cudaStream_t s);
+
 constexpr int IMAGE_BLOCK = 128;
 KG_HD constexpr int64_t image_adjoint_blocks(int64_t npix) { return (npix + IMAGE_BLOCK - 1) / IMAGE_BLOCK; }
 

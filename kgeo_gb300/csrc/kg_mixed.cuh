@@ -207,16 +207,20 @@ KG_HD ThetaOut theta_assemble_mixed(const FV& f, int code, const ThetaState& st)
   const double s = f[F_S];
   out.Gph = f[T_PREF] * st.pi - s * f[T_GPH];
   const float up = (float)f[T_UP];
+  // 1 - u_+ in FP64: for observers near the pole u_+ is within 1e-4 of 1, where an FP32
+  // difference would keep only a few bits of sin(theta)
+  const float omu = (float)(1.0 - f[T_UP]);
   const float sn = (float)st.sn, cn = (float)st.cn;
   if (code_th(code) == TH_ORD) {
     float cth = (float)(-s) * sqrtf(up) * sn;
-    float sth = sqrtf((1.0f - up) + up * (cn * cn));
+    float sth = sqrtf(omu + up * (cn * cn));
     out.th = (double)atan2f(sth, cth);
     out.Gt = -(2 * f[T_UP] * f[T_PREF] * st.e) / (2 * f[T_KK]) - s * f[T_GT];
   } else {
     const float um = (float)f[T_UM];
-    float cth = (float)f[T_H] * sqrtf(um + (up - um) * (sn * sn));
-    float sth = sqrtf((1.0f - up) + (up - um) * (cn * cn));
+    const float upm = (float)(f[T_UP] - f[T_UM]);
+    float cth = (float)f[T_H] * sqrtf(um + upm * (sn * sn));
+    float sth = sqrtf(omu + upm * (cn * cn));
     out.th = (double)atan2f(sth, cth);
     out.Gt = f[T_PREFC] * st.e - s * f[T_GT];
   }

@@ -100,4 +100,60 @@ cudaError_t launch_samples(const SampleArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// batched images: persistent kernel over the work items of every image
+// ---------------------------------------------------------------------------
+
+// A block takes tiles of `tile` consecutive work items from a global counter until the items
+// run out, so images of different size and cost balance across the SMs without a host-side
+// schedule. Inside an image, items are chunk-major over its class-sorted rays (as in
+// stepped_kernel); a tile may span two images.
+template <bool MIXED>
+__global__ void __launch_bounds__(256) batch_samples_kernel(BatchArgs a) {
+  __shared__ long long tile_id;
+  const int64_t total = a.item_off[a.nimg];
+  for (;;) {
+    if (threadIdx.x == 0) tile_id = (long long)atomicAdd(a.work, 1ull);
+    __syncthreads();
+    const int64_t base = (int64_t)tile_id * a.tile * a.tile_skip;
+    __syncthreads();
+    if (base >= total) break;
+    for (int64_t k = threadIdx.x; k < a.tile; k += blockDim.x) {
+      const int64_t item = base + k;
+      if (item >= total) break;
+      const int im = batch_find(a.item_off, a.nimg, item);
+      const BatchImage& B = a.img[im];
+      const int64_t local = item - a.item_off[im];
+      const int64_t c = local / B.npix;
+      const int64_t p = __ldg(a.perm + B.pix_off + (local - c * B.npix));
+      const uint32_t fl = __ldg(a.flags + im);
+      const bool ordinary_active = (fl & FLAG_ANY_ETA_POS) != 0;
+      const bool step_zero = (fl & FLAG_ANY_STEP_ZERO) != 0;
+      RecView f{a.rec + p, a.ntot};
+      const int code = __ldg(a.code + p);
+      const int64_t g0 = c * a.chunk;
+      const int64_t g1 = g0 + a.chunk < B.ngeo ? g0 + a.chunk : B.ngeo;
+      const int64_t obase = B.out_off + (p - B.pix_off);
+      const int64_t np = B.npix;
+      auto emit = [&](int64_t g, double tau, const Sample& S) {
+        const int64_t o = obase + g * np;
+        if (a.t) a.t[o] = S.t;
+        if (a.r) a.r[o] = S.r;
+        if (a.th) a.th[o] = S.th;
+        if (a.ph) a.ph[o] = S.ph;
+        if (a.sig) a.sig[o] = S.sig;
+        if (a.mino) a.mino[o] = tau;
+      };
+      if (MIXED) ray_chunk_mixed(B.obs, f, code, g0, g1, B.ngeo, ordinary_active, step_zero, emit);
+      else ray_chunk(B.obs, f, code, g0, g1, B.ngeo, ordinary_active, step_zero, emit);
+    }
+  }
+}
+
+cudaError_t launch_batch_samples(const BatchArgs& a, int block, int grid, cudaStream_t s) {
+  if (a.mixed) batch_samples_kernel<true><<<grid, block, 0, s>>>(a);
+  else batch_samples_kernel<false><<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 }  // namespace kg

@@ -105,4 +105,97 @@ cudaError_t launch_crossings(const CrossingArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// batched images
+// ---------------------------------------------------------------------------
+
+// Work-item offsets of the sample kernel: image i has npix * ceil(ngeo / chunk) items.
+__global__ void batch_item_offsets_kernel(BatchArgs a) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int64_t acc = 0;
+  for (int i = 0; i < a.nimg; ++i) {
+    a.item_off[i] = acc;
+    const int64_t ng = a.img[i].ngeo;
+    acc += a.img[i].npix * ((ng + a.chunk - 1) / a.chunk);
+  }
+  a.item_off[a.nimg] = acc;
+}
+
+__global__ void __launch_bounds__(128) batch_setup_kernel(BatchArgs a) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int key = -1;
+  unsigned fl = 0;
+  int im = 0;
+  if (r < a.ntot) {
+    im = batch_find(a.pix_off, a.nimg, r);
+    const BatchImage& B = a.img[im];
+    RayRec R;
+    int rc = 0, tc = 0;
+    fl = ray_setup(B.obs, a.alpha[r], a.beta[r], B.maxtaufrac, &R, &rc, &tc);
+    if (B.ngeo > 1) {
+      const double step = R.f[F_TAUMAX] / (double)(B.ngeo - 1);
+      R.code = step_constants<const double*>(R.f, R.code, step, R.f);
+      if (step == 0.0) fl |= FLAG_ANY_STEP_ZERO;
+    }
+#pragma unroll
+    for (int k = 0; k < NUM_FIELDS; ++k) a.rec[(int64_t)k * a.ntot + r] = R.f[k];
+    a.code[r] = R.code;
+    if (a.rclass) a.rclass[r] = rc;
+    if (a.thclass) a.thclass[r] = tc;
+    if (a.tau_tot) a.tau_tot[r] = R.f[F_TAUTOT];
+    key = im * NBUCKET + ray_bucket(R.code);
+  }
+  // flags: one atomic per image present in the warp (warp-uniform loop, full-mask reductions)
+  const int lane = threadIdx.x & 31;
+  unsigned pending = __ballot_sync(0xffffffffu, r < a.ntot);
+  while (pending) {
+    const int leader = __ffs(pending) - 1;
+    const int lim = __shfl_sync(0xffffffffu, im, leader);
+    const bool mine = r < a.ntot && im == lim;
+    const unsigned in = __ballot_sync(0xffffffffu, mine);
+    const unsigned v = __reduce_or_sync(0xffffffffu, mine ? fl : 0u);
+    if (lane == leader && v) atomicOr(a.flags + lim, v);
+    pending &= ~in;
+  }
+  // bucket counts: one atomic per distinct (image, bucket) key of the warp
+  const unsigned grp = __match_any_sync(0xffffffffu, key);
+  if (key >= 0 && lane == __ffs(grp) - 1) atomicAdd(a.counts + key, (uint32_t)__popc(grp));
+}
+
+// Per image: exclusive scan of its NBUCKET counts into cursors that start at its first ray.
+__global__ void batch_scan_kernel(BatchArgs a) {
+  const int im = blockIdx.x, lane = threadIdx.x;
+  const uint32_t c = a.counts[im * NBUCKET + lane];
+  uint32_t v = c;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += u;
+  }
+  a.counts[(int64_t)a.nimg * NBUCKET + im * NBUCKET + lane] = (uint32_t)a.img[im].pix_off + (v - c);
+}
+
+__global__ void __launch_bounds__(128) batch_scatter_kernel(BatchArgs a) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int key = r < a.ntot ? batch_find(a.pix_off, a.nimg, r) * NBUCKET + ray_bucket(a.code[r]) : -1;
+  const unsigned grp = __match_any_sync(0xffffffffu, key);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(grp) - 1;
+  uint32_t base = 0;
+  if (key >= 0 && lane == leader) base = atomicAdd(a.counts + (int64_t)a.nimg * NBUCKET + key, (uint32_t)__popc(grp));
+  base = __shfl_sync(grp, base, leader);
+  if (key >= 0) a.perm[base + __popc(grp & ((1u << lane) - 1u))] = (int)r;
+}
+
+cudaError_t launch_batch_setup(const BatchArgs& a, cudaStream_t s) {
+  batch_item_offsets_kernel<<<1, 32, 0, s>>>(a);
+  if (a.ntot > 0) {
+    const int block = 128;
+    const unsigned grid = (unsigned)((a.ntot + block - 1) / block);
+    batch_setup_kernel<<<grid, block, 0, s>>>(a);
+    batch_scan_kernel<<<a.nimg, 32, 0, s>>>(a);
+    batch_scatter_kernel<<<grid, block, 0, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace kg

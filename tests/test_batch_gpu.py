@@ -1,0 +1,120 @@
+"""GPU tests of batched tracing (kgeo_batch_*): each image of a batch equals the
+single-image trace (kgeo_ray_setup + kgeo_ray_samples) with the same chunk length, for FP64
+and the mixed-precision kernel, through direct launches, the autotuned shape and the CUDA
+graph replay; the batch includes empty images, ngeo = 0 / 1 and both hemispheres."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+DEG = np.pi / 180
+
+
+def batch_images(seed=3, n=7):
+    rng = np.random.default_rng(seed)
+    ims, A, B = [], [], []
+    sides = [17, 0, 33, 8, 24, 1, 41][:n]
+    ngeos = [64, 50, 1, 0, 129, 7, 100][:n]
+    for i, (side, ng) in enumerate(zip(sides, ngeos)):
+        a = float(rng.uniform(0, 0.998))
+        th = float(rng.uniform(1, 89)) * DEG
+        if i % 3 == 2:
+            th = np.pi - th
+        x = np.linspace(-12, 12, side)
+        Ai, Bi = (v.flatten() for v in np.meshgrid(x, x))
+        ims.append(dict(a=a, th_o=th, npix=Ai.size, ngeo=ng))
+        A.append(Ai)
+        B.append(Bi)
+    return ims, np.concatenate(A), np.concatenate(B)
+
+
+def single(im, A, B, chunk, mixed):
+    from kgeo_gb300 import device as dev
+    al, be = dev.as_device(A), dev.as_device(B)
+    prep = dev.PreparedRays(im['a'], 1.e4, im['th_o'], al, be, ngeo=im['ngeo'])
+    out = prep.alloc()
+    if im['npix'] and im['ngeo']:
+        prep.samples(out, chunk=chunk, mixed=mixed)
+    return out, prep
+
+
+def same(x, y):
+    return torch.equal(torch.nan_to_num(x, nan=1234.5), torch.nan_to_num(y, nan=1234.5)) and \
+        torch.equal(torch.isnan(x), torch.isnan(y))
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+def test_batch_equals_single_images(precision):
+    from kgeo_gb300.batch import BatchPlan
+    ims, A, B = batch_images()
+    plan = BatchPlan(ims, precision=precision)
+    plan.bind(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda())
+    for launch in ('run', 'graph_launch'):
+        for v in plan.out.values():
+            v.fill_(-7.0)
+        getattr(plan, launch)()
+        torch.cuda.synchronize()
+        cfg = plan.config
+        off = 0
+        for i, im in enumerate(ims):
+            n = im['npix']
+            ref, prep = single(im, A[off:off + n], B[off:off + n], cfg['chunk'], precision == 'mixed')
+            got = plan.image(i)
+            for k in ('t', 'r', 'th', 'ph', 'sig', 'mino'):
+                assert got[k].shape == ref[k].shape
+                if n and im['ngeo']:
+                    assert same(got[k], ref[k]), (launch, i, k)
+            if n:
+                assert torch.equal(got['rclass'], prep.rclass) and torch.equal(got['thclass'], prep.thclass)
+                assert same(got['tau_tot'], prep.tau_tot)
+            off += n
+    plan.close()
+
+
+def test_batch_autotune_and_graph_replay():
+    from kgeo_gb300.batch import BatchPlan
+    ims, A, B = batch_images(seed=5)
+    plan = BatchPlan(ims, precision='mixed')
+    plan.bind(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda())
+    cfg = plan.autotune(budget_ms=300)
+    assert cfg['tuned'] and cfg['block'] in (128, 256) and cfg['tile'] % cfg['block'] == 0
+    plan.graph_launch()
+    torch.cuda.synchronize()
+    first = {k: v.clone() for k, v in plan.out.items()}
+    plan.graph_launch()
+    plan.graph_launch()
+    torch.cuda.synchronize()
+    for k in first:
+        assert same(first[k], plan.out[k])
+    # a new plan for the same batch shape starts from the cached tuning
+    plan2 = BatchPlan(ims, precision='mixed')
+    assert plan2.config == cfg
+    plan2.bind(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda())
+    plan2.run()
+    torch.cuda.synchronize()
+    for k in first:
+        assert same(first[k], plan2.out[k])
+    # explicit shapes are validated
+    with pytest.raises(Exception):
+        plan2.config = dict(block=96, ctas_per_sm=1, tile=96, chunk=64)
+    plan.close()
+    plan2.close()
+
+
+def test_batch_argument_errors():
+    from kgeo_gb300.batch import BatchPlan
+    with pytest.raises(Exception, match=r"\|a\| should be a float"):
+        BatchPlan([dict(a=1.2, th_o=1.0, npix=4, ngeo=8)])
+    with pytest.raises(Exception, match="th_o should be a float"):
+        BatchPlan([dict(a=0.2, th_o=np.pi / 2, npix=4, ngeo=8)])
+    plan = BatchPlan([dict(a=0.2, th_o=1.0, npix=4, ngeo=8)])
+    with pytest.raises(Exception, match="alpha, beta are different lengths!"):
+        plan.bind(torch.zeros(3, dtype=torch.float64, device='cuda'), torch.zeros(3, dtype=torch.float64,
+                                                                                  device='cuda'))
+    empty = BatchPlan([], precision='fp64')
+    empty.bind(torch.zeros(0, dtype=torch.float64, device='cuda'), torch.zeros(0, dtype=torch.float64,
+                                                                               device='cuda'))
+    empty.run()
+    empty.graph_launch()
+    empty.autotune(budget_ms=10)
