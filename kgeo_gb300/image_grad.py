@@ -80,4 +80,19 @@ def config_params(a, th_o, p, xi, beta_r, beta_phi=1.0):
     return torch.stack([a, th_o, -p, zero, xi, beta_phi, beta_r])
 
 
-__all__ = ['EquatorialImageFunction', 'equatorial_image', 'config_params']
+__all__ = ['EquatorialImageFunction', 'equatorial_image', 'config_params', 'reduce_loss_grad']
+
+
+def reduce_loss_grad(loss, grad, group=None):
+    """Sum a rank's image loss and its gradient over the process group: the one collective of
+    a pixel-sharded image (every rank renders its own pixels; rays need no exchange). loss is a
+    float, grad a sequence of floats; returns (loss, grad) summed over ranks as float64 on the
+    host. Uses the default group's backend (NCCL on GPUs, gloo on CPUs)."""
+    import torch.distributed as dist
+    v = torch.tensor([float(loss)] + [float(g) for g in grad], dtype=torch.float64)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size(group) > 1:
+        if dist.get_backend(group) == 'nccl':
+            v = v.cuda()
+        dist.all_reduce(v, op=dist.ReduceOp.SUM, group=group)
+    v = v.cpu()
+    return float(v[0]), [float(x) for x in v[1:]]
