@@ -42,9 +42,12 @@ typedef enum {
 } kgeo_status;
 
 /* Arithmetic of the sample kernels. FP64: every output within the FP64 parity bars.
- * MIXED: FP32 for the elliptic-integral increments, the chunk-start integrals and theta, FP64
- * for the Jacobi state, r and the final sums; samples next to an elliptic-Pi pole and the
- * final horizon-adjacent sample stay FP64 (error bars: bench.py --case mixed / DESIGN). */
+ * MIXED: the recurrence on the FP32 pipe — Jacobi states, integral accumulators, r and the
+ * sums into t, phi, sigma in float-float (two FP32 words, ~48 bits), the Pi / E increments as a
+ * float-float leading term plus an FP32 correction, theta from an FP32 atan2; FP64 at chunk
+ * starts, next to an elliptic-Pi pole and at the final horizon-adjacent sample. Measured against
+ * the FP64 oracle: r <= 1e-10, theta <= 1.5e-7, phi <= 4e-8 (floor 1), t and sigma <= 2e-8 of
+ * r_o. */
 #define KGEO_PRECISION_FP64 0
 #define KGEO_PRECISION_MIXED 1
 
@@ -213,8 +216,9 @@ int kgeo_image_adjoint(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orde
  * same concatenation; each sample output (t, r, th, ph, sig, mino) holds image i's
  * (ngeo_i, npix_i) row-major block at offset sum_{j<i} ngeo_j npix_j. A run is one setup pass
  * over all rays (per-image class sort) and one persistent sample kernel whose blocks pull
- * tiles of work items from a device counter. Results equal kgeo_raytrace(_mixed) of each image
- * with the same chunk length. A plan and its bound buffers are used by one stream at a time.
+ * tiles of work items from a device counter. Results equal kgeo_raytrace of each image with the
+ * same chunk length (FP64: bit for bit; mixed: to rounding, the kernels may contract different
+ * multiply-adds). A plan and its bound buffers are used by one stream at a time.
  *
  * kgeo_batch_autotune times the sample kernel's launch shapes (block size, CTAs per SM, tile
  * length, samples per work item) on a subset of the bound batch's tiles within about budget_ms

@@ -158,6 +158,7 @@ int kgeo_batch_create(const kgeo_batch_image* images, int32_t nimg, int32_t prec
   if (nimg < 0 || nimg > KGEO_BATCH_MAX_IMAGES) return KGEO_ERR_LENGTHS;
   if (nimg > 0 && !images) return KGEO_ERR_NULL;
   if (precision != KGEO_PRECISION_FP64 && precision != KGEO_PRECISION_MIXED) return KGEO_ERR_MODEL;
+  if (prepare_batch_kernels() != cudaSuccess) return KGEO_ERR_CUDA;
   kgeo_batch_plan* p = new kgeo_batch_plan();
   p->precision = precision;
   p->nimg = nimg;

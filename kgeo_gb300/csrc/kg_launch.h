@@ -116,7 +116,7 @@ constexpr int DEFAULT_CHUNK = 50;
 constexpr int MAX_CHUNK = 64;
 // The mixed recurrence accumulates FP32 increments into FP64 sums, so its chains may be
 // longer: the chunk-start evaluation is amortised over more samples.
-constexpr int DEFAULT_CHUNK_MIXED = 128;
+constexpr int DEFAULT_CHUNK_MIXED = 256;
 constexpr int MAX_CHUNK_MIXED = 256;
 
 // Equatorial image of orders mbar_lo .. mbar_lo + nord - 1 (kg_image.cuh); outputs are
@@ -204,6 +204,7 @@ KG_HD int batch_find(const int64_t* off, int nimg, int64_t x) {
 
 cudaError_t launch_batch_setup(const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_batch_samples(const BatchArgs& a, int block, int grid, cudaStream_t s);
+cudaError_t prepare_batch_kernels();
 
 constexpr int IMAGE_BLOCK = 128;
 KG_HD constexpr int64_t image_adjoint_blocks(int64_t npix) { return (npix + IMAGE_BLOCK - 1) / IMAGE_BLOCK; }

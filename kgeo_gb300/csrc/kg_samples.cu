@@ -2,7 +2,7 @@
 // that the lanes of a warp walk consecutive samples of the same ray and take the same
 // branches; stores go to the (nsamp, npix) row-major outputs.
 #include "kg_launch.h"
-#include "kg_mixed.cuh"
+#include "kg_mixed2.cuh"
 
 namespace kg {
 
@@ -43,6 +43,11 @@ __global__ void __launch_bounds__(256) samples_kernel(SampleArgs a) {
 // Even Mino grid: one thread per (pixel, chunk of `chunk` consecutive samples), items
 // chunk-major over the class-sorted pixels. Each thread evaluates its first sample (and the
 // grid's last) directly and the others by the addition-theorem recurrence (kg::ray_chunk).
+// Dynamic shared memory of the mixed kernels: one FFRay slot per thread.
+extern __shared__ float kg_ffray_smem[];
+
+__device__ __forceinline__ FFRay* ffray_slot() { return reinterpret_cast<FFRay*>(kg_ffray_smem) + threadIdx.x; }
+
 template <bool MIXED>
 __global__ void __launch_bounds__(256) stepped_kernel(SampleArgs a) {
   const uint32_t fl = *a.flags;
@@ -70,7 +75,7 @@ __global__ void __launch_bounds__(256) stepped_kernel(SampleArgs a) {
       if (a.sig) a.sig[o] = S.sig;
       if (a.mino) a.mino[o] = tau;
     };
-    if (MIXED) ray_chunk_mixed(a.obs, f, code, g0, g1, a.nsamp, ordinary_active, step_zero, emit);
+    if (MIXED) ray_chunk_ff(a.obs, f, code, g0, g1, a.nsamp, ordinary_active, step_zero, emit, ffray_slot());
     else ray_chunk(a.obs, f, code, g0, g1, a.nsamp, ordinary_active, step_zero, emit);
   }
 }
@@ -87,8 +92,15 @@ cudaError_t launch_samples(const SampleArgs& a, cudaStream_t s) {
     int64_t grid = (a.npix * nch + block - 1) / block;
     const int64_t cap = (int64_t)sms * 64;
     if (grid > cap) grid = cap;
-    if (a.mixed) stepped_kernel<true><<<(unsigned)grid, block, 0, s>>>(a);
-    else stepped_kernel<false><<<(unsigned)grid, block, 0, s>>>(a);
+    if (a.mixed) {
+      const size_t smem = sizeof(FFRay) * block;
+      if (cudaFuncSetAttribute(stepped_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess)
+        return cudaGetLastError();
+      stepped_kernel<true><<<(unsigned)grid, block, smem, s>>>(a);
+    } else {
+      stepped_kernel<false><<<(unsigned)grid, block, 0, s>>>(a);
+    }
     return cudaGetLastError();
   }
   const int64_t total = total0;
@@ -144,14 +156,21 @@ __global__ void __launch_bounds__(256) batch_samples_kernel(BatchArgs a) {
         if (a.sig) a.sig[o] = S.sig;
         if (a.mino) a.mino[o] = tau;
       };
-      if (MIXED) ray_chunk_mixed(B.obs, f, code, g0, g1, B.ngeo, ordinary_active, step_zero, emit);
+      if (MIXED) ray_chunk_ff(B.obs, f, code, g0, g1, B.ngeo, ordinary_active, step_zero, emit, ffray_slot());
       else ray_chunk(B.obs, f, code, g0, g1, B.ngeo, ordinary_active, step_zero, emit);
     }
   }
 }
 
+// The mixed batch kernel's shared-memory allowance, set once per process outside any stream
+// capture (kgeo_batch_create calls it).
+cudaError_t prepare_batch_kernels() {
+  return cudaFuncSetAttribute(batch_samples_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)(sizeof(FFRay) * 256));
+}
+
 cudaError_t launch_batch_samples(const BatchArgs& a, int block, int grid, cudaStream_t s) {
-  if (a.mixed) batch_samples_kernel<true><<<grid, block, 0, s>>>(a);
+  if (a.mixed) batch_samples_kernel<true><<<grid, block, sizeof(FFRay) * block, s>>>(a);
   else batch_samples_kernel<false><<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }

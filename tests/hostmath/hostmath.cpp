@@ -2,7 +2,7 @@
 // same code the CUDA kernels compile. Test-only: never loaded by the product.
 #include "../../kgeo_gb300/csrc/kg_equatorial.cuh"
 #include "../../kgeo_gb300/csrc/kg_image.cuh"
-#include "../../kgeo_gb300/csrc/kg_mixed.cuh"
+#include "../../kgeo_gb300/csrc/kg_mixed2.cuh"
 
 using namespace kg;
 
@@ -84,16 +84,17 @@ void hm_samples_stepped(const double* ob, const double* rec, const int* code, lo
   }
 }
 void hm_samples_mixed(const double* ob, const double* rec, const int* code, long n, long G, long chunk,
-                      int ordinary_active, double* t, double* r, double* th, double* ph, double* sig, double* mino) {
+                   int ordinary_active, double* t, double* r, double* th, double* ph, double* sig, double* mino) {
   Observer o = make_obs(ob);
   for (long i = 0; i < n; ++i) {
     RecView f{rec + i, n};
     for (long g0 = 0; g0 < G; g0 += chunk) {
       long g1 = g0 + chunk < G ? g0 + chunk : G;
-      ray_chunk_mixed(o, f, code[i], g0, g1, G, ordinary_active != 0, false, [&](long g, double tau, const Sample& S) {
+      FFRay slot;
+      ray_chunk_ff(o, f, code[i], g0, g1, G, ordinary_active != 0, false, [&](long g, double tau, const Sample& S) {
         t[g * n + i] = S.t; r[g * n + i] = S.r; th[g * n + i] = S.th; ph[g * n + i] = S.ph; sig[g * n + i] = S.sig;
         mino[g * n + i] = tau;
-      });
+      }, &slot);
     }
   }
 }
@@ -198,4 +199,20 @@ void hm_image_jac(const double* ob, const int* mi, const double* md, const doubl
     }
   }
 }
+// float-float operations on split doubles: out = add, sub, mul, div, rcp(a), sqr(a), 1 - a
+void hm_ff_ops(double a, double b, double* out) {
+  ff A = ff_from(a), B = ff_from(b);
+  out[0] = ff_to_double(ff_add(A, B));
+  out[1] = ff_to_double(ff_sub(A, B));
+  out[2] = ff_to_double(ff_mul(A, B));
+  out[3] = ff_to_double(ff_div(A, B));
+  out[4] = ff_to_double(ff_rcp(A));
+  out[5] = ff_to_double(ff_sqr(A));
+  out[6] = ff_to_double(ff_one_minus(A));
+  out[7] = ff_to_double(A);
+  out[8] = ff_to_double(B);
+}
+// L(a) = ln|(1 + a) / (1 - a)| in float-float, and R_C(1, 1 + e) - 1 in FP32
+double hm_ff_logratio(double a) { return ff_to_double(ff_logratio(ff_from(a))); }
+double hm_rc_one_m1(double e) { return (double)rc_one_m1_f((float)e); }
 }

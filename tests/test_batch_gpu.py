@@ -1,7 +1,9 @@
 """GPU tests of batched tracing (kgeo_batch_*): each image of a batch equals the
-single-image trace (kgeo_ray_setup + kgeo_ray_samples) with the same chunk length, for FP64
-and the mixed-precision kernel, through direct launches, the autotuned shape and the CUDA
-graph replay; the batch includes empty images, ngeo = 0 / 1 and both hemispheres."""
+single-image trace (kgeo_ray_setup + kgeo_ray_samples) with the same chunk length — bit for
+bit in FP64, and within 1e-12 of the parity scales for the mixed-precision kernel (the two
+kernels may contract different FP32 multiply-adds) — through direct launches, the autotuned
+shape and the CUDA graph replay; the batch includes empty images, ngeo = 0 / 1 and both
+hemispheres."""
 import numpy as np
 import pytest
 import torch
@@ -39,9 +41,16 @@ def single(im, A, B, chunk, mixed):
     return out, prep
 
 
-def same(x, y):
-    return torch.equal(torch.nan_to_num(x, nan=1234.5), torch.nan_to_num(y, nan=1234.5)) and \
-        torch.equal(torch.isnan(x), torch.isnan(y))
+def same(x, y, tol=0.0, floor=1.0):
+    if not torch.equal(torch.isnan(x), torch.isnan(y)):
+        return False
+    x, y = torch.nan_to_num(x, nan=1234.5), torch.nan_to_num(y, nan=1234.5)
+    if tol == 0.0:
+        return torch.equal(x, y)
+    return bool(((x - y).abs() <= tol * torch.clamp(y.abs(), min=floor)).all())
+
+
+SCALE = {'t': 1.e4, 'sig': 1.e4, 'r': 1e-300, 'th': 1.0, 'ph': 1.0, 'mino': 1e-300}
 
 
 @pytest.mark.parametrize('precision', ['fp64', 'mixed'])
@@ -64,7 +73,8 @@ def test_batch_equals_single_images(precision):
             for k in ('t', 'r', 'th', 'ph', 'sig', 'mino'):
                 assert got[k].shape == ref[k].shape
                 if n and im['ngeo']:
-                    assert same(got[k], ref[k]), (launch, i, k)
+                    tol = 0.0 if precision == 'fp64' or k == 'mino' else 1e-12
+                    assert same(got[k], ref[k], tol, SCALE[k]), (launch, i, k)
             if n:
                 assert torch.equal(got['rclass'], prep.rclass) and torch.equal(got['thclass'], prep.thclass)
                 assert same(got['tau_tot'], prep.tau_tot)
