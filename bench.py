@@ -356,10 +356,11 @@ def _oracle_chunk(args):
     import warnings
     warnings.filterwarnings('ignore')
     out = ko.raytrace(a, R_O, th_o, A, B, ngeo)
-    return np.stack([out['r'], out['th'], out['ph'], out['t'], out['affine_times']]), out['rclass']
+    rho = ko.pole_distance(a, R_O, th_o, A, B, out['mino_times'])
+    return np.stack([out['r'], out['th'], out['ph'], out['t'], out['affine_times']]), out['rclass'], rho
 
 
-def error_stats(got, ref, rclass, torch):
+def error_stats(got, ref, rclass, torch, rho=None):
     """Per output max / RMS relative error with the parity scales; the horizon-adjacent last
     sample of rclass 2-4 rays is reported separately."""
     res = {}
@@ -377,7 +378,12 @@ def error_stats(got, ref, rclass, torch):
         mx = max(float(body.max()), float(e_rest.max()) if e_rest.numel() else 0.0)
         rms = float(torch.sqrt((body.double() ** 2).mean()))
         res[k] = {'max': mx, 'rms': rms, 'horizon_sample_max': float(last.max()) if last.numel() else 0.0,
+                  'frac_above_1e-6': float((body > 1e-6).double().mean()),
                   'nonfinite_mismatch': int((torch.isfinite(x) != torch.isfinite(y)).sum())}
+        if rho is not None:
+            # the parity rule near elliptic-Pi poles: bar max(1e-6, 1e-12 / rho) per sample
+            bar = torch.clamp(1e-12 / rho[:G - 1], min=1e-6)
+            res[k]['max_over_bar'] = float((body / bar).max())
     return res
 
 
@@ -430,7 +436,7 @@ def run_mixed(args):
     t_fp64 = timed(step_fp64, max(1, args.steps // 2), 1)
     errs = error_stats(out_m, out_d, prep.rclass, torch)
     # FP64 kernel against the oracle on a seeded 1/64 subsample of the same rays
-    orc = None
+    orc = orc_m = None
     if pool is not None:
         rng = np.random.default_rng(0)
         sub = np.sort(rng.choice(npix, npix // 64, replace=False))
@@ -439,11 +445,14 @@ def run_mixed(args):
         pool.close()
         ref = np.concatenate([p_[0] for p_ in parts], axis=2)
         rc = np.concatenate([p_[1] for p_ in parts])
+        rho = torch.from_numpy(np.concatenate([p_[2] for p_ in parts], axis=1)).to(al.device)
         idx = torch.from_numpy(sub).to(al.device)
-        got = {k: out_d[k][:, idx] for k in ('r', 'th', 'ph', 't', 'sig')}
         refd = {k: torch.from_numpy(ref[i]).to(al.device) for i, k in enumerate(('r', 'th', 'ph', 't', 'sig'))}
-        orc = error_stats(got, refd, torch.from_numpy(rc).to(al.device), torch)
+        rct = torch.from_numpy(rc).to(al.device)
+        orc = error_stats({k: out_d[k][:, idx] for k in refd}, refd, rct, torch, rho)
         orc['rays'] = int(sub.size)
+        orc_m = error_stats({k: out_m[k][:, idx] for k in refd}, refd, rct, torch, rho)
+        orc_m['rays'] = int(sub.size)
     points = npix * G
     line = {
         'metric': 'Kerr rays/s: mixed-precision raytrace (ngeo=256), 2048^2 grid + 256x4096 critical-curve band',
@@ -457,7 +466,10 @@ def run_mixed(args):
         'fp64_recurrence': {'value': npix / t_fp64, 'ms_per_step': t_fp64 * 1e3},
         'fp64_plain': {'value': npix / t_plain, 'ms_per_step': t_plain * 1e3},
         'speedup_vs_fp64_recurrence': t_fp64 / t_mixed, 'speedup_vs_fp64_plain': t_plain / t_mixed,
-        'mixed_vs_fp64_error': errs, 'fp64_vs_oracle_error': orc, 'clocks': ck,
+        'mixed_vs_fp64_error': errs, 'fp64_vs_oracle_error': orc, 'mixed_vs_oracle_error': orc_m,
+        'error_scales': 'relative; floor 1 rad for theta, phi; r_o for t, sigma; max_over_bar = max of error / '
+                        'max(1e-6, 1e-12 / rho), rho = distance to the nearest elliptic-Pi pole',
+        'clocks': ck,
         'gpu_launches': 4 * args.steps,
     }
     print(json.dumps(line))

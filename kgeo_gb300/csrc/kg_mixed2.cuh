@@ -89,7 +89,6 @@ struct FFRay {
   ff K[K_COUNT];
   float al[3], pp[3];       // case 3: alpha_i, p1_i; case 4: g_i, p2_i
   ff alf[3];                // alpha_i / g_i in float-float (the log terms multiply them exactly)
-  ff lp2[3];                // case 4: L(p2_i) = ln|(1 + p2_i) / (1 - p2_i)|
   ff ppf[3];                // p1_i / p2_i in float-float
   float drsc, dxs;          // case 2: rr31 rr43 rr41, -R_XS
   ff drscf, dxsf;           // the same in float-float (dsn2 carries the factor 2)
@@ -145,7 +144,6 @@ KG_HD void ff_ray_consts(const Observer& ob, const FV& f, int code, double step,
   for (int i = 0; i < K_COUNT; ++i) c->K[i] = ff_c(0.0f);
   c->al[0] = c->al[1] = c->al[2] = c->pp[0] = c->pp[1] = c->pp[2] = 0.0f;
   c->alf[0] = c->alf[1] = c->alf[2] = ff_c(0.0f);
-  c->lp2[0] = c->lp2[1] = c->lp2[2] = ff_c(0.0f);
   c->ppf[0] = c->ppf[1] = c->ppf[2] = ff_c(0.0f);
   c->drsc = c->dxs = 0.0f;
   c->drscf = c->dxsf = ff_c(0.0f);
@@ -222,7 +220,6 @@ KG_HD void ff_ray_consts(const Observer& ob, const FV& f, int code, double step,
       const double p2d = sqrt(al2p1 / al2j);
       c->pp[i] = (float)p2d;
       c->ppf[i] = ff_from(p2d);
-      c->lp2[i] = ff_from(log(fabs((1 + p2d) / (1 - p2d))));
       c->K[K4_AL2_0 + i] = ff_from(al2);
       c->K[K4_IP1_0 + i] = ff_from(1.0 / al2p1);
     }
@@ -321,20 +318,49 @@ KG_HD ff pi_inc_ff(const ff& nf, float c, const ff& S3, const ff& X, float rho_u
   return ff_c(pi_add_term_f(n, c, X.hi, S3.hi));
 }
 
+// Within RESEED_RHO of an elliptic-Pi pole an increment is ill-conditioned like 1/rho^2 in the
+// state's rounding, so the characteristic's Pi is re-evaluated directly in FP64 from the
+// float-float Jacobi state instead (Carlson R_F, R_J at the state's amplitude; the state's
+// ~1e-13 error then reaches Pi as ~1e-13 / rho, the conditioning of Pi itself). The zone is
+// small enough that few lanes of a warp enter it at the same step.
+constexpr float RESEED_RHO = 1.0e-3f;
+
+template <class FV>
+KG_HD ff radial_pi_direct(const FV& f, int i, const FFRadial& st, const FFState& w, const ff& Xw) {
+  const double X = ff_to_double(Xw);
+  double v;
+  const double nr = reduce_half_period(X, f[R_K2], &v);
+  const double odd = fmod(fabs(nr), 2.0) == 1.0 ? -1.0 : 1.0;
+  const double sn = odd * ff_to_double(w.sn), cn = odd * ff_to_double(w.cn), dn = ff_to_double(w.dn);
+  const double n = i == 0 ? f[R_N0] : (i == 1 ? f[R_N1] : f[R_N2]);
+  const double pic = i == 0 ? f[R_PIC0] : (i == 1 ? f[R_PIC1] : f[R_PIC2]);
+  const double s2 = sn * sn, x = cn * cn, y = dn * dn;
+  const double rf = carlson_rf(x, y, 1.0);
+  const double rj = rj_any(x, y, 1.0, 1.0 - n * s2, rf);
+  const double am = nr * PI + atan2(sn, cn);
+  (void)st;
+  return ff_from(pi_assemble(n, am, nr, sn * rf + (n / 3.0) * (s2 * sn) * rj, pic, f[R_M]));
+}
+
 // One theta step. Unlike the FP64 recurrence it does not stop at a Pi pole: the float-float
 // state carries ~48 bits, so the 1/rho amplification near a pole stays far below the mixed
 // error bars, and the increments there are taken in FP64 (pi_inc_ff).
 template <class FV>
-KG_HD void ff_theta_step(const FV& f, const FFRay& c, int code, FFTheta* st) {
+KG_HD void ff_theta_step(const FV& f, const FFRay& c, int code, double tau, FFTheta* st) {
   const FFState w = ff_jacobi_add(st->j, c.tj);
   const ff rho_w = ff_one_minus(ff_mul(ff_sqr(w.sn), c.tnf));
   const ff S3 = ff_mul(ff_mul(st->j.sn, c.tj.snv), w.sn);
   const ff q = ff_mul(ff_mul(st->j.sn, c.tj.snv), ff_mul(w.cn, w.dn));
   const ff X = ff_add(rho_w, ff_mul(q, c.tnf));
-  const ff inc = pi_inc_ff(c.tnf, c.tc, S3, X, st->rho, rho_w.hi, code_f64(code, 0), f[T_N], f[S_TC],
-                           ff_to_double(st->j.sn), -f[S_TSN], w);
   st->e = ff_sub(ff_sub(st->e, c.t_e), ff_mul(S3, c.tkkf));
-  st->pi = ff_add(ff_sub(st->pi, c.t_pi), inc);
+  if (c.tn > 0.0f && (fabsf(st->rho) < RESEED_RHO || fabsf(rho_w.hi) < RESEED_RHO)) {
+    // theta Pi from the FP64 direct evaluation at this sample
+    st->pi = ff_from(theta_state_direct(f, code, theta_snarg(f, tau)).pi);
+  } else {
+    const ff inc = pi_inc_ff(c.tnf, c.tc, S3, X, st->rho, rho_w.hi, code_f64(code, 0), f[T_N], f[S_TC],
+                             ff_to_double(st->j.sn), -f[S_TSN], w);
+    st->pi = ff_add(ff_sub(st->pi, c.t_pi), inc);
+  }
   st->j = w;
   st->rho = rho_w.hi;
 }
@@ -352,16 +378,21 @@ KG_HD void ff_radial_step(const FV& f, const FFRay& c, int code, FFRadial* st) {
   const double snu_d = ff_to_double(st->j.sn);
   const double cd[3] = {f[S_RC0], f[S_RC1], f[S_RC2]};
   const double nd[3] = {f[R_N0], f[R_N1], f[R_N2]};
+  const ff Xw = ff_sub(st->X, c.dX);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const ff X = ff_add(rho_w[i], ff_mul(q, c.rnf[i]));
-    const ff inc = pi_inc_ff(c.rnf[i], c.rc[i], S3, X, st->rho[i], rho_w[i].hi, code_f64(code, 1 + i), nd[i], cd[i],
-                             snu_d, -f[S_RSN], w);
-    st->P[i] = ff_add(ff_sub(st->P[i], c.r_p[i]), inc);
+    if (c.rn[i] > 0.0f && (fabsf(st->rho[i]) < RESEED_RHO || fabsf(rho_w[i].hi) < RESEED_RHO)) {
+      st->P[i] = radial_pi_direct(f, i, *st, w, Xw);
+    } else {
+      const ff X = ff_add(rho_w[i], ff_mul(q, c.rnf[i]));
+      const ff inc = pi_inc_ff(c.rnf[i], c.rc[i], S3, X, st->rho[i], rho_w[i].hi, code_f64(code, 1 + i), nd[i],
+                               cd[i], snu_d, -f[S_RSN], w);
+      st->P[i] = ff_add(ff_sub(st->P[i], c.r_p[i]), inc);
+    }
     st->rho[i] = rho_w[i].hi;
   }
   st->E = ff_sub(ff_sub(st->E, c.r_e), ff_mul(S3, c.rkf));
-  st->X = ff_sub(st->X, c.dX);
+  st->X = Xw;
   st->j = w;
 }
 
@@ -437,7 +468,11 @@ KG_HD ff ff_logterm(const FV& f, const FFRay& c, int code, int rc, int i, const 
     const double dn = ff_to_double(st.j.dn);
     return ff_from(ald * (0.5 * pd * log(fabs(((1 - pd) * (1 + pd * dn)) / ((1 + pd) * (1 - pd * dn))))));
   }
-  const ff L = ff_sub(ff_logratio(ff_mul(st.j.dn, c.ppf[i])), c.lp2[i]);
+  // ((1 - p2)(1 + p2 dn)) / ((1 + p2)(1 - p2 dn)) = (1 + y) / (1 - y) with
+  // y = p2 (dn - 1) / (1 - p2^2 dn) and dn - 1 = -k sn^2 / (1 + dn): no cancellation as dn -> 1
+  const ff om = ff_div(ff_mul(c.rkf, ff_sqr(st.j.sn)), ff_add_f(st.j.dn, 1.0f));
+  const ff y = ff_neg(ff_div(ff_mul(c.ppf[i], om), ff_one_minus(ff_mul(ff_sqr(c.ppf[i]), st.j.dn))));
+  const ff L = ff_logratio(y);
   return ff_mul(c.alf[i], ff_mul_f(ff_mul(L, c.ppf[i]), 0.5f));
 }
 
@@ -561,7 +596,7 @@ KG_HD void ray_chunk_ff(const Observer& ob, const FV& f, int code, int64_t g0, i
       ts = ff_theta_from(t0, c.tnf);
       rs = ff_radial_from(r0, c);
     } else {
-      ff_theta_step(f, c, code, &ts);
+      ff_theta_step(f, c, code, tau, &ts);
       ff_radial_step(f, c, code, &rs);
     }
     FFOut o;

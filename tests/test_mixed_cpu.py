@@ -70,10 +70,12 @@ def _host_mixed(a, r_o, th_o, A, B, ngeo, chunk=256):
     return dict(zip(['t', 'r', 'th', 'ph', 'sig', 'mino'], outs))
 
 
-@pytest.mark.parametrize('geom', [(0.94, 17.0, 128), (0.3, 70.0, 64)])
+@pytest.mark.parametrize('geom', [(0.94, 17.0, 128, 10.0), (0.3, 70.0, 64, 10.0), (0.94, 17.0, 256, 2.5),
+                                  (0.5, 60.0, 256, 2.5)])
 def test_host_mixed_recurrence_error_bars(geom):
-    a, th, chunk = geom[0], geom[1] * np.pi / 180, geom[2]
-    x = np.linspace(-10, 10, 20)
+    # the 2.5 M boxes hold the vortical rays and the near-unit Pi characteristics of the centre
+    a, th, chunk, lim = geom[0], geom[1] * np.pi / 180, geom[2], geom[3]
+    x = np.linspace(-lim, lim, 20)
     A, B = (v.flatten() for v in np.meshgrid(x, x))
     ref = ko.raytrace(a, 1.e4, th, A, B, 200)
     got = _host_mixed(a, 1.e4, th, A, B, 200, chunk)
@@ -83,5 +85,5 @@ def test_host_mixed_recurrence_error_bars(geom):
     rho = ko.pole_distance(a, 1.e4, th, A, B, got['mino'])
     for k, rk, scale, bar in (('r', 'r', 1e-300, 1e-9), ('th', 'th', 1.0, 5e-7), ('ph', 'ph', 1.0, 1e-6),
                               ('t', 't', 1.e4, 1e-7), ('sig', 'affine_times', 1.e4, 1e-7)):
-        e = rel_err(got[k], ref[rk], scale) / np.maximum(bar, 1e-13 / rho)
+        e = rel_err(got[k], ref[rk], scale) / np.maximum(bar, 1e-12 / rho)
         assert e[~last].max() <= 1.0, (k, e[~last].max())

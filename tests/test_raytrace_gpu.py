@@ -251,8 +251,8 @@ def test_recurrence_matches_independent_samples(kg, chunk):
 def test_mixed_precision_error_bars(kg, geom):
     """Mixed-precision (float-float) recurrence against the FP64 oracle: r 1e-9, theta 5e-7,
     phi 1e-6 (relative, floor 1), t and sigma 1e-7 of r_o; within rho = |1 - n sn^2| of an
-    elliptic-Pi pole the bar widens to 1e-13 / rho (the float-float state's rounding amplified by
-    the pole, as the FP64 bars widen by 10 eps / rho); the horizon-adjacent last sample is
+    elliptic-Pi pole the bar widens to 1e-12 / rho (the float-float state's rounding amplified by
+    the pole (~1e-12 after a 256-step chain), as the FP64 bars widen by 10 eps / rho); the last sample is
     checked at the FP64 path's bar (it is evaluated in FP64)."""
     import torch
     from oracle import kgeo_oracle as ko
@@ -272,5 +272,5 @@ def test_mixed_precision_error_bars(kg, geom):
     rho = ko.pole_distance(a, 1.e4, th, A, B, ref['mino_times'])
     for k, rk, scale, bar in (('r', 'r', 1e-300, 1e-9), ('th', 'th', 1.0, 5e-7), ('ph', 'ph', 1.0, 1e-6),
                               ('t', 't', 1.e4, 1e-7), ('sig', 'affine_times', 1.e4, 1e-7)):
-        e = rel_err(got[k], ref[rk], scale) / np.maximum(bar, 1e-13 / rho)
+        e = rel_err(got[k], ref[rk], scale) / np.maximum(bar, 1e-12 / rho)
         assert e[~last].max() <= 1.0, (k, e[~last].max())
