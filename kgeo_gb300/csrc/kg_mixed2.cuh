@@ -342,6 +342,26 @@ KG_HD ff radial_pi_direct(const FV& f, int i, const FFRadial& st, const FFState&
   return ff_from(pi_assemble(n, am, nr, sn * rf + (n / 3.0) * (s2 * sn) * rj, pic, f[R_M]));
 }
 
+// theta_state_direct's Pi from the float-float Jacobi state (no Landen): the reduced Jacobi
+// values at parameter m follow from sn, cn, dn at parameter kk (J.dn = 1 / dn, J.cn = odd cn / dn,
+// sin(phi0) dn(v|m) = odd sn / dn), the half-period count from the sample's snarg.
+template <class FV>
+KG_HD ff theta_pi_direct(const FV& f, double tau, const FFState& w) {
+  const double x = theta_snarg(f, tau) / f[T_S1M];
+  double v;
+  const double nr = reduce_half_period(x, f[T_K2], &v);
+  const double odd = fmod(fabs(nr), 2.0) == 1.0 ? -1.0 : 1.0;
+  const double dn = ff_to_double(w.dn);
+  const double idn = 1.0 / dn;
+  const double Jdn = idn, Jcn = odd * ff_to_double(w.cn) * idn, ys = odd * ff_to_double(w.sn) * idn;
+  const double n = f[T_N];
+  const double xc = Jcn * Jcn, zc = Jdn * Jdn;
+  const double rf = carlson_rf(xc, 1.0, zc);
+  const double rj = rj_any(xc, 1.0, zc, zc - n * (ys * ys), rf);
+  const double Phi = nr * PI + atan2(ys, Jcn);
+  return ff_from(pi_assemble(n, Phi, nr, ys * rf + (n / 3.0) * (ys * ys * ys) * rj, f[T_PIC], f[T_KK]));
+}
+
 // One theta step. Unlike the FP64 recurrence it does not stop at a Pi pole: the float-float
 // state carries ~48 bits, so the 1/rho amplification near a pole stays far below the mixed
 // error bars, and the increments there are taken in FP64 (pi_inc_ff).
@@ -355,7 +375,7 @@ KG_HD void ff_theta_step(const FV& f, const FFRay& c, int code, double tau, FFTh
   st->e = ff_sub(ff_sub(st->e, c.t_e), ff_mul(S3, c.tkkf));
   if (c.tn > 0.0f && (fabsf(st->rho) < RESEED_RHO || fabsf(rho_w.hi) < RESEED_RHO)) {
     // theta Pi from the FP64 direct evaluation at this sample
-    st->pi = ff_from(theta_state_direct(f, code, theta_snarg(f, tau)).pi);
+    st->pi = theta_pi_direct(f, tau, w);
   } else {
     const ff inc = pi_inc_ff(c.tnf, c.tc, S3, X, st->rho, rho_w.hi, code_f64(code, 0), f[T_N], f[S_TC],
                              ff_to_double(st->j.sn), -f[S_TSN], w);
@@ -584,9 +604,21 @@ KG_HD void ray_chunk_ff(const Observer& ob, const FV& f, int code, int64_t g0, i
   FFRadial rs;
   for (int64_t g = g0; g < g1; ++g) {
     const double tau = grid.at(g);
+    if (g == G - 1 && g != g0) {
+      // the horizon-adjacent last sample: r, I_+-, I_1, I_2 diverge there (condition ~1e10), so
+      // the radial part is the FP64 direct evaluation; theta stays well conditioned and takes
+      // its float-float step
+      ff_theta_step(f, c, code, tau, &ts);
+      FFOut o;
+      ff_theta_assemble(c, ts, &o);
+      const ThetaOut T{(double)o.th, ff_to_double(o.Gph), ff_to_double(o.Gt)};
+      const RadialState r0 = radial_state_direct(f, code, radial_X(f, tau), true);
+      emit(g, tau, combine(ob, f, tau, T, radial_assemble(f, code, tau, r0, true)));
+      continue;
+    }
     if (g == g0 || g == G - 1) {
-      // chunk start and the horizon-adjacent last sample: FP64 direct evaluation (the start
-      // seeds the float-float state; the last sample is emitted from FP64)
+      // chunk start (and a last sample that starts its chunk): FP64 direct evaluation (the start
+      // seeds the float-float state)
       const ThetaState t0 = theta_state_direct(f, code, theta_snarg(f, tau));
       const RadialState r0 = radial_state_direct(f, code, radial_X(f, tau), true);
       if (g == G - 1) {
