@@ -98,12 +98,97 @@ KG_HD bool code_minspin(int code) { return (code >> 9) & 1; }
 KG_HD bool code_step(int code) { return (code >> 10) & 1; }
 KG_HD bool code_f64(int code, int i) { return (code >> (CODE_F64_SHIFT + i)) & 1; }
 
+// One Carlson evaluation at (x, y, z) for up to three Pi's plus R_D; rho[i] = the (scaled)
+// 1 - n_i sin^2. For rho_i < 0 the DLMF 19.20.14 transform is used; rho == 0 gives +inf
+// like the reference.
+template <int NP>
+KG_HD void carlson_set(double x, double y, double z, const double* rho, double* rj, double* rd, double* rf) {
+  double p[NP + 1];
+  double q[NP];
+  bool neg[NP];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    neg[i] = !(rho[i] > 0.0);
+    q[i] = -rho[i];
+    p[i] = neg[i] ? (z * (x + y + q[i]) - x * y) / (z + q[i]) : rho[i];
+    if (rho[i] == 0.0) p[i] = z;  // placeholder, result replaced below
+  }
+  p[NP] = z;  // R_D(x,y,z) = R_J(x,y,z,z)
+  double out[NP + 1];
+  rj_multi<NP + 1>(x, y, z, p, out, rf);
+  *rd = out[NP];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    if (rho[i] == 0.0) {
+      rj[i] = kg_inf();
+    } else if (neg[i]) {
+      double pq = p[i] * q[i];
+      double xy = x * y;
+      double rc = carlson_rc(xy + pq, pq);
+      rj[i] = ((p[i] - z) * out[i] - 3.0 * (*rf) + 3.0 * sqrt((xy * z) / (xy + pq)) * rc) / (q[i] + z);
+    } else {
+      rj[i] = out[i];
+    }
+  }
+}
+
+// F(phi|m), E(phi|m) and Pi(n_i; phi|m) at one amplitude with the semantics of ellip_f,
+// ellip_e_inc and ellip_pi_ref (kgeo/scipy_ellip_binding.py:87-237 special cases included),
+// from one shared Carlson duplication at the reduced amplitude; beyond |phi| > pi/2 the periodic
+// parts come from `complete` (this function's result at pi/2 for the same m and n).
+template <int NP>
+struct EllipSet {
+  double F, E, P[NP];
+};
+
+template <int NP>
+KG_HD EllipSet<NP> ellip_set_at(double phi, double m, const double* n, const EllipSet<NP>* complete) {
+  const double nr = rint(phi / PI);
+  const double p0 = phi - nr * PI;
+  const double s = sin(p0), c = cos(p0);
+  double rho[NP], rj[NP], rd, rf;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) rho[i] = 1.0 - n[i] * s * s;
+  carlson_set<NP>(c * c, 1.0 - m * s * s, 1.0, rho, rj, &rd, &rf);
+  const double s3 = s * s * s;
+  EllipSet<NP> out;
+  const double F0 = s * rf;
+  out.F = nr == 0.0 ? F0 : F0 + 2.0 * nr * complete->F;
+  const double E0 = s * rf - (m / 3.0) * s3 * rd;
+  out.E = nr == 0.0 ? E0 : E0 + 2.0 * nr * complete->E;
+  // ellip_pi_ref's rules, tested on the full amplitude
+  const double sf = sin(phi);
+  const double yf = 1.0 - m * sf * sf;
+  const double aphi = fabs(phi);
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    const double ni = n[i];
+    const double rhof = 1.0 - ni * sf * sf;
+    double v;
+    if (aphi <= PHI_ZERO) v = phi;
+    else if (m < M_NEG_INF) v = 0.0;
+    else if (yf < 0.0) v = kg_nan();
+    else if (aphi > HALFPI && m >= 1.0) v = kg_nan();
+    else if (aphi > HALFPI && ni == 1.0) v = kg_inf();
+    else if (rhof == 0.0) v = kg_inf();
+    else if (std::isinf(ni)) v = 0.0;
+    else {
+      const double core = fabs(p0) <= PHI_ZERO && aphi > HALFPI ? p0 : s * rf + (ni / 3.0) * s3 * rj[i];
+      v = aphi > HALFPI ? 2.0 * nr * complete->P[i] + core : core;
+    }
+    out.P[i] = v;
+  }
+  return out;
+}
+
 // ---------------------------------------------------------------------------
 // building blocks at a generic amplitude (ray constants)
 // ---------------------------------------------------------------------------
 
-// S1, S2 of GL19a B92/B93 (kgeo/kerr_raytracing_ana.py:638-663) at amplitude phi.
-KG_HD void s1s2_at(double al, double phi, double j, bool want_s2, double* S1, double* S2) {
+// S1, S2 of GL19a B92/B93 (kgeo/kerr_raytracing_ana.py:638-663) at amplitude phi, from
+// F(phi|j), E(phi|j) and Pi(1 + al^2; phi|j) evaluated by the caller (ellip_set_at).
+KG_HD void s1s2_at(double al, double phi, double j, double F, double E, double Pi, bool want_s2, double* S1,
+                   double* S2) {
   double al2 = al * al;
   double al2p1 = 1 + al2;
   double al2j = 1 - j + al2;
@@ -111,10 +196,8 @@ KG_HD void s1s2_at(double al, double phi, double j, bool want_s2, double* S1, do
   double s2phi = sqrt(1. - j * (sphi * sphi));
   double p2 = sqrt(al2p1 / al2j);
   double f2 = 0.5 * p2 * log(fabs(((1 - p2) * (1 + p2 * s2phi)) / ((1 + p2) * (1 - p2 * s2phi))));
-  double F = ellip_f(phi, j);
-  *S1 = (F + al2 * ellip_pi_ref(al2p1, phi, j) - al * f2) / al2p1;
+  *S1 = (F + al2 * Pi - al * f2) / al2p1;
   if (want_s2) {
-    double E = ellip_e_inc(phi, j);
     double tanphi = tan(phi);
     double S2a = (1 - j) * F + al2 * E + al2 * s2phi * (al - tanphi) / (1 + al * tanphi) - al2 * al;
     S2a = -S2a / (al2p1 * al2j);
@@ -123,18 +206,18 @@ KG_HD void s1s2_at(double al, double phi, double j, bool want_s2, double* S1, do
   }
 }
 
-// R1, R2 of GL19a B62/B65 (kgeo/kerr_raytracing_ana.py:666-683) at amplitude phi.
-KG_HD void r1r2_at(double al, double phi, double j, bool want_r2, double* R1, double* R2) {
+// R1, R2 of GL19a B62/B65 (kgeo/kerr_raytracing_ana.py:666-683) at amplitude phi, from
+// F(phi|j), E(phi|j) and Pi(al^2 / (al^2 - 1); phi|j) evaluated by the caller.
+KG_HD void r1r2_at(double al, double phi, double j, double F, double E, double Pi, bool want_r2, double* R1,
+                   double* R2) {
   double al2 = al * al;
   double sphi = sin(phi);
   double s2phi = sqrt(1 - j * (sphi * sphi));
   double p1 = sqrt((al2 - 1) / (j + (1 - j) * al2));
   double f1 = 0.5 * p1 * log(fabs((p1 * s2phi + sphi) / (p1 * s2phi - sphi)));
   double nn = al2 / (al2 - 1);
-  *R1 = (ellip_pi_ref(nn, phi, j) - al * f1) / (1 - al2);
+  *R1 = (Pi - al * f1) / (1 - al2);
   if (want_r2) {
-    double F = ellip_f(phi, j);
-    double E = ellip_e_inc(phi, j);
     double r2 = (F - (al2 / (j + (1 - j) * al2)) * (E - al * sphi * s2phi / (1 + al * cos(phi)))) / (al2 - 1);
     *R2 = r2 + (2 * j - nn) * *R1 / (j + (1 - j) * al2);
   }
@@ -341,12 +424,16 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     }
     double pref = 1 / sqrt(-a2um);
     double arg = asin(o.cos_th / sqrt(up));
-    double F = ellip_f(arg, kk);
+    // F, E, Pi at the observer's amplitude and the complete set, each from one duplication
+    const double nth[1] = {up};
+    const EllipSet<1> cth = ellip_set_at<1>(HALFPI, kk, nth, nullptr);
+    const EllipSet<1> ath = ellip_set_at<1>(arg, kk, nth, &cth);
+    double F = ath.F;
     double Gth_o = -pref * F;
-    double Gph_o = -pref * ellip_pi_ref(up, arg, kk);
+    double Gph_o = -pref * ath.P[0];
     double Gt_o;
     if (kk == 0) Gt_o = 2 * up * pref * 0.125 * (-2 * arg + sin(2 * arg));
-    else Gt_o = 2 * up * pref * (ellip_e_inc(arg, kk) - F) / (2 * kk);
+    else Gt_o = 2 * up * pref * (ath.E - F) / (2 * kk);
     double m = kk / (kk - 1);
     f[T_SCALE] = sqrt(-a2um);
     f[T_GTH] = Gth_o;
@@ -355,9 +442,9 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     f[T_K2] = 2.0 * ellip_k(m);
     f[T_N] = up;
     f[T_KK] = kk;
-    f[T_PIC] = ellip_pi_ref(up, HALFPI, kk);
-    f[T_EC] = ellip_e(kk);
-    f[T_KC] = ellip_k(kk);
+    f[T_PIC] = cth.P[0];
+    f[T_EC] = cth.E;
+    f[T_KC] = cth.F;
     f[T_PREF] = pref;
     f[T_GPH] = Gph_o;
     f[T_GT] = Gt_o;
@@ -375,9 +462,12 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     double nu_o = asin(sqrt((o.cos2 - um) / (up - um)));
     double kk = 1 - ratio;
     double upm = (up - um) / (1. - um);
-    double Gth_o = -h * prefA * ellip_f(nu_o, kk);
-    double Gph_o = -h * prefB * ellip_pi_ref(upm, nu_o, kk);
-    double Gt_o = -h * prefC * ellip_e_inc(nu_o, kk);
+    const double nth[1] = {upm};
+    const EllipSet<1> cth = ellip_set_at<1>(HALFPI, kk, nth, nullptr);
+    const EllipSet<1> ath = ellip_set_at<1>(nu_o, kk, nth, &cth);
+    double Gth_o = -h * prefA * ath.F;
+    double Gph_o = -h * prefB * ath.P[0];
+    double Gt_o = -h * prefC * ath.E;
     double m = kk / (kk - 1);
     f[T_SCALE] = sqrt(a2um);
     f[T_GTH] = Gth_o;
@@ -386,9 +476,9 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     f[T_K2] = 2.0 * ellip_k(m);
     f[T_N] = upm;
     f[T_KK] = kk;
-    f[T_PIC] = ellip_pi_ref(upm, HALFPI, kk);
-    f[T_EC] = ellip_e(kk);
-    f[T_KC] = ellip_k(kk);
+    f[T_PIC] = cth.P[0];
+    f[T_EC] = cth.E;
+    f[T_KC] = cth.F;
     f[T_PREF] = prefB;
     f[T_GPH] = Gph_o;
     f[T_GT] = Gt_o;
@@ -417,25 +507,28 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     double gm = (g0 * x4rm - 1.) / (g0 + x4rm);
     double aux = atan(x4ro) + atan(g0);
     double pref = 2. / (CC + DD);
-    double Ir_o = pref * ellip_f(aux, k4);
+    const double nn4[3] = {1 + g0 * g0, 1 + gp * gp, 1 + gm * gm};
+    const EllipSet<3> comp = ellip_set_at<3>(HALFPI, k4, nn4, nullptr);
+    const EllipSet<3> at = ellip_set_at<3>(aux, k4, nn4, &comp);
+    double Ir_o = pref * at.F;
     double S1b0, S2b0, S1bp, S1bm, dummy;
-    s1s2_at(g0, aux, k4, true, &S1b0, &S2b0);
-    s1s2_at(gp, aux, k4, false, &S1bp, &dummy);
-    s1s2_at(gm, aux, k4, false, &S1bm, &dummy);
+    s1s2_at(g0, aux, k4, at.F, at.E, at.P[0], true, &S1b0, &S2b0);
+    s1s2_at(gp, aux, k4, at.F, at.E, at.P[1], false, &S1bp, &dummy);
+    s1s2_at(gm, aux, k4, at.F, at.E, at.P[2], false, &S1bm, &dummy);
     double aa0 = (a2i / g0) * (1 + g0 * g0);
     double aa1 = (a2i / g0 - b1);
     f[R_XS] = 1. / pref;
     f[R_IRO] = Ir_o;
     f[R_M] = k4;
-    f[R_KC] = ellip_k(k4);
+    f[R_KC] = comp.F;
     f[R_K2] = 2.0 * f[R_KC];
-    f[R_EC] = ellip_e(k4);
-    f[R_N0] = 1 + g0 * g0;
-    f[R_N1] = 1 + gp * gp;
-    f[R_N2] = 1 + gm * gm;
-    f[R_PIC0] = ellip_pi_ref(f[R_N0], HALFPI, k4);
-    f[R_PIC1] = ellip_pi_ref(f[R_N1], HALFPI, k4);
-    f[R_PIC2] = ellip_pi_ref(f[R_N2], HALFPI, k4);
+    f[R_EC] = comp.E;
+    f[R_N0] = nn4[0];
+    f[R_N1] = nn4[1];
+    f[R_N2] = nn4[2];
+    f[R_PIC0] = comp.P[0];
+    f[R_PIC1] = comp.P[1];
+    f[R_PIC2] = comp.P[2];
     f[R_C0] = a2i;
     f[R_C1] = b1;
     f[R_C2] = g0;
@@ -471,25 +564,28 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     double al0 = (BB + AA) / (BB - AA);
     double aux = acos(x3ro);
     double pref = (1. / sqrt(AA * BB));
-    double Ir_o = pref * ellip_f(aux, k3);
+    double a0s = al0 * al0, aps = alp * alp, ams = alm * alm;
+    const double nn3[3] = {a0s / (a0s - 1), aps / (aps - 1), ams / (ams - 1)};
+    const EllipSet<3> comp = ellip_set_at<3>(HALFPI, k3, nn3, nullptr);
+    const EllipSet<3> at = ellip_set_at<3>(aux, k3, nn3, &comp);
+    double Ir_o = pref * at.F;
     double R1b0, R2b0, R1bp, R1bm = 0.0, dummy;
-    r1r2_at(al0, aux, k3, true, &R1b0, &R2b0);
-    r1r2_at(alp, aux, k3, false, &R1bp, &dummy);
-    if (fabs(a) > MINSPIN) r1r2_at(alm, aux, k3, false, &R1bm, &dummy);
+    r1r2_at(al0, aux, k3, at.F, at.E, at.P[0], true, &R1b0, &R2b0);
+    r1r2_at(alp, aux, k3, at.F, at.E, at.P[1], false, &R1bp, &dummy);
+    if (fabs(a) > MINSPIN) r1r2_at(alm, aux, k3, at.F, at.E, at.P[2], false, &R1bm, &dummy);
     double sAB = sqrt(AA * BB);
     f[R_XS] = 1. / pref;
     f[R_IRO] = Ir_o;
     f[R_M] = k3;
-    f[R_KC] = ellip_k(k3);
+    f[R_KC] = comp.F;
     f[R_K2] = 2.0 * f[R_KC];
-    f[R_EC] = ellip_e(k3);
-    double a0s = al0 * al0, aps = alp * alp, ams = alm * alm;
-    f[R_N0] = a0s / (a0s - 1);
-    f[R_N1] = aps / (aps - 1);
-    f[R_N2] = ams / (ams - 1);
-    f[R_PIC0] = ellip_pi_ref(f[R_N0], HALFPI, k3);
-    f[R_PIC1] = ellip_pi_ref(f[R_N1], HALFPI, k3);
-    f[R_PIC2] = ellip_pi_ref(f[R_N2], HALFPI, k3);
+    f[R_EC] = comp.E;
+    f[R_N0] = nn3[0];
+    f[R_N1] = nn3[1];
+    f[R_N2] = nn3[2];
+    f[R_PIC0] = comp.P[0];
+    f[R_PIC1] = comp.P[1];
+    f[R_PIC2] = comp.P[2];
     f[R_C0] = AA;
     f[R_C1] = BB;
     f[R_C2] = rr1;
@@ -520,33 +616,36 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     double k2 = (rr32 * rr41) / (rr31 * rr42);
     double x2ro = o.r_o_inf ? sqrt(rr31 / rr41) : sqrt((rr31 * (r_o - rr4)) / (rr41 * (r_o - rr3)));
     double aux = asin(x2ro);
-    double Ir_o = 2 * ellip_f(aux, k2) / sqrt(rr31 * rr42);
     double n1 = rr41 / rr31;
     double np = (rrp3 * rr41) / (rrp4 * rr31);
     double nm = (rrm3 * rr41) / (rrm4 * rr31);
+    const double nn2[3] = {n1, np, nm};
+    const EllipSet<3> comp = ellip_set_at<3>(HALFPI, k2, nn2, nullptr);
+    const EllipSet<3> at = ellip_set_at<3>(aux, k2, nn2, &comp);
+    double Ir_o = 2 * at.F / sqrt(rr31 * rr42);
     double Rpot_o = (r_o - rr1) * (r_o - rr2) * (r_o - rr3) * (r_o - rr4);
     double drs_o = sqrt(Rpot_o);
     double c2c = 2. / sqrt(rr31 * rr42);
     f[R_XS] = 0.5 * sqrt(rr31 * rr42);
     f[R_IRO] = Ir_o;
     f[R_M] = k2;
-    f[R_KC] = ellip_k(k2);
+    f[R_KC] = comp.F;
     f[R_K2] = 2.0 * f[R_KC];
-    f[R_EC] = ellip_e(k2);
+    f[R_EC] = comp.E;
     f[R_N0] = n1;
     f[R_N1] = np;
     f[R_N2] = nm;
-    f[R_PIC0] = ellip_pi_ref(n1, HALFPI, k2);
-    f[R_PIC1] = ellip_pi_ref(np, HALFPI, k2);
-    f[R_PIC2] = ellip_pi_ref(nm, HALFPI, k2);
+    f[R_PIC0] = comp.P[0];
+    f[R_PIC1] = comp.P[1];
+    f[R_PIC2] = comp.P[2];
     f[R_C0] = rr1;
     f[R_C1] = rr2;
     f[R_C2] = rr3;
     f[R_C3] = rr4;
-    f[R_C4] = ellip_e_inc(aux, k2);          // E(aux)
-    f[R_C5] = ellip_pi_ref(n1, aux, k2);     // Pi(n1; aux)
-    f[R_C6] = ellip_pi_ref(np, aux, k2);
-    f[R_C7] = ellip_pi_ref(nm, aux, k2);
+    f[R_C4] = at.E;                          // E(aux)
+    f[R_C5] = at.P[0];                       // Pi(n1; aux)
+    f[R_C6] = at.P[1];
+    f[R_C7] = at.P[2];
     f[R_C8] = drs_o / (r_o - rr3);           // second term of H
     f[R_C9] = c2c;
     f[R_C10] = c2c * (rr43 / (rrp3 * rrp4));
@@ -596,39 +695,6 @@ KG_HD double pi_assemble(double n, double Phi, double nr, double inc, double pic
   return nr == 0.0 ? inc : 2.0 * nr * pic + inc;
 }
 
-// One Carlson evaluation at (x, y, z) for up to three Pi's plus R_D; rho[i] = the (scaled)
-// 1 - n_i sin^2. For rho_i < 0 the DLMF 19.20.14 transform is used; rho == 0 gives +inf
-// like the reference.
-template <int NP>
-KG_HD void carlson_set(double x, double y, double z, const double* rho, double* rj, double* rd, double* rf) {
-  double p[NP + 1];
-  double q[NP];
-  bool neg[NP];
-#pragma unroll
-  for (int i = 0; i < NP; ++i) {
-    neg[i] = !(rho[i] > 0.0);
-    q[i] = -rho[i];
-    p[i] = neg[i] ? (z * (x + y + q[i]) - x * y) / (z + q[i]) : rho[i];
-    if (rho[i] == 0.0) p[i] = z;  // placeholder, result replaced below
-  }
-  p[NP] = z;  // R_D(x,y,z) = R_J(x,y,z,z)
-  double out[NP + 1];
-  rj_multi<NP + 1>(x, y, z, p, out, rf);
-  *rd = out[NP];
-#pragma unroll
-  for (int i = 0; i < NP; ++i) {
-    if (rho[i] == 0.0) {
-      rj[i] = kg_inf();
-    } else if (neg[i]) {
-      double pq = p[i] * q[i];
-      double xy = x * y;
-      double rc = carlson_rc(xy + pq, pq);
-      rj[i] = ((p[i] - z) * out[i] - 3.0 * (*rf) + 3.0 * sqrt((xy * z) / (xy + pq)) * rc) / (q[i] + z);
-    } else {
-      rj[i] = out[i];
-    }
-  }
-}
 
 // ---- addition theorems -----------------------------------------------------
 
