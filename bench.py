@@ -41,9 +41,9 @@ CPU_SAMPLE_RAYS = 16384      # rays of the bounded CPU sample (every 16th pixel 
 # per geodesic point on this workload, from the ncu capture summarised in
 # profiles/geo_samples_fp64_config2.md: (dadd + dmul + 2 dfma thread instructions) / points.
 # Used for roofline.achieved.
-FP64_FLOP_PER_POINT = 1190
+FP64_FLOP_PER_POINT = 1179
 # DRAM bytes per point of the same capture (dram__bytes_read + dram__bytes_write) / points
-DRAM_BYTES_PER_POINT = 54.6
+DRAM_BYTES_PER_POINT = 54.3
 BYTES_PER_POINT = 48          # t, r, theta, phi, sigma, Mino tau written per point (8 B each)
 L2_FLUSH_BYTES = 256 << 20
 
