@@ -217,8 +217,8 @@ int kgeo_image_adjoint(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orde
  * (ngeo_i, npix_i) row-major block at offset sum_{j<i} ngeo_j npix_j. A run is one setup pass
  * over all rays (per-image class sort) and one persistent sample kernel whose blocks pull
  * tiles of work items from a device counter. Results equal kgeo_raytrace of each image with the
- * same chunk length (FP64: bit for bit; mixed: to rounding, the kernels may contract different
- * multiply-adds). A plan and its bound buffers are used by one stream at a time.
+ * same chunk length to rounding (the kernels may contract different multiply-adds; Mino times and
+ * classes are identical). A plan and its bound buffers are used by one stream at a time.
  *
  * kgeo_batch_autotune times the sample kernel's launch shapes (block size, CTAs per SM, tile
  * length, samples per work item) on a subset of the bound batch's tiles within about budget_ms
