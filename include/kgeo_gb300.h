@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define KGEO_ABI_VERSION 1
+#define KGEO_ABI_VERSION 2
 
 /* Return codes. The argument errors correspond one-to-one to the reference's
  * exceptions (kgeo/kerr_raytracing_ana.py:59-71, kgeo/equatorial_lensing.py:100-101). */
@@ -37,7 +37,7 @@ typedef enum {
   KGEO_ERR_WORKSPACE = 7,   /* workspace too small */
   KGEO_ERR_NULL = 8,        /* a required pointer is NULL */
   KGEO_ERR_CUDA = 9,        /* a CUDA runtime call failed */
-  KGEO_ERR_MODEL = 10,      /* unknown / out-of-range emissivity or velocity model parameter */
+  KGEO_ERR_MODEL = 10,      /* unknown / out-of-range emissivity, velocity or B-field model parameter, or image option */
   KGEO_ERR_NOALLOC_SIZE = 11 /* npix above KGEO_NOALLOC_MAX_PIXELS for kgeo_raytrace_noalloc */
 } kgeo_status;
 
@@ -187,6 +187,10 @@ typedef struct {
   double* imax;     /* (npix) Imax, the total Mino time (Iobs' Imax) */
   double* nmax;     /* (npix) Nmax, make_image's outarr_n */
   double* npol;     /* (npix) nmax_poloidal, make_image's outarr_np */
+  double* Q;        /* kgeo_image_ex with polarization: cos(2 chi) I (make_image's outarr_Q) */
+  double* U;        /* kgeo_image_ex with polarization: sin(2 chi) I (outarr_U) */
+  double* lp;       /* kgeo_image_ex with pathlength: rest-frame path length (outarr_lp) */
+  double* Ie;       /* kgeo_image_ex with pathlength: emission before g^3 (outarr_Ie) */
 } kgeo_image_out;
 
 /* make_image(a, r_o, th_o, mbar_max, ...) with polarization=False, pathlength=False
@@ -196,6 +200,41 @@ typedef struct {
  * reference are zero in this mode and are not produced. */
 int kgeo_image(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha, const double* beta,
                int64_t npix, const kgeo_emission* model, kgeo_image_out* out, void* stream);
+
+/* Lab-frame magnetic field of a polarised image: Bfield(fieldtype, **kwargs).bfield_lab
+ * (kgeo/bfields.py:33-131; model functions :429-736) in the equatorial plane. Only the
+ * lab-frame B^i enter the image (calc_polquantities, kgeo/equatorial_images.py:336-487). */
+#define KGEO_BFIELD_SIMPLE 0       /* 'simple', 'rad' (1,0,0), 'vert' (0,1,0), 'tor' (0,0,1): c = (Cr, Cvert, Cph) */
+#define KGEO_BFIELD_SIMPLE_RM1 1   /* 'simple_rm1': c = (Cr, Cvert, Cph) */
+#define KGEO_BFIELD_MONOPOLE_A 2   /* 'monopoleA': c = (C, omegafac) */
+#define KGEO_BFIELD_BZ_GUESS 3     /* 'bz_guess': c = (C) */
+#define KGEO_BFIELD_BZ_MONOPOLE 4  /* 'bz_monopole': c = (C); flag = secondorder_only. f(r) in closed form */
+#define KGEO_BFIELD_BZ_PARA 5      /* 'bz_para': c = (C) */
+#define KGEO_BFIELD_POWER 6        /* 'power': c = (C, p); flag = usemono */
+#define KGEO_BFIELD_GEN_POWER 7    /* 'gen_power': c = (n_I, p_val); flag = isAbove */
+typedef struct {
+  int32_t field;  /* KGEO_BFIELD_* */
+  int32_t flag;
+  double c[3];
+} kgeo_bfield;
+
+/* make_image / Iobs options beyond the emission model (kgeo/equatorial_images.py:23-32). */
+typedef struct {
+  int32_t polarization;  /* sin(theta_B) and the EVPA from the field: calc_polquantities + calc_evpa (:524-544) */
+  int32_t pathlength;    /* I = g^3 j |l_p|, l_p from calc_pathlength_equatorial (:489-522) */
+  double diskangle;      /* full opening angle h/r of the disk for the path length (0.1 in the reference) */
+  kgeo_bfield bfield;    /* read when polarization != 0 */
+} kgeo_image_options;
+
+/* kgeo_image with options: make_image(..., bfield, polarization, pathlength, diskangle)
+ * (kgeo/equatorial_images.py:23-122, Iobs :124-264). options == NULL is kgeo_image. With
+ * polarization, sinthb is the computed sin(theta_B) and Q, U are written when non-NULL;
+ * with pathlength, lp and Ie are written when non-NULL. The reference's make_image raises
+ * for 'bz_para' with polarization=True (its complex-typed Omega reaches an in-place float
+ * multiply); here the field's real value is used. */
+int kgeo_image_ex(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha,
+                  const double* beta, int64_t npix, const kgeo_emission* model, const kgeo_image_options* options,
+                  kgeo_image_out* out, void* stream);
 
 /* Adjoint of kgeo_image's I (no counterpart in the reference): given grad_I = dL/dI
  * (npix, n_orders) for the orders mbar_lo .. mbar_lo + n_orders - 1, writes grad[7] = dL/dq for q = (a, th_o, emis_p[0], emis_p[1],

@@ -36,7 +36,18 @@ class Emission(ctypes.Structure):
 class ImageOut(ctypes.Structure):
     """kgeo_image_out."""
     _fields_ = [('I', c_void_p), ('g', c_void_p), ('r_s', c_void_p), ('Ir', c_void_p), ('sinthb', c_void_p),
-                ('imax', c_void_p), ('nmax', c_void_p), ('npol', c_void_p)]
+                ('imax', c_void_p), ('nmax', c_void_p), ('npol', c_void_p), ('Q', c_void_p), ('U', c_void_p),
+                ('lp', c_void_p), ('Ie', c_void_p)]
+
+
+class BField(ctypes.Structure):
+    """kgeo_bfield."""
+    _fields_ = [('field', c_int32), ('flag', c_int32), ('c', c_double * 3)]
+
+
+class ImageOptions(ctypes.Structure):
+    """kgeo_image_options."""
+    _fields_ = [('polarization', c_int32), ('pathlength', c_int32), ('diskangle', c_double), ('bfield', BField)]
 
 
 class BatchImage(ctypes.Structure):
@@ -52,6 +63,8 @@ class BatchConfig(ctypes.Structure):
 
 EMIS = {'bpl': 0, 'constant': 1, 'glm': 2, 'ring': 3}
 VEL = {'zamo': 0, 'infall': 1, 'kep': 2, 'cunningham': 2, 'subkep': 3, 'cunningham_subkep': 3, 'general': 4}
+BFIELD = {'simple': 0, 'rad': 0, 'vert': 0, 'tor': 0, 'simple_rm1': 1, 'monopoleA': 2, 'bz_guess': 3,
+          'bz_monopole': 4, 'bz_para': 5, 'power': 6, 'gen_power': 7}
 N_IMAGE_PARAMS = 7  # a, th_o, emis_p[0..1], vel_p[0..2]
 
 # name -> (restype, argtypes); kept in step with include/kgeo_gb300.h
@@ -76,6 +89,9 @@ SIGNATURES = {
                                           c_void_p, c_void_p, c_void_p, c_void_p]),
     'kgeo_image': (c_int, [ctypes.POINTER(Observer), c_int32, c_int32, c_void_p, c_void_p, c_int64,
                            ctypes.POINTER(Emission), ctypes.POINTER(ImageOut), c_void_p]),
+    'kgeo_image_ex': (c_int, [ctypes.POINTER(Observer), c_int32, c_int32, c_void_p, c_void_p, c_int64,
+                              ctypes.POINTER(Emission), ctypes.POINTER(ImageOptions), ctypes.POINTER(ImageOut),
+                              c_void_p]),
     'kgeo_image_adjoint_workspace_size': (c_size_t, [c_int64]),
     'kgeo_image_adjoint': (c_int, [ctypes.POINTER(Observer), c_int32, c_int32, c_void_p, c_void_p, c_int64,
                                    ctypes.POINTER(Emission), c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),

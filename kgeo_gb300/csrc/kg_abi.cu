@@ -155,6 +155,33 @@ int make_model(const kgeo_emission* m, EmissionModel* out) {
   return KGEO_OK;
 }
 
+// Image options (NULL: unpolarised, no path length). Field coefficients must be finite;
+// 'simple' fields need a non-zero coefficient (kgeo/bfields.py:87-91).
+int make_options(const kgeo_image_options* p, ImageOptions* out) {
+  out->polarization = 0;
+  out->pathlength = 0;
+  out->diskangle = 0.1;
+  out->field = FieldModel{0, 0, {0.0, 0.0, 0.0}};
+  if (!p) return KGEO_OK;
+  out->polarization = p->polarization != 0;
+  out->pathlength = p->pathlength != 0;
+  if (out->pathlength && !std::isfinite(p->diskangle)) return KGEO_ERR_MODEL;
+  out->diskangle = p->diskangle;
+  if (out->polarization) {
+    const kgeo_bfield& b = p->bfield;
+    if (b.field < KGEO_BFIELD_SIMPLE || b.field > KGEO_BFIELD_GEN_POWER) return KGEO_ERR_MODEL;
+    for (int k = 0; k < 3; ++k)
+      if (!std::isfinite(b.c[k])) return KGEO_ERR_MODEL;
+    if ((b.field == KGEO_BFIELD_SIMPLE || b.field == KGEO_BFIELD_SIMPLE_RM1) && b.c[0] == 0 && b.c[1] == 0 &&
+        b.c[2] == 0)
+      return KGEO_ERR_MODEL;
+    out->field.field = b.field;
+    out->field.flag = b.flag != 0;
+    for (int k = 0; k < 3; ++k) out->field.c[k] = b.c[k];
+  }
+  return KGEO_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -207,12 +234,20 @@ int kgeo_r_equatorial(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_order
 
 int kgeo_image(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha, const double* beta,
                int64_t npix, const kgeo_emission* model, kgeo_image_out* out, void* stream) {
+  return kgeo_image_ex(obs, mbar_lo, n_orders, alpha, beta, npix, model, nullptr, out, stream);
+}
+
+int kgeo_image_ex(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha,
+                  const double* beta, int64_t npix, const kgeo_emission* model, const kgeo_image_options* options,
+                  kgeo_image_out* out, void* stream) {
   int st = check_observer(obs);
   if (st) return st;
   if (mbar_lo < 0 || n_orders < 1) return KGEO_ERR_MBAR;
   if (npix < 0) return KGEO_ERR_LENGTHS;
   ImageArgs ia;
   st = make_model(model, &ia.model);
+  if (st) return st;
+  st = make_options(options, &ia.opts);
   if (st) return st;
   if (!out) return KGEO_ERR_NULL;
   if (npix > 0 && (!alpha || !beta || !out->I)) return KGEO_ERR_NULL;
@@ -230,6 +265,11 @@ int kgeo_image(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, cons
   ia.imax = out->imax;
   ia.nmax = out->nmax;
   ia.npol = out->npol;
+  const bool ex = options != nullptr;
+  ia.Q = (ex && ia.opts.polarization) ? out->Q : nullptr;
+  ia.U = (ex && ia.opts.polarization) ? out->U : nullptr;
+  ia.lp = (ex && ia.opts.pathlength) ? out->lp : nullptr;
+  ia.Ie = (ex && ia.opts.pathlength) ? out->Ie : nullptr;
   return launch_image(ia, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
 }
 
@@ -325,7 +365,7 @@ const char* kgeo_status_string(int status) {
     case KGEO_ERR_WORKSPACE: return "workspace too small";
     case KGEO_ERR_NULL: return "a required pointer is NULL";
     case KGEO_ERR_CUDA: return "CUDA runtime error";
-    case KGEO_ERR_MODEL: return "emissivity / velocity model parameter out of range";
+    case KGEO_ERR_MODEL: return "emissivity / velocity / B-field model or image option out of range";
     case KGEO_ERR_NOALLOC_SIZE: return "npix exceeds KGEO_NOALLOC_MAX_PIXELS (kgeo_raytrace_noalloc)";
     default: return "unknown status";
   }

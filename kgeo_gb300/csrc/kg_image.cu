@@ -5,6 +5,9 @@
 
 namespace kg {
 
+// OPTS: polarisation and / or path length requested (kg_polar.cuh); the plain image keeps
+// the shorter kernel.
+template <bool OPTS>
 __global__ void __launch_bounds__(IMAGE_BLOCK) image_kernel(ImageArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.npix) return;
@@ -16,16 +19,26 @@ __global__ void __launch_bounds__(IMAGE_BLOCK) image_kernel(ImageArgs a) {
     pixel_geo(o, alpha, beta, a.mbar_lo + m0, n, &p);
     for (int j = 0; j < n; ++j) {
       const int64_t k = i * a.nord + m0 + j;
-      double I = 0.0, g = 0.0, sb = 0.0;
+      PixelOut px{0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
       if (!image_zero(a.model, o, p, j)) {
-        emission_px(a.model, o, p, j, &I, &g);
-        sb = a.model.sinthb;
+        if (OPTS) {
+          emission_px_opts(a.model, a.opts, o, p, j, alpha, beta, &px);
+        } else {
+          emission_px(a.model, o, p, j, &px.I, &px.g);
+          px.sinthb = a.model.sinthb;
+        }
       }
-      a.I[k] = I;
-      if (a.g) a.g[k] = g;
+      a.I[k] = px.I;
+      if (a.g) a.g[k] = px.g;
       if (a.r_s) a.r_s[k] = p.r_s[j];
       if (a.Ir) a.Ir[k] = p.Ir[j];
-      if (a.sinthb) a.sinthb[k] = sb;
+      if (a.sinthb) a.sinthb[k] = px.sinthb;
+      if (OPTS) {
+        if (a.Q) a.Q[k] = px.Q;
+        if (a.U) a.U[k] = px.U;
+        if (a.lp) a.lp[k] = px.lp;
+        if (a.Ie) a.Ie[k] = px.Ie;
+      }
     }
   }
   if (a.imax) a.imax[i] = p.Imax;
@@ -35,7 +48,11 @@ __global__ void __launch_bounds__(IMAGE_BLOCK) image_kernel(ImageArgs a) {
 
 cudaError_t launch_image(const ImageArgs& a, cudaStream_t s) {
   if (a.npix <= 0) return cudaSuccess;
-  image_kernel<<<(unsigned)image_adjoint_blocks(a.npix), IMAGE_BLOCK, 0, s>>>(a);
+  const unsigned nb = (unsigned)image_adjoint_blocks(a.npix);
+  if (a.opts.polarization || a.opts.pathlength)
+    image_kernel<true><<<nb, IMAGE_BLOCK, 0, s>>>(a);
+  else
+    image_kernel<false><<<nb, IMAGE_BLOCK, 0, s>>>(a);
   return cudaGetLastError();
 }
 

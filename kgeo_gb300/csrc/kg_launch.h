@@ -4,7 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
-#include "kg_image.cuh"
+#include "kg_polar.cuh"
 
 namespace kg {
 
@@ -137,6 +137,11 @@ struct ImageArgs {
   double* imax;   // (npix)
   double* nmax;   // (npix)
   double* npol;   // (npix)
+  ImageOptions opts;
+  double* Q;      // polarised: cos(2 chi) I
+  double* U;      // polarised: sin(2 chi) I
+  double* lp;     // path length (pathlength)
+  double* Ie;     // emission before g^3 (pathlength)
 };
 
 // Adjoint of the image: sum over pixels and orders of grad_I * dI/dq for the NQ parameters.

@@ -1,14 +1,16 @@
-"""Drop-in for kgeo.equatorial_images (unpolarised images of an equatorial source) on the GPU.
+"""Drop-in for kgeo.equatorial_images (images of an equatorial source) on the GPU.
 
 make_image: kgeo/equatorial_images.py:23-122; Iobs: :124-264. Same signatures, argument
 checks, defaults and output tuples. Every order of every pixel runs in one CUDA kernel
-(kgeo_image in include/kgeo_gb300.h): r_equatorial's source radius, the zero mask, the
-momentum signs, the lab-frame velocity, the redshift and the emissivity.
+(kgeo_image_ex in include/kgeo_gb300.h): r_equatorial's source radius, the zero mask, the
+momentum signs, the lab-frame velocity, the redshift, the emissivity and, with
+polarization=True, the B-field, sin(theta_B) and the EVPA (calc_polquantities, calc_evpa),
+with pathlength=True the rest-frame path length (calc_pathlength_equatorial).
 
-Scope: polarization=False and pathlength=False, equatorial emission (th_s = pi/2),
-emissivities 'bpl' / 'constant' / 'glm' / 'ring' and velocities 'zamo' / 'infall' / 'kep' /
-'cunningham' / 'subkep' / 'cunningham_subkep' / 'general'. Other options raise
-NotImplementedError (the polarised path and the B-field models are outside this package).
+Scope: equatorial emission (th_s = pi/2); emissivities 'bpl' / 'constant' / 'glm' / 'ring';
+velocities 'zamo' / 'infall' / 'kep' / 'cunningham' / 'subkep' / 'cunningham_subkep' /
+'general'; the lab-frame B-field models of kgeo_gb300.bfields. The thermal emissivity,
+tabulated ('fromfile') inputs and comoving-frame fields raise NotImplementedError.
 """
 import ctypes
 
@@ -17,6 +19,7 @@ import torch
 
 from . import _lib
 from . import device as _dev
+from .bfields import Bfield, field_struct
 from .emissivities import Emissivity
 from .velocities import Velocity
 
@@ -27,7 +30,7 @@ OBSFREQ = 230.e9
 
 emis_default = Emissivity('bpl')
 vel_default = Velocity('zamo')
-bfield_default = None
+bfield_default = Bfield('rad')
 
 
 def _p(t):
@@ -88,23 +91,45 @@ def model_params(model):
     return [model.emis_p[0], model.emis_p[1], model.vel_p[0], model.vel_p[1], model.vel_p[2]]
 
 
-def image_device(a, r_o, th_o, mbar_lo, n_orders, alpha, beta, model, outputs=('I',), stream=None):
-    """Run kgeo_image on CUDA tensors alpha, beta (npix). Returns a dict of CUDA tensors:
-    per-order outputs (npix, n_orders) among I, g, r_s, Ir, sinthb; per-pixel imax, nmax, npol."""
+def image_options(bfield=bfield_default, polarization=False, pathlength=False, diskangle=DISKANGLE):
+    """kgeo_image_options, or None for the plain unpolarised image."""
+    if getattr(bfield, 'fieldframe', 'lab') != 'lab':
+        raise NotImplementedError("comoving-frame fields are not on the GPU image path")
+    if not polarization and not pathlength:
+        return None
+    o = _lib.ImageOptions()
+    o.polarization = int(bool(polarization))
+    o.pathlength = int(bool(pathlength))
+    o.diskangle = float(diskangle)
+    if polarization:
+        o.bfield = field_struct(bfield)
+    return o
+
+
+def image_device(a, r_o, th_o, mbar_lo, n_orders, alpha, beta, model, outputs=('I',), stream=None, options=None):
+    """Run kgeo_image_ex on CUDA tensors alpha, beta (npix). Returns a dict of CUDA tensors:
+    per-order outputs (npix, n_orders) among I, g, r_s, Ir, sinthb, Q, U, lp, Ie; per-pixel
+    imax, nmax, npol. options: kgeo_image_options (image_options) or None."""
     _dev.require_cuda()
     lib = _lib.load()
     npix = alpha.numel()
     dev = alpha.device
     res = {}
-    per_order = ('I', 'g', 'r_s', 'Ir', 'sinthb')
+    per_order = ('I', 'g', 'r_s', 'Ir', 'sinthb', 'Q', 'U', 'lp', 'Ie')
     for k in set(outputs) | {'I'}:
         shape = (npix, n_orders) if k in per_order else (npix,)
         res[k] = torch.empty(shape, dtype=torch.float64, device=dev)
-    out = _lib.ImageOut(*[_p(res.get(k)) for k in ('I', 'g', 'r_s', 'Ir', 'sinthb', 'imax', 'nmax', 'npol')])
+    out = _lib.ImageOut(*[_p(res.get(k)) for k in ('I', 'g', 'r_s', 'Ir', 'sinthb', 'imax', 'nmax', 'npol',
+                                                   'Q', 'U', 'lp', 'Ie')])
     ob = _lib.Observer(float(a), float(r_o), float(th_o))
     s = stream if stream is not None else torch.cuda.current_stream(dev)
-    _lib.check(lib.kgeo_image(ctypes.byref(ob), int(mbar_lo), int(n_orders), _p(alpha), _p(beta), npix,
-                              ctypes.byref(model), ctypes.byref(out), ctypes.c_void_p(s.cuda_stream)))
+    opt = ctypes.byref(options) if options is not None else None
+    _lib.check(lib.kgeo_image_ex(ctypes.byref(ob), int(mbar_lo), int(n_orders), _p(alpha), _p(beta), npix,
+                                 ctypes.byref(model), opt, ctypes.byref(out), ctypes.c_void_p(s.cuda_stream)))
+    for k in ('Q', 'U', 'lp', 'Ie'):
+        if k in res and (options is None or (k in ('Q', 'U') and not options.polarization)
+                         or (k in ('lp', 'Ie') and not options.pathlength)):
+            res[k].zero_()
     return res
 
 
@@ -127,13 +152,9 @@ def image_adjoint_device(a, r_o, th_o, mbar_lo, n_orders, alpha, beta, model, gr
     return grad
 
 
-def _unsupported(polarization, pathlength, emissivity, th_s=np.pi / 2):
-    if polarization:
-        raise NotImplementedError("polarization=True (calc_polquantities / B-field models) is not on the GPU path")
-    if pathlength:
-        raise NotImplementedError("pathlength=True is not on the GPU path")
+def _unsupported(emissivity, th_s=np.pi / 2):
     if getattr(emissivity, 'emistype', None) == 'thermal':
-        raise NotImplementedError("the thermal emissivity needs the B-field models, not on the GPU path")
+        raise NotImplementedError("the thermal emissivity is not on the GPU image path")
     if th_s != np.pi / 2:
         raise NotImplementedError("only equatorial emission (th_s = pi/2) is on the GPU path")
 
@@ -160,10 +181,11 @@ def make_image(a, r_o, th_o, mbar_max, alpha_min, alpha_max, beta_min, beta_max,
                nu_obs=OBSFREQ,
                device_arrays=False):
     """Image in (alpha_min, alpha_max) x (beta_min, beta_max) for all orders m <= mbar_max
-    (kgeo/equatorial_images.py:23-122). Returns (I, Q, U, r, t, g, sinthb, n, np); the
-    per-order arrays are (npix, mbar_max + 1). With nmax_only=True only n and np are
-    computed (the reference leaves its return value unassigned on that branch; here the
-    tuple is returned with zero images). device_arrays=True returns CUDA tensors."""
+    (kgeo/equatorial_images.py:23-122). Returns (I, Q, U, r, t, g, sinthb, n, np), plus
+    (lp, Ie) with pathlength=True; the per-order arrays are (npix, mbar_max + 1). With
+    nmax_only=True only n and np are computed (the reference leaves its return value
+    unassigned on that branch; here the tuple is returned with zero images).
+    device_arrays=True returns CUDA tensors."""
     if not (isinstance(a, float) and (0 <= np.abs(a) < 1)):
         raise Exception("|a| should be a float in range [0,1)")
     if not (isinstance(r_o, float) and (r_o >= 100)):
@@ -172,13 +194,15 @@ def make_image(a, r_o, th_o, mbar_max, alpha_min, alpha_max, beta_min, beta_max,
         raise Exception("th_o should be a float in range (0,pi/2) or (pi/2,pi)")
     if not (isinstance(mbar_max, int) and (mbar_max >= 0)):
         raise Exception("mbar_max should be an integer >=0!")
-    _unsupported(polarization, pathlength, emissivity)
+    _unsupported(emissivity)
     A, B = image_pixels(alpha_min, alpha_max, beta_min, beta_max, psize)
     model = emission_model(emissivity, velocity, specind)
+    opts = image_options(bfield, polarization, pathlength, diskangle)
     al, be = _dev.as_device(A), _dev.as_device(B)
     n = mbar_max + 1
+    extra = ('lp', 'Ie') if pathlength else ()
     res = image_device(a, r_o, th_o, 0, n, al, be, model,
-                       outputs=('I', 'g', 'r_s', 'Ir', 'sinthb', 'nmax', 'npol'))
+                       outputs=('I', 'Q', 'U', 'g', 'r_s', 'Ir', 'sinthb', 'nmax', 'npol') + extra, options=opts)
     if nmax_only:
         from .equatorial_lensing import nmax_equatorial
         zeros = torch.zeros((A.size, n), dtype=torch.float64, device=al.device)
@@ -186,9 +210,8 @@ def make_image(a, r_o, th_o, mbar_max, alpha_min, alpha_max, beta_min, beta_max,
         outs = [zeros, zeros.clone(), zeros.clone(), zeros.clone(), zeros.clone(), zeros.clone(), zeros.clone(),
                 nmax, res['npol']]
     else:
-        zeros = torch.zeros((A.size, n), dtype=torch.float64, device=al.device)
-        outs = [res['I'], zeros, zeros.clone(), res['r_s'], res['Ir'], res['g'], res['sinthb'], res['nmax'],
-                res['npol']]
+        outs = [res['I'], res['Q'], res['U'], res['r_s'], res['Ir'], res['g'], res['sinthb'], res['nmax'],
+                res['npol']] + [res[k] for k in extra]
     if device_arrays:
         return tuple(outs)
     return tuple(_dev.to_host(outs))
@@ -198,8 +221,8 @@ def Iobs(a, r_o, th_o, mbar, alpha, beta,
          emissivity=emis_default, velocity=vel_default, bfield=bfield_default,
          polarization=False, pathlength=False, specind=SPECIND, diskangle=DISKANGLE, nu_obs=OBSFREQ,
          th_s=np.pi / 2, device_arrays=False):
-    """(Iobs, Qobs, Uobs, g, r_s, sin_thb, Ir, Imax, Nmax) of image order mbar
-    (kgeo/equatorial_images.py:124-264)."""
+    """(Iobs, Qobs, Uobs, g, r_s, sin_thb, Ir, Imax, Nmax), plus (lp, Ie) with
+    pathlength=True, of image order mbar (kgeo/equatorial_images.py:124-264)."""
     if not (isinstance(a, float) and (0 <= np.abs(a) < 1)):
         raise Exception("|a| should be a float in range [0,1)")
     if not (isinstance(r_o, float) and (r_o >= 100)):
@@ -214,14 +237,15 @@ def Iobs(a, r_o, th_o, mbar, alpha, beta,
         beta = np.array([beta]).flatten()
     if len(alpha) != len(beta):
         raise Exception("alpha, beta are different lengths!")
-    _unsupported(polarization, pathlength, emissivity, th_s)
+    _unsupported(emissivity, th_s)
     model = emission_model(emissivity, velocity, specind)
+    opts = image_options(bfield, polarization, pathlength, diskangle)
     al, be = _dev.as_device(alpha), _dev.as_device(beta)
+    extra = ('lp', 'Ie') if pathlength else ()
     res = image_device(a, r_o, th_o, mbar, 1, al, be, model,
-                       outputs=('I', 'g', 'r_s', 'Ir', 'sinthb', 'imax', 'nmax'))
-    zero = torch.zeros(al.numel(), dtype=torch.float64, device=al.device)
-    outs = [res['I'][:, 0], zero, zero.clone(), res['g'][:, 0], res['r_s'][:, 0], res['sinthb'][:, 0],
-            res['Ir'][:, 0], res['imax'], res['nmax']]
+                       outputs=('I', 'Q', 'U', 'g', 'r_s', 'Ir', 'sinthb', 'imax', 'nmax') + extra, options=opts)
+    outs = [res['I'][:, 0], res['Q'][:, 0], res['U'][:, 0], res['g'][:, 0], res['r_s'][:, 0], res['sinthb'][:, 0],
+            res['Ir'][:, 0], res['imax'], res['nmax']] + [res[k][:, 0] for k in extra]
     if device_arrays:
         return tuple(outs)
     return tuple(_dev.to_host([o.contiguous() for o in outs]))

@@ -953,11 +953,245 @@ def emissivity(a, r, emistype, kw):
     raise ValueError(emistype)
 
 
-def make_image_px(a, r_o, th_o, mbar_max, alpha, beta, emis=('bpl', {}), vel=('zamo', {}), specind=1,
-                  sinthb=np.pi / 4.):
-    """make_image's (I, Q, U, r, t, g, sinthb, n, np) on given pixels, unpolarised.
+# ----------------------------------------------------------------------------
+# polarised equatorial image: lab-frame B-field models, comoving tetrads,
+# calc_polquantities, calc_evpa, calc_pathlength_equatorial
+# ----------------------------------------------------------------------------
 
-    kgeo/equatorial_images.py:23-122 (the pixel grid is image_grid's) with Iobs :124-264.
+
+def bz_f(r):
+    """BZ monopole radial function f(r) (kgeo/bfields.py:7-13) and its derivative, in closed
+    form: Re Li2(2/r) through scipy.special.spence (spence(z) = Li2(1 - z)). The reference
+    evaluates f by linear interpolation of a table of f on [1, 100] that it does not ship
+    (kgeo/bfields.py:21-31), and 1/(4r), -1/(4r^2) beyond r = 100 (:540-543), as here."""
+    r = np.asarray(r, dtype=float)
+    x = 2. / r
+    li2 = np.real(sp.spence(1 - x + 0j))
+    lr = np.log(r / 2.)
+    with np.errstate(divide='ignore', invalid='ignore'):
+        P = li2 - np.where(r == 2., 0., np.log(np.abs(1 - x)) * lr)  # ln|1 - 2/r| ln(r/2) -> 0 at r = 2
+    f = P * r * r * (2 * r - 3) / 8.
+    f += (1 + 3 * r - 6 * r * r) * lr / 12.
+    f += 11. / 72. + 1. / (3. * r) + r / 2. - r * r / 2.
+    with np.errstate(invalid='ignore', divide='ignore'):
+        q = np.where(r == 2., 0.5, np.log1p((r - 2.) / 2.) / (r - 2.))
+    dP = -2. * q / r
+    fp = dP * r * r * (2 * r - 3) / 8. + P * 3. * r * (r - 1) / 4.
+    fp += (3 - 12 * r) * lr / 12. + (1 + 3 * r - 6 * r * r) / (12. * r)
+    fp += -1. / (3. * r * r) + 0.5 - r
+    big = r > 100.
+    f = np.where(big, 1. / (4. * r), f)
+    fp = np.where(big, -1. / (4. * r * r), fp)
+    return f, fp
+
+
+def bfield_lab(a, r, fieldtype, kw, th=np.pi / 2):
+    """Lab-frame B^i = *F^{i0} of Bfield(fieldtype, **kw).bfield_lab(a, r, th)
+    (kgeo/bfields.py:93-131) with the model functions :429-736."""
+    r = np.asarray(r, dtype=float)
+    a2 = a ** 2
+    r2 = r ** 2
+    sth = np.sin(th)
+    cth = np.cos(th)
+    abscth = np.abs(cth)
+    cth2 = cth ** 2
+    sth2 = sth ** 2
+    Delta = r2 - 2 * r + a2
+    Sigma = r2 + a2 * cth2
+    gdet = sth * Sigma
+    rp = 1 + np.sqrt(1 - a2)
+    if fieldtype in ('rad', 'vert', 'tor', 'simple', 'simple_rm1'):
+        coef = {'rad': (1, 0, 0), 'vert': (0, 1, 0), 'tor': (0, 0, 1)}.get(
+            fieldtype, (kw.get('Cr', 0), kw.get('Cvert', 0), kw.get('Cph', 0)))
+        arad, avert, ator = coef
+        gd = np.abs(sth) * Sigma
+        if fieldtype == 'simple_rm1':
+            Br = arad * (r * sth / gd) + avert * (r * cth / gd)
+        else:
+            Br = arad * (sth / gd) + avert * (r * cth / gd)
+        return Br, avert * (-sth / gd), ator * (1. / gd)
+    C = kw.get('C', 1)
+    if fieldtype == 'monopoleA':
+        omegah = a / (2 * rp)
+        phih = 4 * np.pi * C
+        omegaf = kw.get('omegafac', 0.5) * omegah
+        I = phih * (sth ** 2) * rp * (omegaf - omegah) / (rp ** 2 + a ** 2 * cth ** 2)
+        return (phih / (4 * np.pi)) / Sigma, 0 * r, I / (2 * np.pi * Delta * (sth ** 2))
+    if fieldtype == 'bz_guess':
+        Pi = (r2 + a2) ** 2 - a2 * Delta * sth2
+        OmegaH = a / (2 * rp)
+        spin = np.abs(a)
+        f2 = (6 * np.pi * np.pi - 49.) / 72.
+        omega2 = 1. / 32. - (4 * f2 - 1) * sth2 / 64.
+        OmegaBZ = spin * (1. / 8.) + (spin ** 3) * omega2
+        if a < 0:
+            OmegaBZ *= -1
+        Br = C / r2
+        return Br, 0 * Br, (-1 * (OmegaH - OmegaBZ) * np.sqrt(Pi) / Delta) * Br
+    if fieldtype == 'bz_monopole':
+        fr, frp = bz_f(r)
+        f2 = (6 * np.pi * np.pi - 49.) / 72.
+        omega2 = 1. / 32. - sth2 * (4 * f2 - 1) / 64.
+        if kw.get('secondorder_only', False):
+            Br = C / r2 + C * a2 * (-cth2 / (r2 * r2) + fr * (0.5 + 1.5 * np.cos(2 * th)) / r2)
+            Bth = -C * a2 * frp * cth * sth / r2
+            Bph = -C * 0.125 * a / (r2 - 2 * r) + C * (a ** 3) * (0.125 / ((r2 - 2 * r) ** 2)
+                                                                - (omega2 + 0.25 * cth2 * fr) / (r2 - 2 * r))
+            return Br, Bth, Bph
+        dphidtheta = C * sth * (1 + 0.5 * a2 * fr * (1 + 3 * np.cos(2 * th)))
+        dphidr = C * a2 * sth2 * cth * frp
+        I = -1 * C * 2 * np.pi * sth2 * (a / 8. + (a ** 3) * (omega2 + 0.25 * fr * cth2))
+        return dphidtheta / gdet, -dphidr / gdet, I / (2 * np.pi * Delta * sth2)
+    if fieldtype == 'bz_para':
+        psi = r * (1 - abscth) + rp * (1 + abscth) * (1 - np.log(1 + abscth)) - 2 * rp * (1 - np.log(2))
+        dpsidtheta = np.sign(cth) * sth * (r + rp * np.log(1 + abscth))
+        dpsidr = 1 - abscth
+        argvals = -psi / rp + np.log(4)
+        w = sp.lambertw(argvals, k=0)
+        x = np.exp(w)
+        y = 1 + psi / (1 + w) / (x * (2 - x))
+        om = np.real(a / 4 / y)
+        OmegaBZ = np.where(argvals >= -1 / np.e, C * om, 0.)
+        I = -4 * np.pi * psi * OmegaBZ * np.sign(cth)
+        return C * dpsidtheta / gdet, -C * dpsidr / gdet, I / (2 * np.pi * Delta * sth2)
+    if fieldtype == 'power':
+        p = kw.get('p', 1)
+        psi = r ** p * (1 - abscth)
+        dpsidtheta = np.sign(cth) * sth * (r ** p)
+        dpsidr = p * psi / r
+        if kw.get('usemono', False) or p == 0:
+            OmegaBZ = a / 8
+        else:
+            cthh = 1 - psi * rp ** (-p)
+            OmegaBZ = a / (4 + 8 / (1 + cthh))
+        if p > 0:
+            I = -4 * np.pi * psi * OmegaBZ * np.sign(cth)
+        else:
+            I = -2 * np.pi * psi * (2 - psi) * OmegaBZ * np.sign(cth)
+        return C * dpsidtheta / gdet, -C * dpsidr / gdet, I / (2 * np.pi * Delta * sth2)
+    if fieldtype == 'gen_power':
+        n_I = kw.get('n_I', 0)
+        p_val = kw.get('p_val', 1)
+        I_0 = (a * np.pi * sth2) / (rp * rp + a2 * cth2)
+        dpsidtheta = sth * ((r / rp) ** p_val)
+        if not kw.get('isAbove', True):
+            I_0 = -1 * I_0
+            dpsidtheta = -1 * dpsidtheta
+        I = I_0 * (r / rp) ** (-1 * n_I)
+        dpsidr = (1 - np.abs(cth)) * ((p_val * (r ** (p_val - 1))) / (rp ** p_val))
+        return dpsidtheta / gdet, -1 * (dpsidr / gdet), I / (2 * np.pi * Delta * sth2)
+    raise ValueError(fieldtype)
+
+
+def pol_quantities(a, r, lam, eta, kr_sign, kth_sign, u, B, th=np.pi / 2):
+    """(sinthb, kappa, cos2chi-free pieces) of calc_polquantities for a lab-frame field
+    (kgeo/equatorial_images.py:336-487) with the tetrads of Velocity.tetrades
+    (kgeo/velocities.py:124-176). u = (u0, u1, u2, u3), B = (B1, B2, B3). Returns
+    (sinthb, kappa) with kappa the complex Penrose-Walker constant."""
+    a2 = a ** 2
+    r2 = r ** 2
+    cth2 = np.cos(th) ** 2
+    sth2 = np.sin(th) ** 2
+    Delta = r2 - 2 * r + a2
+    Sigma = r2 + a2 * cth2
+    g00 = -(1 - 2 * r / Sigma)
+    g11 = Sigma / Delta
+    g22 = Sigma
+    g33 = (r2 + a2 + 2 * r * a2 * sth2 / Sigma) * sth2
+    g03 = -2 * r * a * sth2 / Sigma
+    g00_up = -(r2 + a2 + 2 * r * a2 * sth2 / Sigma) / Delta
+    g11_up = Delta / Sigma
+    g22_up = 1. / Sigma
+    g33_up = (Delta - a2 * sth2) / (Sigma * Delta * sth2)
+    g03_up = -(2 * a * r) / (Sigma * Delta)
+    u0, u1, u2, u3 = u
+    u0_l = g00 * u0 + g03 * u3
+    u1_l = g11 * u1
+    u2_l = g22 * u2
+    u3_l = g33 * u3 + g03 * u0
+    # tetrads (kgeo/velocities.py:145-168)
+    Nr = np.sqrt(-g11 * (u0_l * u0 + u3_l * u3) * (1 + u2_l * u2))
+    Nth = np.sqrt(g22 * (1 + u2_l * u2))
+    Nph = np.sqrt(-Delta * sth2 * (u0_l * u0 + u3_l * u3))
+    e0_x, e1_x, e2_x, e3_x = u1_l * u0 / Nr, -(u0_l * u0 + u3_l * u3) / Nr, 0, u1_l * u3 / Nr
+    e0_y, e1_y, e2_y, e3_y = u2_l * u0 / Nth, u2_l * u1 / Nth, (1 + u2_l * u2) / Nth, u2_l * u3 / Nth
+    e0_z, e1_z, e2_z, e3_z = u3_l / Nph, 0, 0, -u0_l / Nph
+    # fluid-frame field, e^mu = 0 (kgeo/equatorial_images.py:395-414)
+    B1, B2, B3 = B
+    b0 = B1 * u1_l + B2 * u2_l + B3 * u3_l
+    b1 = (B1 + b0 * u1) / u0
+    b2 = (B2 + b0 * u2) / u0
+    b3 = (B3 + b0 * u3) / u0
+    b0_l = g00 * b0 + g03 * b3
+    b1_l = g11 * b1
+    b2_l = g22 * b2
+    b3_l = g33 * b3 + g03 * b0
+    Bp_x = e0_x * b0_l + e1_x * b1_l + e2_x * b2_l + e3_x * b3_l
+    Bp_y = e0_y * b0_l + e1_y * b1_l + e2_y * b2_l + e3_y * b3_l
+    Bp_z = e0_z * b0_l + e1_z * b1_l + e2_z * b2_l + e3_z * b3_l
+    Bp_mag = np.sqrt(Bp_x ** 2 + Bp_y ** 2 + Bp_z ** 2)
+    # photon wavevector (kgeo/equatorial_images.py:442-462)
+    R = (r2 + a2 - a * lam) ** 2 - Delta * (eta + (lam - a) ** 2)
+    TH = eta + a2 * cth2 - lam * lam * cth2 / sth2
+    k0_l = -1
+    k1_l = kr_sign * np.sqrt(R) / Delta
+    k2_l = kth_sign * np.sqrt(TH)
+    k3_l = lam
+    k0 = g00_up * k0_l + g03_up * k3_l
+    k1 = g11_up * k1_l
+    k2 = g22_up * k2_l
+    k3 = g33_up * k3_l + g03_up * k0_l
+    kp_x = e0_x * k0_l + e1_x * k1_l + e2_x * k2_l + e3_x * k3_l
+    kp_y = e0_y * k0_l + e1_y * k1_l + e2_y * k2_l + e3_y * k3_l
+    kp_z = e0_z * k0_l + e1_z * k1_l + e2_z * k2_l + e3_z * k3_l
+    kp_mag = np.sqrt(kp_x ** 2 + kp_y ** 2 + kp_z ** 2)
+    # polarisation vector and emission angle (:470-485)
+    f_x = (kp_y * Bp_z - kp_z * Bp_y) / kp_mag
+    f_y = (kp_z * Bp_x - kp_x * Bp_z) / kp_mag
+    f_z = (kp_x * Bp_y - kp_y * Bp_x) / kp_mag
+    sinthb = np.sqrt(f_x ** 2 + f_y ** 2 + f_z ** 2) / Bp_mag
+    f0 = e0_x * f_x + e0_y * f_y + e0_z * f_z
+    f1 = e1_x * f_x + e1_y * f_y + e1_z * f_z
+    f2 = e2_x * f_x + e2_y * f_y + e2_z * f_z
+    f3 = e3_x * f_x + e3_y * f_y + e3_z * f_z
+    A = k0 * f1 - k1 * f0 + a * sth2 * (k1 * f3 - k3 * f1)
+    Bk = ((r2 + a2) * (k3 * f2 - k2 * f3) - a * (k0 * f2 - k2 * f0)) * np.sin(th)
+    kappa = (r - 1j * a * np.cos(th)) * (A - 1j * Bk)
+    return sinthb, kappa
+
+
+def evpa(a, th_o, alpha, beta, kappa):
+    """(cos 2chi, sin 2chi) at the observer by the Penrose-Walker constant;
+    kgeo/equatorial_images.py:524-544."""
+    mu = -(alpha + a * np.sin(th_o))
+    k1 = np.real(kappa)
+    k2 = np.imag(kappa)
+    den = (beta ** 2 + mu ** 2) * (k1 ** 2 + k2 ** 2)
+    c2 = ((beta * k1 + mu * k2) ** 2 - (mu * k1 - beta * k2) ** 2) / den
+    s2 = (2 * (beta * k1 + mu * k2) * (mu * k1 - beta * k2)) / den
+    return c2, s2
+
+
+def pathlength_equatorial(a, r, lam, eta, kth_sign, g, diskangle=0.1, th=np.pi / 2):
+    """Rest-frame path length through a disk of opening angle diskangle (Narayan+2021 eq 13);
+    kgeo/equatorial_images.py:489-522 (u^theta = 0, th = pi/2)."""
+    cth2 = np.cos(th) ** 2
+    sth2 = np.sin(th) ** 2
+    TH = eta + a * a * cth2 - lam * lam * cth2 / sth2
+    k2_l = kth_sign * np.sqrt(TH)
+    kyhat = -k2_l / r
+    return (diskangle * r) * ((1 / g) / kyhat)
+
+
+def make_image_px(a, r_o, th_o, mbar_max, alpha, beta, emis=('bpl', {}), vel=('zamo', {}), specind=1,
+                  sinthb=np.pi / 4., bfield=('rad', {}), polarization=False, pathlength=False, diskangle=0.1):
+    """make_image's (I, Q, U, r, t, g, sinthb, n, np [, lp, Ie]) on given pixels.
+
+    kgeo/equatorial_images.py:23-122 (the pixel grid is image_grid's) with Iobs :124-264:
+    polarization=True takes sin(theta_B) and the EVPA from calc_polquantities / calc_evpa
+    (:336-487, :524-544) for the lab-frame field ``bfield`` = (fieldtype, kwargs);
+    pathlength=True multiplies the emission by |calc_pathlength_equatorial| (:489-522) and one
+    more power of g.
     """
     emistype, ekw = emis
     veltype, vkw = vel
@@ -967,7 +1201,8 @@ def make_image_px(a, r_o, th_o, mbar_max, alpha, beta, emis=('bpl', {}), vel=('z
     lam = -alpha * np.sin(th_o)
     eta = (alpha ** 2 - a ** 2) * np.cos(th_o) ** 2 + beta ** 2
     n_pix = len(alpha)
-    out = {k: np.zeros((n_pix, mbar_max + 1)) for k in ('I', 'Q', 'U', 'r', 't', 'g', 'sinthb')}
+    keys = ('I', 'Q', 'U', 'r', 't', 'g', 'sinthb') + (('lp', 'Ie') if pathlength else ())
+    out = {k: np.zeros((n_pix, mbar_max + 1)) for k in keys}
     nmax_out = None
     for mbar in range(mbar_max + 1):
         r_s, Ir, Imax, Nmax = r_equatorial(a, r_o, th_o, mbar, alpha, beta)
@@ -976,29 +1211,42 @@ def make_image_px(a, r_o, th_o, mbar_max, alpha, beta, emis=('bpl', {}), vel=('z
             zero = zero + (r_s < cut_in)
         if cut_out > 0:
             zero = zero + (r_s > cut_out)
-        g = np.zeros(n_pix)
-        I = np.zeros(n_pix)
-        sb = np.zeros(n_pix)
+        cols = {k: np.zeros(n_pix) for k in keys}
         if np.any(~zero):
             live = ~zero
+            rl = r_s[live]
             inside = ~outside_critical(a, th_o, alpha[live], beta[live]).astype(bool)
             kr = np.where(inside + (Ir[live] <= 0.5 * Imax[live]), 1., -1.)
             kth = -1 * np.power(-1, np.mod(mbar, 2)) if th_o < 0.5 * np.pi else 1 * np.power(-1, np.mod(mbar, 2))
-            u0, u1, u2, u3 = velocity(a, r_s[live], veltype, vkw)
-            gg = redshift(a, r_s[live], lam[live], eta[live], kr, kth, u0, u1, u2, u3)
-            j = emissivity(a, r_s[live], emistype, ekw)
+            u0, u1, u2, u3 = velocity(a, rl, veltype, vkw)
+            gg = redshift(a, rl, lam[live], eta[live], kr, kth, u0, u1, u2, u3)
+            if polarization:
+                B = bfield_lab(a, rl, bfield[0], bfield[1])
+                sb, kappa = pol_quantities(a, rl, lam[live], eta[live], kr, kth, (u0, u1, u2, u3), B)
+                c2, s2 = evpa(a, th_o, alpha[live], beta[live], kappa)
+            else:
+                sb = sinthb
+            j = emissivity(a, rl, emistype, ekw)
             j = j * gg ** specind
-            j = j * sinthb ** (1 + specind)
-            g[live] = gg
-            I[live] = (gg ** 2) * j
-            sb[live] = sinthb
-        out['I'][:, mbar] = I
-        out['g'][:, mbar] = g
-        out['r'][:, mbar] = r_s
-        out['t'][:, mbar] = Ir
-        out['sinthb'][:, mbar] = sb
+            j = j * sb ** (1 + specind)
+            if pathlength:
+                lp = pathlength_equatorial(a, rl, lam[live], eta[live], kth, gg, diskangle=diskangle)
+                j = j * np.abs(lp)
+                cols['I'][live] = (gg ** 3) * j
+                cols['Ie'][live] = j
+                cols['lp'][live] = lp
+            else:
+                cols['I'][live] = (gg ** 2) * j
+            if polarization:
+                cols['Q'][live] = c2 * cols['I'][live]
+                cols['U'][live] = s2 * cols['I'][live]
+            cols['g'][live] = gg
+            cols['sinthb'][live] = sb
+        cols['r'] = r_s
+        cols['t'] = Ir
+        for k in keys:
+            out[k][:, mbar] = cols[k]
         nmax_out = Nmax
-    tau_tot = np.zeros(n_pix)
     r1, r2, r3, r4, _ = quartic_roots(a, lam, eta)
     tau_tot = mino_total(a, r_o, eta, r1, r2, r3, r4)
     out['n'] = nmax_out

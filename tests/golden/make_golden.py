@@ -8,7 +8,8 @@ The reference is imported unmodified. Its optional plotting / HDF5 / ehtim
 imports are replaced by inert stand-ins, numpy-2 removed aliases (np.infty,
 np.NaN) are restored, and the B-field data table that kgeo loads at import
 time (absent from the checkout) is regenerated into a temporary folder from
-the recipe in kgeo/bfields.py:7-20. None of those touch the hot path.
+the recipe in kgeo/bfields.py:7-20 (100000 nodes on [1, 100]); only the
+'bz_monopole' cases of the polarised-image fixture read it.
 
 Each fixture is a compressed .npz holding the inputs and the reference's
 outputs; tests/test_oracle_golden.py pins the CPU oracle to them and the GPU
@@ -71,7 +72,7 @@ def import_reference(path):
                     out += (1 + 3 * r - 6 * r * r) * np.log(r / 2.) / 12.
                     out += 11. / 72. + 1. / (3. * r) + r / 2. - r * r / 2.
                     return float(np.real(complex(out)))
-                rs = np.linspace(1, 100, 2000)
+                rs = np.linspace(1, 100, 100000)  # the nodes of the table's generator, kgeo/bfields.py:16-20
                 np.savetxt(table, np.vstack((rs, np.array([f(r) for r in rs]))))
             return open(table, 'rb')
         return orig(pkg, name)
@@ -86,8 +87,9 @@ def import_reference(path):
     import kgeo.scipy_ellip_binding as binding
     import kgeo.velocities as vel
     import kgeo.emissivities as emis
+    import kgeo.bfields as bfields
     return types.SimpleNamespace(ana=ana, utils=utils, lensing=lensing, images=images,
-                                 binding=binding, vel=vel, emis=emis)
+                                 binding=binding, vel=vel, emis=emis, bfields=bfields)
 
 
 def quiet(fn, *a, **k):
@@ -223,6 +225,89 @@ def main(path):
         for k, v in zip(['I', 'Q', 'U', 'r', 't', 'g', 'sinthb', 'n', 'np'], res):
             out['%s%d' % (k, i)] = v
     save('image_models', out)
+
+    # polarised make_image: every lab-frame B-field model, path length, r_o = inf, negative spin
+    pcases = [
+        (0.5, 60, 1.e4, 1, ('bpl', {}), ('kep', {}), ('rad', {}), False, 1.),
+        (0.9, 25, 1.e4, 2, ('ring', {'r_ring': 4.0}), ('subkep', {'fac_subkep': 0.7}), ('vert', {}), False, 1.),
+        (0.3, 130, 1.e4, 1, ('glm', {}), ('zamo', {}), ('tor', {}), False, 0.5),
+        (0.7, 45, 1.e4, 1, ('bpl', {}), ('general', {'fac_subkep': 0.6, 'beta_phi': 0.7, 'beta_r': 0.8}),
+         ('simple', {'Cr': 0.3, 'Cvert': -0.5, 'Cph': 0.8}), False, 1.),
+        (0.6, 70, 1.e4, 1, ('constant', {}), ('infall', {}), ('simple_rm1', {'Cr': 1.0, 'Cvert': 0.4, 'Cph': -0.2}),
+         False, 1.),
+        (0.8, 35, 1.e4, 1, ('bpl', {}), ('kep', {'retrograde': True}), ('monopoleA', {'C': -1, 'omegafac': 0.3}),
+         False, 1.),
+        (0.42, 60, np.inf, 2, ('ring', {}), ('general', {}), ('bz_guess', {'C': 1.}), False, 1.),
+        (-0.6, 50, 1.e4, 1, ('bpl', {}), ('subkep', {'fac_subkep': 0.8}), ('bz_guess', {'C': -1.}), False, 1.),
+        (0.9, 80, 1.e4, 1, ('glm', {}), ('kep', {}), ('power', {'p': 0.75}), False, 1.),
+        (0.3, 40, 1.e4, 1, ('bpl', {}), ('zamo', {}), ('power', {'p': 0.0, 'C': -1}), False, 1.),
+        (0.7, 55, 1.e4, 1, ('bpl', {}), ('kep', {}), ('power', {'p': 1.2, 'usemono': True}), False, 1.),
+        (0.94, 30, 1.e4, 1, ('bpl', {}), ('general', {'beta_r': 0.3}),
+         ('gen_power', {'n_I': 0.5, 'p_val': 0.8, 'isAbove': False}), False, 1.),
+        (0.5, 65, 1.e4, 1, ('bpl', {}), ('kep', {}), ('bz_monopole', {'C': 1}), False, 1.),
+        (0.5, 65, 1.e4, 1, ('bpl', {}), ('kep', {}), ('bz_monopole', {'C': 1, 'secondorder_only': True}), False, 1.),
+        (0.7, 50, 1.e4, 1, ('bpl', {}), ('general', {'fac_subkep': 0.5}), ('bz_guess', {}), True, 1.),
+    ]
+    psize = 16. / 20
+    n_side = int(np.floor(8. - -8.) / psize)
+    side = np.linspace(-8., -8. + n_side * psize, n_side)
+    Ai, Bi = np.meshgrid(side, side)
+    out = dict(alpha=Ai.flatten(), beta=Bi.flatten(), psize=psize, ncase=len(pcases))
+    for i, (a, th, r_o, mbar_max, (et, ek), (vt, vk), (bt, bk), plen, spec) in enumerate(pcases):
+        em = ref.emis.Emissivity(et, **ek)
+        ve = ref.vel.Velocity(vt, **vk)
+        bf = ref.bfields.Bfield(bt, **bk)
+        with warnings.catch_warnings():
+            warnings.simplefilter('ignore')
+            res = quiet(ref.images.make_image, a, r_o, th * deg, mbar_max, -8., 8., -8., 8., psize,
+                        emissivity=em, velocity=ve, bfield=bf, polarization=True, pathlength=plen,
+                        specind=spec)
+        out.update({'case%d' % i: repr((a, th, r_o, mbar_max, et, ek, vt, vk, bt, bk, plen, spec))})
+        names = ['I', 'Q', 'U', 'r', 't', 'g', 'sinthb', 'n', 'np'] + (['lp', 'Ie'] if plen else [])
+        for k, v in zip(names, res):
+            out['%s%d' % (k, i)] = np.real(v)
+    # pathlength=True without polarisation
+    em = ref.emis.Emissivity('bpl')
+    ve = ref.vel.Velocity('kep')
+    res = quiet(ref.images.make_image, 0.5, 1.e4, 60 * deg, 1, -8., 8., -8., 8., psize,
+                emissivity=em, velocity=ve, pathlength=True, diskangle=0.2)
+    for k, v in zip(['I', 'Q', 'U', 'r', 't', 'g', 'sinthb', 'n', 'np', 'lp', 'Ie'], res):
+        out['%s_unpol' % k] = v
+    save('image_pol', out)
+
+    # lab-frame fields of every model on a radial grid (bz_para is pinned here only: with
+    # polarization=True the reference's make_image raises for it, as its complex-typed
+    # Omega reaches an in-place float multiply in Emissivity.jrest)
+    bout = {}
+    rr = np.concatenate([np.linspace(1.05, 12., 150), np.linspace(12.5, 140., 50)])
+    models = [('rad', {}), ('vert', {}), ('tor', {}), ('simple', {'Cr': 0.3, 'Cvert': -0.5, 'Cph': 0.8}),
+              ('simple_rm1', {'Cr': 1.0, 'Cvert': 0.4, 'Cph': -0.2}), ('monopoleA', {'C': -1, 'omegafac': 0.3}),
+              ('bz_guess', {'C': 1.}), ('bz_guess', {'C': -2.}), ('bz_para', {'C': 1}), ('bz_para', {'C': -1.5}),
+              ('power', {'p': 0.75}), ('power', {'p': 0.0, 'C': -1}), ('power', {'p': 1.2, 'usemono': True}),
+              ('gen_power', {'n_I': 0.5, 'p_val': 0.8, 'isAbove': False}), ('gen_power', {}),
+              ('bz_monopole', {'C': 1}), ('bz_monopole', {'C': 1, 'secondorder_only': True})]
+    spins = (0.3, 0.9375, -0.6)
+    for i, (bt, bk) in enumerate(models):
+        bf = ref.bfields.Bfield(bt, **bk)
+        for j, a in enumerate(spins):
+            rh = 1 + np.sqrt(1 - a * a)
+            r = rr[rr > rh]
+            with warnings.catch_warnings():
+                warnings.simplefilter('ignore')
+                B = bf.bfield_lab(a, r)
+            bout['r_%d_%d' % (i, j)] = r
+            bout['B_%d_%d' % (i, j)] = np.real(np.stack([np.broadcast_to(np.asarray(b), r.shape) for b in B]))
+        bout['model%d' % i] = repr((bt, bk))
+    bout['spins'] = np.array(spins)
+    bout['nmodel'] = len(models)
+    save('bfield_lab', bout)
+
+    # EVPA of ipole images (the reference's tests/data/*.csv, from tests/test_images.py):
+    # pixel location and EVPA along the middle row / column for image orders 0 and 1
+    ip = {}
+    for name in ('lowspin_keplerian', 'midspin_inclined_keplerian', 'midspin_inclined_subkep'):
+        ip[name] = np.loadtxt(os.path.join(path, 'tests', 'data', name + '.csv'), delimiter=',', unpack=True)
+    save('ipole_evpa', ip)
 
     # elliptic Pi adapter: random in-domain points plus every special-case mask
     rng = np.random.default_rng(2)

@@ -74,6 +74,70 @@ def image(a, r_o, th_o, alpha, beta, nord, mi, md):
     return dict(zip(['I', 'g', 'r_s', 'Ir', 'sinthb', 'nmax', 'npol'], outs))
 
 
+BFIELD = {'simple': 0, 'rad': 0, 'vert': 0, 'tor': 0, 'simple_rm1': 1, 'monopoleA': 2, 'bz_guess': 3,
+          'bz_monopole': 4, 'bz_para': 5, 'power': 6, 'gen_power': 7}
+
+
+def field_arrays(fieldtype, kw):
+    """(field, flag, c[3]) of a Bfield(fieldtype, **kw), the kgeo_bfield encoding."""
+    flag = 0
+    if fieldtype in ('rad', 'vert', 'tor'):
+        c = {'rad': [1, 0, 0], 'vert': [0, 1, 0], 'tor': [0, 0, 1]}[fieldtype]
+    elif fieldtype in ('simple', 'simple_rm1'):
+        c = [kw.get('Cr', 0), kw.get('Cvert', 0), kw.get('Cph', 0)]
+    elif fieldtype == 'monopoleA':
+        c = [kw.get('C', 1), kw.get('omegafac', 0.5), 0]
+    elif fieldtype in ('bz_guess', 'bz_para'):
+        c = [kw.get('C', 1), 0, 0]
+    elif fieldtype == 'bz_monopole':
+        c = [kw.get('C', 1), 0, 0]
+        flag = int(bool(kw.get('secondorder_only', False)))
+    elif fieldtype == 'power':
+        c = [kw.get('C', 1), kw.get('p', 1), 0]
+        flag = int(bool(kw.get('usemono', False)))
+    else:
+        c = [kw.get('n_I', 0), kw.get('p_val', 1), 0]
+        flag = int(bool(kw.get('isAbove', True)))
+    return BFIELD[fieldtype], flag, np.array(c, float)
+
+
+def image_opts(a, r_o, th_o, alpha, beta, nord, mi, md, bfield=('rad', {}), polarization=True, pathlength=False,
+               diskangle=0.1):
+    L = load()
+    n = len(alpha)
+    ob = observer(a, r_o, th_o)
+    alpha = np.ascontiguousarray(alpha, float)
+    beta = np.ascontiguousarray(beta, float)
+    f, flag, c = field_arrays(*bfield)
+    oi = np.array([int(polarization), int(pathlength), f, flag], np.int32)
+    od = np.array([diskangle, c[0], c[1], c[2]], float)
+    outs = [np.zeros((n, nord)) for _ in range(7)]
+    L.hm_image_opts(dp(ob), ip(mi), dp(md), ip(oi), dp(od), dp(alpha), dp(beta), ctypes.c_long(n),
+                    ctypes.c_int(nord), *[dp(o) for o in outs])
+    return dict(zip(['I', 'Q', 'U', 'g', 'sinthb', 'lp', 'Ie'], outs))
+
+
+def bfield(a, r, fieldtype, kw):
+    L = load()
+    f, flag, c = field_arrays(fieldtype, kw)
+    r = np.ascontiguousarray(r, float)
+    out = np.zeros((len(r), 3))
+    L.hm_bfield(ctypes.c_int(f), ctypes.c_int(flag), dp(c), D(a), dp(r), ctypes.c_long(len(r)), dp(out))
+    return out.T
+
+
+def lambert_w0(z):
+    L = load()
+    L.hm_lambert_w0.restype = D
+    return L.hm_lambert_w0(D(z))
+
+
+def re_li2(x):
+    L = load()
+    L.hm_re_li2.restype = D
+    return L.hm_re_li2(D(x))
+
+
 def image_jac(a, r_o, th_o, alpha, beta, nord, mi, md):
     L = load()
     n = len(alpha)

@@ -2,6 +2,7 @@
 // same code the CUDA kernels compile. Test-only: never loaded by the product.
 #include "../../kgeo_gb300/csrc/kg_equatorial.cuh"
 #include "../../kgeo_gb300/csrc/kg_image.cuh"
+#include "../../kgeo_gb300/csrc/kg_polar.cuh"
 #include "../../kgeo_gb300/csrc/kg_mixed2.cuh"
 
 using namespace kg;
@@ -174,6 +175,41 @@ void hm_image(const double* ob, const int* mi, const double* md, const double* a
     npol[i] = p.npol;
   }
 }
+// image with options: oi = (polarization, pathlength, field, flag); od = (diskangle, c0, c1, c2).
+// outs: I, Q, U, g, sinthb, lp, Ie (npix, nord)
+void hm_image_opts(const double* ob, const int* mi, const double* md, const int* oi, const double* od,
+                   const double* alpha, const double* beta, long n, int nord, double* I, double* Q, double* U,
+                   double* g, double* sinthb, double* lp, double* Ie) {
+  Observer o = make_obs(ob);
+  EmissionModel M = make_model(mi, md);
+  ImageOptions P;
+  P.polarization = oi[0]; P.pathlength = oi[1]; P.field.field = oi[2]; P.field.flag = oi[3];
+  P.diskangle = od[0]; P.field.c[0] = od[1]; P.field.c[1] = od[2]; P.field.c[2] = od[3];
+  for (long i = 0; i < n; ++i) {
+    PixelGeo p;
+    for (int m0 = 0; m0 < nord; m0 += ORDER_GROUP) {
+      const int k = std::min(ORDER_GROUP, nord - m0);
+      pixel_geo(o, alpha[i], beta[i], m0, k, &p);
+      for (int j = 0; j < k; ++j) {
+        long q = i * nord + m0 + j;
+        PixelOut px{0, 0, 0, 0, 0, 0, 0};
+        if (!image_zero(M, o, p, j)) emission_px_opts(M, P, o, p, j, alpha[i], beta[i], &px);
+        I[q] = px.I; Q[q] = px.Q; U[q] = px.U; g[q] = px.g; sinthb[q] = px.sinthb; lp[q] = px.lp; Ie[q] = px.Ie;
+      }
+    }
+  }
+}
+// lab-frame field at (r, pi/2): out (n, 3)
+void hm_bfield(int field, int flag, const double* c, double a, const double* r, long n, double* out) {
+  FieldModel F{field, flag, {c[0], c[1], c[2]}};
+  const double rp = 1 + std::sqrt(1 - a * a);
+  for (long i = 0; i < n; ++i) {
+    BLab B = bfield_lab(F, a, r[i], rp);
+    out[3 * i] = B.b1; out[3 * i + 1] = B.b2; out[3 * i + 2] = B.b3;
+  }
+}
+double hm_lambert_w0(double z) { return lambert_w0(z); }
+double hm_re_li2(double x) { return re_li2(x); }
 // per pixel and order dI/dq (npix, nord, NQ); rs_d (npix, nord, 2) = d r_s / d(a, th_o)
 void hm_image_jac(const double* ob, const int* mi, const double* md, const double* alpha, const double* beta,
                   long n, int nord, double* jac, double* rs_d) {

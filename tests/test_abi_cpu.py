@@ -44,7 +44,7 @@ def test_ctypes_signatures_cover_header(lib):
 
 
 def test_host_only_calls(lib):
-    assert lib.kgeo_abi_version() == 1
+    assert lib.kgeo_abi_version() == 2
     assert lib.kgeo_workspace_size(1000) >= 1000 * 8 * 50
     assert lib.kgeo_status_string(1) == b'|a| should be a float in range [0,1)'
     assert lib.kgeo_status_string(2) == b'r_o should be a float > 100'

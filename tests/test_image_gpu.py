@@ -104,8 +104,12 @@ def test_model_errors():
         make_image(0.5, 1.e4, 1.0, 1, -4., 4., -4., 4., 1.0, velocity=Velocity('general', beta_r=-0.1))
     with pytest.raises(Exception, match="mbar_max should be an integer >=0!"):
         make_image(0.5, 1.e4, 1.0, -1, -4., 4., -4., 4., 1.0)
+    from kgeo_gb300.bfields import Bfield
     with pytest.raises(NotImplementedError):
-        make_image(0.5, 1.e4, 1.0, 1, -4., 4., -4., 4., 1.0, polarization=True)
+        make_image(0.5, 1.e4, 1.0, 1, -4., 4., -4., 4., 1.0, polarization=True,
+                   bfield=Bfield('const_comoving', Cr=1.))
+    with pytest.raises(Exception, match="all field coefficients are 0!"):
+        Bfield('simple')
     with pytest.raises(NotImplementedError):
         make_image(0.5, 1.e4, 1.0, 1, -4., 4., -4., 4., 1.0, velocity=Velocity('gelles'))
     with pytest.raises(Exception, match="th_o should be a float"):
