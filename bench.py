@@ -643,6 +643,148 @@ def run_image(args):
 
 
 # ---------------------------------------------------------------------------
+# polarised image: the reference's tests/test_images.py configuration at full size
+# ---------------------------------------------------------------------------
+
+POL_NX = 800
+POL_MBAR = 2
+POL_MODEL = dict(a=0.7, inc=45.0, fac_subkep=0.6, beta_phi=0.8, beta_r=0.7)
+# FP64 FLOP per pixel of the polarised image kernel (three orders), from the ncu capture in
+# profiles/image_pol_800.md: (dadd + dmul + 2 dfma thread instructions) / pixels, and the
+# FP64 pipe instructions (dadd + dmul + dfma) per pixel.
+POL_FLOP_PER_PIXEL = 10445
+POL_FP64_INST_PER_PIXEL = 6800
+CPU_POL_SAMPLE = 160000
+
+
+def pol_workload(nx=POL_NX):
+    psize = 20. / nx
+    side = np.linspace(-10., -10. + nx * psize, nx)   # make_image's grid
+    A, B = np.meshgrid(side, side)
+    return A.flatten(), B.flatten()
+
+
+def _pol_objects():
+    from kgeo_gb300.bfields import Bfield
+    from kgeo_gb300.emissivities import Emissivity
+    from kgeo_gb300.velocities import Velocity
+    m = POL_MODEL
+    return (Emissivity('ring'), Velocity('general', fac_subkep=m['fac_subkep'], beta_phi=m['beta_phi'],
+                                         beta_r=m['beta_r']), Bfield('bz_guess', C=1.))
+
+
+def _cpu_pol_chunk(args):
+    A, B = args
+    from oracle import kgeo_oracle as ko
+    import warnings
+    warnings.filterwarnings('ignore')
+    m = POL_MODEL
+    ko.make_image_px(m['a'], np.inf, m['inc'] * np.pi / 180, POL_MBAR, A, B, emis=('ring', {}),
+                     vel=('general', {'fac_subkep': m['fac_subkep'], 'beta_phi': m['beta_phi'],
+                                      'beta_r': m['beta_r']}),
+                     specind=1., bfield=('bz_guess', {'C': 1.}), polarization=True)
+    return len(A)
+
+
+def run_polimage(args):
+    small = args.case == 'polimage-small'
+    pool = cores = None
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()
+    import torch
+    from kgeo_gb300.equatorial_images import emission_model, image_device, image_options, make_image
+    nx = 160 if small else POL_NX
+    A, B = pol_workload(nx)
+    npix = A.size
+    norders = POL_MBAR + 1
+    m = POL_MODEL
+    th_o = m['inc'] * np.pi / 180
+    em, ve, bf = _pol_objects()
+    model = emission_model(em, ve, 1.)
+    opts = image_options(bf, polarization=True)
+    al = torch.from_numpy(A).cuda()
+    be = torch.from_numpy(B).cuda()
+    outs = ('I', 'Q', 'U', 'g', 'r_s', 'Ir', 'sinthb', 'nmax', 'npol')
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    for _ in range(args.warmup):
+        image_device(m['a'], np.inf, th_o, 0, norders, al, be, model, outputs=outs, options=opts)
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(args.steps):
+        image_device(m['a'], np.inf, th_o, 0, norders, al, be, model, outputs=outs, options=opts)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    t_step = e0.elapsed_time(e1) / 1e3 / args.steps
+    # end to end through the drop-in make_image: host grid in, nine host arrays out
+    for _ in range(2):
+        make_image(m['a'], np.inf, th_o, POL_MBAR, -10., 10., -10., 10., 20. / nx, emissivity=em, velocity=ve,
+                   bfield=bf, polarization=True, specind=1.)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = make_image(m['a'], np.inf, th_o, POL_MBAR, -10., 10., -10., 10., 20. / nx, emissivity=em,
+                         velocity=ve, bfield=bf, polarization=True, specind=1.)
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    lit = float((res[0] > 0).mean())
+    fp64_peak = None
+    try:
+        from kgeo_gb300 import device as dev
+        fp64_peak = dev.fp64_peak_tflops()
+    except Exception:
+        pass
+    roof = {'bound': 'fp64', 'unit': 'TFLOP/s', 'kernel': 'image_kernel<true>', 'launch_ms': t_step * 1e3,
+            'peak': fp64_peak, 'peak_source': 'FP64 FMA loop measured live by bench.py (kgeo_measure_fp64_peak)',
+            'achieved': None, 'frac': None, 'fp64_flop_per_pixel': POL_FLOP_PER_PIXEL,
+            # ncu dram__bytes_read + write of the 160x160 capture scaled by pixels; the capture's
+            # outputs (4 MB) stayed in L2, so the writes of a full launch (7 x 3 x 8 B per pixel)
+            # are not in it
+            'traffic': (1.569e6 + 1.28e3) * npix / 25600,
+            'algorithmic_bytes': npix * (16 + norders * 7 * 8 + 2 * 8)}
+    if POL_FLOP_PER_PIXEL and fp64_peak:
+        roof['achieved'] = POL_FLOP_PER_PIXEL * npix / t_step / 1e12
+        roof['frac'] = roof['achieved'] / fp64_peak
+        # the FMA loop's peak issues one FP64 instruction per 2 FLOP; dadd / dmul occupy the pipe
+        # like a dfma, so the pipe-instruction bound is fp64_peak / 2 instructions per second
+        roof['fp64_pipe_frac'] = POL_FP64_INST_PER_PIXEL * npix / t_step / (fp64_peak * 1e12 / 2)
+    cpu = None
+    if pool is not None:
+        idx = np.arange(0, npix, max(1, npix // CPU_POL_SAMPLE))[:CPU_POL_SAMPLE]
+        chunks = np.array_split(idx, cores * 2)
+        t0 = time.time()
+        pool.map(_cpu_pol_chunk, [(A[c], B[c]) for c in chunks])
+        dt = time.time() - t0
+        cpu = {'value': (idx.size / npix) / dt, 'unit': 'images/s', 'cores': cores, 'kind': 'port',
+               'sample': '%d pixels (every %dth of the %dx%d image), 3 orders, polarised; oracle/kgeo_oracle.py '
+                         'make_image_px on a %d-process pool, %.1f s wall, scaled to the full image'
+                         % (idx.size, npix // idx.size, nx, nx, cores, dt)}
+        pool.close()
+    line = {
+        'metric': 'images/s: polarised equatorial image (%dx%d, orders 0..2, I Q U sin(theta_B))' % (nx, nx),
+        'value': 1.0 / t_step, 'unit': 'images/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': t_step * 1e3, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f64', 'data': 'synthetic: make_image pixel grid over [-10, 10] M',
+        'config': {'workload': 'reference tests/test_images.py midspin_inclined_subkep: a=0.7, theta_o=45 deg, '
+                               'r_o=inf, %dx%d, orders 0..2, ring emissivity, general velocity (xi=0.6, '
+                               'beta_phi=0.8, beta_r=0.7), bz_guess field, specind 1' % (nx, nx),
+                   'npix': npix, 'orders': norders, 'case': args.case, 'lit_fraction': lit,
+                   'l2': 'inputs %d MB, outputs %d MB (compute-bound kernel; not flushed)'
+                         % (npix * 16 >> 20, npix * norders * 7 * 8 >> 20)},
+        'pixels_per_s': npix / t_step,
+        'roofline': roof, 'cpu_baseline': cpu,
+        'e2e': {'value': 1.0 / t_e2e, 'unit': 'images/s', 'h2d_bytes_per_step': 2 * 8 * npix,
+                'd2h_bytes_per_step': 8 * npix * (7 * norders + 2), 'ms_per_step': t_e2e * 1e3,
+                'path': 'kgeo_gb300.equatorial_images.make_image (host grid in, host arrays out)'},
+        'gpu_launches': args.steps, 'clocks': ck,
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
 # configuration 4: batched images (64 images, one persistent launch, CUDA graph)
 # ---------------------------------------------------------------------------
 
@@ -804,7 +946,7 @@ def main():
     p.add_argument('--warmup', type=int, default=3)
     p.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     p.add_argument('--case', choices=('full', 'small', 'mixed', 'mixed-small', 'image', 'image-small', 'batch',
-                                      'batch-small'), default='full')
+                                      'batch-small', 'polimage', 'polimage-small'), default='full')
     p.add_argument('--no-cpu-baseline', action='store_true')
     args = p.parse_args()
     if args.impl == 'reference':
@@ -813,6 +955,8 @@ def main():
         run_mixed(args)
     elif args.case.startswith('image'):
         run_image(args)
+    elif args.case.startswith('polimage'):
+        run_polimage(args)
     elif args.case.startswith('batch'):
         run_batch(args)
     else:
