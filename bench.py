@@ -239,6 +239,11 @@ def run_ours(args):
     # end to end through the public API with host buffers: numpy in, numpy out
     e2e = None
     if args.steps > 0:
+        # one untimed pass: the page-locked host outputs come from torch's pinned-memory cache
+        # in steady state
+        g = kra.raytrace_ana(a=a, observer_coords=[0, R_O, th_o, 0], image_coords=[A, B], ngeo=NGEO,
+                             plotdata=False)
+        del g
         torch.cuda.synchronize()
         t_e = time.perf_counter()
         nsteps_e = max(1, min(args.steps, 3))

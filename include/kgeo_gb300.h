@@ -99,6 +99,23 @@ int kgeo_raytrace_mixed(const kgeo_observer* obs, const double* alpha, const dou
                         int32_t ngeo, double maxtaufrac, kgeo_geodesics* out, void* workspace,
                         size_t workspace_bytes, void* stream);
 
+/* raytrace_ana with HOST buffers end to end (kgeo/kerr_raytracing_ana.py:46-122, the call a
+ * numpy caller makes): alpha, beta (npix) and every non-NULL output of `out` (t, r, th, ph,
+ * sig, mino (ngeo, npix) row-major; tau_tot, rclass, thclass (npix); flags, one word) are
+ * host pointers. The samples are computed in windows of whole recurrence chunks into a ring of
+ * device buffers, and each window is copied to the host on a second stream while the next one
+ * computes, so the device-to-host traffic (48 B per sample) overlaps the kernels; results
+ * equal kgeo_raytrace / kgeo_raytrace_mixed (precision = KGEO_PRECISION_FP64 / _MIXED).
+ * Page-locked host outputs (cudaHostAlloc, cudaHostRegister) are needed for the copies to
+ * overlap; pageable ones work but serialise. workspace: device scratch of
+ * kgeo_raytrace_host_workspace_size(npix, ngeo, precision) bytes, or NULL (allocated and freed
+ * stream-ordered). The call returns once the work is queued on `stream`; the host outputs are
+ * complete when that stream has synchronised. */
+size_t kgeo_raytrace_host_workspace_size(int64_t npix, int32_t ngeo, int32_t precision);
+int kgeo_raytrace_host(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                       int32_t ngeo, double maxtaufrac, int32_t precision, kgeo_geodesics* out, void* workspace,
+                       size_t workspace_bytes, void* stream);
+
 /* coords_at_tau(a, observer_coords, image_coords, tau, do_phi_and_t)
  * (kgeo/kerr_raytracing_ana.py:126-193): coordinates at caller-given Mino times
  * tau (ntau, npix). With do_phi_and_t == 0 only r and theta are meaningful

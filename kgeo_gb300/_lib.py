@@ -78,6 +78,9 @@ SIGNATURES = {
                                c_size_t, ctypes.POINTER(GeodesicsOut), c_void_p]),
     'kgeo_ray_samples': (c_int, [ctypes.POINTER(Observer), c_void_p, c_size_t, c_int64, c_void_p, c_int32, c_int32,
                                  c_int32, c_int32, ctypes.POINTER(GeodesicsOut), c_void_p]),
+    'kgeo_raytrace_host_workspace_size': (c_size_t, [c_int64, c_int32, c_int32]),
+    'kgeo_raytrace_host': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_int32, c_double, c_int32,
+                                   ctypes.POINTER(GeodesicsOut), c_void_p, c_size_t, c_void_p]),
     'kgeo_raytrace_mixed': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_int32, c_double,
                                     ctypes.POINTER(GeodesicsOut), c_void_p, c_size_t, c_void_p]),
     'kgeo_raytrace_noalloc': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_int32, c_double,

@@ -98,6 +98,9 @@ int samples_common(const kgeo_observer* obs, const Workspace& w, int64_t npix, i
       pa.chunk = chunk < 0 ? DEFAULT_CHUNK : (chunk > MAX_CHUNK ? MAX_CHUNK : chunk);
     pa.perm = w.perm;
     pa.mixed = mixed;
+    pa.c_begin = 0;
+    pa.c_end = -1;
+    pa.row0 = 0;
     pa.flags = w.flags;
     pa.t = out->t;
     pa.r = out->r;
@@ -182,6 +185,169 @@ int make_options(const kgeo_image_options* p, ImageOptions* out) {
   return KGEO_OK;
 }
 
+// ---------------------------------------------------------------------------
+// host-buffer raytrace: windows of whole recurrence chunks computed into a ring of device
+// buffers while the previous windows are copied to the host on a second stream
+// ---------------------------------------------------------------------------
+constexpr int HOST_RING = 4;      // device window buffers in flight (two computing, two copying)
+constexpr int HOST_WINDOWS = 8;   // target number of windows per call
+
+struct HostPlan {
+  int64_t chunk, nch, wch, nwin;
+  size_t n, base, io, slot, total;
+};
+
+HostPlan host_plan(int64_t npix, int64_t ngeo, int mixed) {
+  HostPlan h;
+  h.chunk = mixed ? DEFAULT_CHUNK_MIXED : DEFAULT_CHUNK;
+  h.nch = ngeo > 0 ? (ngeo + h.chunk - 1) / h.chunk : 0;
+  h.wch = h.nch > 0 ? (h.nch + HOST_WINDOWS - 1) / HOST_WINDOWS : 1;
+  h.nwin = h.nch > 0 ? (h.nch + h.wch - 1) / h.wch : 0;
+  h.n = (size_t)(npix > 0 ? npix : 1);
+  h.base = workspace_bytes(npix);
+  h.io = 2 * align_up(sizeof(double) * h.n, 256) + align_up(sizeof(double) * h.n, 256) +
+         2 * align_up(sizeof(int32_t) * h.n, 256);
+  h.slot = 6 * align_up(sizeof(double) * h.n * (size_t)(h.wch * h.chunk), 256);
+  h.total = h.base + h.io + (size_t)HOST_RING * h.slot;
+  return h;
+}
+
+// The copy stream, a second compute stream and the ring's events; destroying them while
+// work is queued is allowed (the driver releases them when that work completes).
+struct HostPipe {
+  cudaStream_t cs = nullptr;  // device-to-host copies
+  cudaStream_t s2 = nullptr;  // odd windows: a window's last blocks overlap the next window's first
+  cudaEvent_t done[HOST_RING] = {}, copied[HOST_RING] = {}, setup = nullptr, s2_end = nullptr;
+  bool ok = false;
+  HostPipe() {
+    ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&setup, cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&s2_end, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 0; k < HOST_RING && ok; ++k)
+      ok = cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming) == cudaSuccess &&
+           cudaEventCreateWithFlags(&copied[k], cudaEventDisableTiming) == cudaSuccess;
+  }
+  ~HostPipe() {
+    for (int k = 0; k < HOST_RING; ++k) {
+      if (done[k]) cudaEventDestroy(done[k]);
+      if (copied[k]) cudaEventDestroy(copied[k]);
+    }
+    if (setup) cudaEventDestroy(setup);
+    if (s2_end) cudaEventDestroy(s2_end);
+    if (cs) cudaStreamDestroy(cs);
+    if (s2) cudaStreamDestroy(s2);
+  }
+};
+
+int raytrace_host(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix, int64_t ngeo,
+                  double maxtaufrac, int mixed, kgeo_geodesics* out, void* workspace, size_t workspace_bytes_,
+                  cudaStream_t s) {
+  const HostPlan h = host_plan(npix, ngeo, mixed);
+  Scratch sc;
+  sc.s = s;
+  if (workspace) {
+    if (workspace_bytes_ < h.total) return KGEO_ERR_WORKSPACE;
+    sc.ptr = workspace;
+  } else {
+    if (cudaMallocAsync(&sc.ptr, h.total, s) != cudaSuccess) return KGEO_ERR_CUDA;
+    sc.owned = true;
+  }
+  char* p = static_cast<char*>(sc.ptr);
+  Workspace w = carve_workspace(p, npix);
+  p += h.base;
+  double* al = reinterpret_cast<double*>(p);
+  p += align_up(sizeof(double) * h.n, 256);
+  double* be = reinterpret_cast<double*>(p);
+  p += align_up(sizeof(double) * h.n, 256);
+  double* tau_tot = reinterpret_cast<double*>(p);
+  p += align_up(sizeof(double) * h.n, 256);
+  int32_t* rclass = reinterpret_cast<int32_t*>(p);
+  p += align_up(sizeof(int32_t) * h.n, 256);
+  int32_t* thclass = reinterpret_cast<int32_t*>(p);
+  p += align_up(sizeof(int32_t) * h.n, 256);
+  char* ring = p;
+  const size_t bytes_px = sizeof(double) * (size_t)npix;
+  if (npix > 0) {
+    if (cudaMemcpyAsync(al, alpha, bytes_px, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(be, beta, bytes_px, cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return KGEO_ERR_CUDA;
+  }
+  kgeo_geodesics per{};
+  per.tau_tot = tau_tot;
+  per.rclass = rclass;
+  per.thclass = thclass;
+  int st = setup_common(obs, al, be, npix, ngeo, maxtaufrac, w, &per, s);
+  if (st) return st;
+  HostPipe pipe;
+  if (!pipe.ok) return KGEO_ERR_CUDA;
+  double* const host_out[6] = {out->t, out->r, out->th, out->ph, out->sig, out->mino};
+  const size_t slot_arr = align_up(sizeof(double) * h.n * (size_t)(h.wch * h.chunk), 256);
+  int last = -1;
+  bool fail = cudaEventRecord(pipe.setup, s) != cudaSuccess || cudaStreamWaitEvent(pipe.s2, pipe.setup, 0) != cudaSuccess;
+  for (int64_t wi = 0; npix > 0 && wi < h.nwin && !fail; ++wi) {
+    const int k = (int)(wi % HOST_RING);
+    cudaStream_t cw = (wi & 1) ? pipe.s2 : s;
+    const int64_t cb = wi * h.wch;
+    const int64_t ce = cb + h.wch < h.nch ? cb + h.wch : h.nch;
+    const int64_t g0 = cb * h.chunk;
+    const int64_t g1 = ce * h.chunk < ngeo ? ce * h.chunk : ngeo;
+    double* slot[6];
+    for (int j = 0; j < 6; ++j) slot[j] = reinterpret_cast<double*>(ring + (size_t)k * h.slot + (size_t)j * slot_arr);
+    if (wi >= HOST_RING && cudaStreamWaitEvent(cw, pipe.copied[k], 0) != cudaSuccess) {
+      fail = true;
+      break;
+    }
+    SampleArgs pa;
+    pa.obs = make_observer(obs);
+    pa.rec = w.rec;
+    pa.code = w.code;
+    pa.npix = npix;
+    pa.nsamp = ngeo;
+    pa.tau = nullptr;
+    pa.do_phi_t = 1;
+    pa.chunk = (int)h.chunk;
+    pa.perm = w.perm;
+    pa.mixed = mixed;
+    pa.c_begin = cb;
+    pa.c_end = ce;
+    pa.row0 = g0;
+    pa.flags = w.flags;
+    pa.t = slot[0];
+    pa.r = slot[1];
+    pa.th = slot[2];
+    pa.ph = slot[3];
+    pa.sig = slot[4];
+    pa.mino = slot[5];
+    if (launch_samples(pa, cw) != cudaSuccess || cudaEventRecord(pipe.done[k], cw) != cudaSuccess ||
+        cudaStreamWaitEvent(pipe.cs, pipe.done[k], 0) != cudaSuccess) {
+      fail = true;
+      break;
+    }
+    for (int j = 0; j < 6 && !fail; ++j)
+      fail = host_out[j] && cudaMemcpyAsync(host_out[j] + g0 * npix, slot[j], bytes_px * (size_t)(g1 - g0),
+                                            cudaMemcpyDeviceToHost, pipe.cs) != cudaSuccess;
+    if (cudaEventRecord(pipe.copied[k], pipe.cs) != cudaSuccess) fail = true;
+    else last = k;
+  }
+  if (!fail && npix > 0) {
+    fail = (out->tau_tot && cudaMemcpyAsync(out->tau_tot, tau_tot, bytes_px, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+           (out->rclass && cudaMemcpyAsync(out->rclass, rclass, sizeof(int32_t) * (size_t)npix,
+                                           cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+           (out->thclass && cudaMemcpyAsync(out->thclass, thclass, sizeof(int32_t) * (size_t)npix,
+                                            cudaMemcpyDeviceToHost, s) != cudaSuccess);
+  }
+  if (!fail && out->flags)
+    fail = cudaMemcpyAsync(out->flags, w.flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess;
+  // join before anything else is queued on s (also on failure, so that the scratch is freed
+  // only after the kernels and copies that use it): the copy stream is in order, its last
+  // event covers every copy; s2_end covers the odd windows' kernels
+  if (cudaEventRecord(pipe.s2_end, pipe.s2) != cudaSuccess || cudaStreamWaitEvent(s, pipe.s2_end, 0) != cudaSuccess)
+    fail = true;
+  if (last >= 0 && cudaStreamWaitEvent(s, pipe.copied[last], 0) != cudaSuccess) fail = true;
+  return fail ? KGEO_ERR_CUDA : KGEO_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -193,6 +359,24 @@ int kgeo_raytrace(const kgeo_observer* obs, const double* alpha, const double* b
                   size_t workspace_bytes_, void* stream) {
   return trace_common(obs, alpha, beta, npix, ngeo, nullptr, 1, maxtaufrac, out, workspace, workspace_bytes_,
                       stream);
+}
+
+size_t kgeo_raytrace_host_workspace_size(int64_t npix, int32_t ngeo, int32_t precision) {
+  return host_plan(npix, ngeo, precision == KGEO_PRECISION_MIXED).total;
+}
+
+int kgeo_raytrace_host(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                       int32_t ngeo, double maxtaufrac, int32_t precision, kgeo_geodesics* out, void* workspace,
+                       size_t workspace_bytes_, void* stream) {
+  int st = check_observer(obs);
+  if (st) return st;
+  if (npix < 0) return KGEO_ERR_LENGTHS;
+  if (ngeo < 0) return KGEO_ERR_NGEO;
+  if (precision != KGEO_PRECISION_FP64 && precision != KGEO_PRECISION_MIXED) return KGEO_ERR_MODEL;
+  if (!out) return KGEO_ERR_NULL;
+  if (npix > 0 && (!alpha || !beta)) return KGEO_ERR_NULL;
+  return raytrace_host(obs, alpha, beta, npix, ngeo, maxtaufrac, precision == KGEO_PRECISION_MIXED, out, workspace,
+                       workspace_bytes_, static_cast<cudaStream_t>(stream));
 }
 
 int kgeo_raytrace_mixed(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,

@@ -76,6 +76,9 @@ struct SampleArgs {
   int chunk;            // > 0: even grid by the addition-theorem recurrence, chunk samples per thread
   const int* perm;      // class-sorted rays for the recurrence kernel
   int mixed;            // 1: mixed-precision recurrence (kg_mixed.cuh)
+  int64_t c_begin;      // recurrence kernel: chunks [c_begin, c_end) only (c_end < 0: to the last)
+  int64_t c_end;
+  int64_t row0;         // sample g is stored in row g - row0 of the outputs
   const uint32_t* flags;
   double* t;
   double* r;

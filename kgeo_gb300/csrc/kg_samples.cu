@@ -55,19 +55,21 @@ __global__ void __launch_bounds__(256) stepped_kernel(SampleArgs a) {
   const bool step_zero = (fl & FLAG_ANY_STEP_ZERO) != 0;
   const int64_t chunk = a.chunk;
   const int64_t nch = (a.nsamp + chunk - 1) / chunk;
-  const int64_t total = a.npix * nch;
+  const int64_t c_end = a.c_end < 0 ? nch : a.c_end;
+  const int64_t total = a.npix * (c_end - a.c_begin);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
     // lanes take consecutive rays of the class-sorted order at the same chunk: uniform
     // branches across the warp and (mostly) contiguous stores
-    const int64_t c = i / a.npix;
-    const int64_t p = __ldg(a.perm + (i - c * a.npix));
+    const int64_t ci = i / a.npix;
+    const int64_t c = a.c_begin + ci;
+    const int64_t p = __ldg(a.perm + (i - ci * a.npix));
     RecView f{a.rec + p, a.npix};
     const int code = __ldg(a.code + p);
     const int64_t g0 = c * chunk;
     const int64_t g1 = g0 + chunk < a.nsamp ? g0 + chunk : a.nsamp;
     auto emit = [&](int64_t g, double tau, const Sample& S) {
-      const int64_t o = g * a.npix + p;
+      const int64_t o = (g - a.row0) * a.npix + p;
       if (a.t) a.t[o] = S.t;
       if (a.r) a.r[o] = S.r;
       if (a.th) a.th[o] = S.th;
@@ -88,7 +90,9 @@ cudaError_t launch_samples(const SampleArgs& a, cudaStream_t s) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (a.tau == nullptr && a.do_phi_t && a.chunk > 0) {
     const int block = 256;
-    const int64_t nch = (a.nsamp + a.chunk - 1) / a.chunk;
+    const int64_t nch_all = (a.nsamp + a.chunk - 1) / a.chunk;
+    const int64_t nch = (a.c_end < 0 ? nch_all : a.c_end) - a.c_begin;
+    if (nch <= 0) return cudaSuccess;
     int64_t grid = (a.npix * nch + block - 1) / block;
     const int64_t cap = (int64_t)sms * 64;
     if (grid > cap) grid = cap;

@@ -88,6 +88,49 @@ def trace(a, r_o, th_o, alpha, beta, ngeo=None, tau=None, maxtaufrac=1.0 - 1.0e-
     return res
 
 
+_HOST_WS = {}
+
+
+def trace_host(a, r_o, th_o, alpha, beta, ngeo, maxtaufrac=1.0 - 1.0e-10, mixed=False, device=None):
+    """kgeo_raytrace_host: numpy alpha, beta (npix) in, numpy outputs out.
+
+    The outputs live in page-locked host tensors (torch's pinned allocator caches them), so
+    each window's device-to-host copy overlaps the next window's kernel. Returns a dict of
+    numpy arrays t, r, th, ph, sig, mino (ngeo, npix), tau_tot, rclass, thclass (npix) and
+    the flags word (int).
+    """
+    require_cuda()
+    lib = _lib.load()
+    dev = torch.device('cuda', torch.cuda.current_device()) if device is None else device
+    alpha = np.ascontiguousarray(alpha, dtype=np.float64)
+    beta = np.ascontiguousarray(beta, dtype=np.float64)
+    npix = alpha.size
+    prec = _lib.PRECISION_MIXED if mixed else _lib.PRECISION_FP64
+    need = int(lib.kgeo_raytrace_host_workspace_size(npix, int(ngeo), prec))
+    key = (dev.type, dev.index)
+    ws = _HOST_WS.get(key)
+    if ws is None or ws.numel() < need:
+        ws = _HOST_WS[key] = torch.empty(max(need, 1), dtype=torch.uint8, device=dev)
+    res = {}
+    for k in ('t', 'r', 'th', 'ph', 'sig', 'mino'):
+        res[k] = torch.empty((int(ngeo), npix), dtype=torch.float64, pin_memory=True)
+    res['tau_tot'] = torch.empty(npix, dtype=torch.float64, pin_memory=True)
+    res['rclass'] = torch.empty(npix, dtype=torch.int32, pin_memory=True)
+    res['thclass'] = torch.empty(npix, dtype=torch.int32, pin_memory=True)
+    res['flags'] = torch.zeros(1, dtype=torch.int32, pin_memory=True)
+    g = _lib.GeodesicsOut(*[_ptr(res[k]) for k in ('t', 'r', 'th', 'ph', 'sig', 'mino', 'tau_tot', 'rclass',
+                                                  'thclass', 'flags')])
+    ob = _lib.Observer(float(a), float(r_o), float(th_o))
+    s = torch.cuda.current_stream(dev)
+    _lib.check(lib.kgeo_raytrace_host(ctypes.byref(ob), ctypes.c_void_p(alpha.ctypes.data),
+                                      ctypes.c_void_p(beta.ctypes.data), npix, int(ngeo), float(maxtaufrac), prec,
+                                      ctypes.byref(g), _ptr(ws), need, ctypes.c_void_p(s.cuda_stream)))
+    s.synchronize()
+    out = {k: v.numpy() for k, v in res.items() if k != 'flags'}
+    out['flags'] = int(res['flags'][0])
+    return out
+
+
 class PreparedRays:
     """Rays set up once on the device (kgeo_ray_setup), sampled any number of times (kgeo_ray_samples)."""
 

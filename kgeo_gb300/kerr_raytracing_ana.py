@@ -49,7 +49,7 @@ def _pixels(alpha, beta):
 
 
 def _flags_check(a, flags):
-    f = int(flags.item())
+    f = flags if isinstance(flags, int) else int(flags.item())
     if f & _lib.FLAG_MINSPIN_VORTICAL:
         raise Exception("below MINSPIN but there are eta<0 points in th_integrate!")
     if np.abs(a) < MINSPIN and (f & _lib.FLAG_ANY_ETA_NONPOS):
@@ -68,12 +68,21 @@ def raytrace_ana(a=SPIN, observer_coords=[0, ROUT, INC, 0], image_coords=[alpha_
     [alpha, beta] = image_coords
     _check_args(a, r_o, th_o)
     alpha, beta = _pixels(alpha, beta)
-    al = _dev.as_device(alpha)
-    be = _dev.as_device(beta)
-    res = _dev.trace(a, r_o, th_o, al, be, ngeo=ngeo, maxtaufrac=maxtaufrac)
-    _flags_check(a, res['flags'])
     keys = ('mino', 'sig', 't', 'r', 'th', 'ph')
-    vals = [res[k] for k in keys] if device_arrays else _dev.to_host([res[k] for k in keys])
+    if not device_arrays and not (isinstance(alpha, torch.Tensor) and alpha.is_cuda):
+        # host arrays in and out: kgeo_raytrace_host overlaps the copies with the kernels
+        _dev.require_cuda()
+        al = alpha.cpu().numpy() if isinstance(alpha, torch.Tensor) else alpha
+        be = beta.cpu().numpy() if isinstance(beta, torch.Tensor) else beta
+        res = _dev.trace_host(a, r_o, th_o, al, be, ngeo, maxtaufrac=maxtaufrac)
+        _flags_check(a, res['flags'])
+        vals = [res[k] for k in keys]
+    else:
+        al = _dev.as_device(alpha)
+        be = _dev.as_device(beta)
+        res = _dev.trace(a, r_o, th_o, al, be, ngeo=ngeo, maxtaufrac=maxtaufrac)
+        _flags_check(a, res['flags'])
+        vals = [res[k] for k in keys] if device_arrays else _dev.to_host([res[k] for k in keys])
     return Geodesics(a, observer_coords, image_coords, vals[0], vals[1], list(vals[2:]))
 
 
