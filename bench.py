@@ -790,6 +790,115 @@ def run_polimage(args):
 
 
 # ---------------------------------------------------------------------------
+# curve library: generate_library('rh') of the reference (99 spins x 89 inclinations x
+# orders 0..5 x 360 angles, one Brent solve per angle)
+# ---------------------------------------------------------------------------
+
+CPU_LIB_SAMPLE = 600     # (curve, angle) roots of the bounded CPU sample
+
+
+def library_workload(small=False):
+    spins = np.linspace(0.01, 0.99, 99)
+    incs = np.linspace(1, 89, 89)
+    if small:
+        spins, incs = spins[::10], incs[::10]
+    allincs, allspins = np.meshgrid(incs, spins)
+    curves = []
+    for sp, inc in zip(allspins.flatten(), allincs.flatten()):
+        for m in range(6):
+            curves.append((float(sp), float(inc) * np.pi / 180., 1 + np.sqrt(1 - sp * sp), m))
+    return curves, np.linspace(-180, 179, 360) * np.pi / 180.
+
+
+def _cpu_lib_chunk(items):
+    from oracle import kgeo_oracle as ko
+    from scipy.optimize import brentq
+    import warnings
+    warnings.filterwarnings('ignore')
+    n = 0
+    for (a, th0, req, m, vp) in items:
+        lo, hi = ko.rho_bracket(m, req)
+        try:
+            brentq(lambda rho: ko.r_equatorial2(rho, vp, a, th0, mbar=m) - req, lo, hi)
+        except (ValueError, RuntimeError):
+            pass
+        n += 1
+    return n
+
+
+def run_library(args):
+    small = args.case == 'library-small'
+    pool = cores = None
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()
+    import torch
+    from kgeo_gb300.equatorial_lensing import rho_of_req_device
+    curves, vp = library_workload(small)
+    vpd = torch.from_numpy(vp).cuda()
+    nroots = len(curves) * vp.size
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    for _ in range(args.warmup):
+        rho_of_req_device(curves, vpd)
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(args.steps):
+        rho, st = rho_of_req_device(curves, vpd)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    t_step = e0.elapsed_time(e1) / 1e3 / args.steps
+    st = st.cpu().numpy()
+    # end to end: the public make_library call (angles from the host, tables to the host)
+    from kgeo_gb300.equatorial_lensing import make_library
+    sp = np.array(sorted({c[0] for c in curves}))
+    inc = np.array(sorted({round(c[1] * 180 / np.pi, 9) for c in curves}))
+    I, S = np.meshgrid(inc, sp)
+    make_library(S.flatten(), I.flatten(), which='rh', mmax=5)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        tabs = make_library(S.flatten(), I.flatten(), which='rh', mmax=5)
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    cpu = None
+    if pool is not None:
+        rng = np.random.default_rng(0)
+        pick = rng.choice(nroots, size=CPU_LIB_SAMPLE, replace=False)
+        items = [curves[k // vp.size][:4] + (float(vp[k % vp.size]),) for k in pick]
+        chunks = [items[j::cores * 2] for j in range(cores * 2)]
+        t0 = time.time()
+        pool.map(_cpu_lib_chunk, chunks)
+        dt = time.time() - t0
+        cpu = {'value': CPU_LIB_SAMPLE / dt, 'unit': 'roots/s', 'cores': cores, 'kind': 'port',
+               'sample': '%d random (curve, angle) roots of the same library; oracle/kgeo_oracle.py r_equatorial2 '
+                         'under scipy.optimize.brentq (the reference\'s rho_of_req loop) on a %d-process pool, '
+                         '%.1f s wall' % (CPU_LIB_SAMPLE, cores, dt)}
+        pool.close()
+    line = {
+        'metric': 'roots/s: curve library (rho_of_req roots, one per curve and angle)',
+        'value': nroots / t_step, 'unit': 'roots/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': t_step * 1e3, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f64', 'data': 'synthetic: the library grid of generate_library',
+        'config': {'workload': "generate_library('rh'): %d spins x %d inclinations x orders 0..5 x 360 angles, "
+                               'r_eq = r_h, r_o = inf, brentq xtol 2e-12' % (sp.size, inc.size),
+                   'curves': len(curves), 'roots': nroots, 'case': args.case,
+                   'failed_roots': int((st != 0).sum()), 'l2': 'compute-bound; inputs and outputs < 160 MB'},
+        'curves_per_s': len(curves) / t_step,
+        'roofline': {'bound': 'fp64', 'kernel': 'curve_kernel', 'launch_ms': t_step * 1e3, 'achieved': None,
+                     'frac': None, 'traffic': None},
+        'cpu_baseline': cpu,
+        'e2e': {'value': nroots / t_e2e, 'unit': 'roots/s', 'h2d_bytes_per_step': 8 * vp.size + 48 * len(curves),
+                'd2h_bytes_per_step': 12 * nroots, 'ms_per_step': t_e2e * 1e3,
+                'path': 'kgeo_gb300.equatorial_lensing.make_library (tables to the host, no files)'},
+        'gpu_launches': args.steps, 'clocks': ck,
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
 # configuration 4: batched images (64 images, one persistent launch, CUDA graph)
 # ---------------------------------------------------------------------------
 
@@ -951,7 +1060,8 @@ def main():
     p.add_argument('--warmup', type=int, default=3)
     p.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     p.add_argument('--case', choices=('full', 'small', 'mixed', 'mixed-small', 'image', 'image-small', 'batch',
-                                      'batch-small', 'polimage', 'polimage-small'), default='full')
+                                      'batch-small', 'polimage', 'polimage-small', 'library', 'library-small'),
+                   default='full')
     p.add_argument('--no-cpu-baseline', action='store_true')
     args = p.parse_args()
     if args.impl == 'reference':
@@ -962,6 +1072,8 @@ def main():
         run_image(args)
     elif args.case.startswith('polimage'):
         run_polimage(args)
+    elif args.case.startswith('library'):
+        run_library(args)
     elif args.case.startswith('batch'):
         run_batch(args)
     else:

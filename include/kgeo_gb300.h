@@ -38,7 +38,8 @@ typedef enum {
   KGEO_ERR_NULL = 8,        /* a required pointer is NULL */
   KGEO_ERR_CUDA = 9,        /* a CUDA runtime call failed */
   KGEO_ERR_MODEL = 10,      /* unknown / out-of-range emissivity, velocity or B-field model parameter, or image option */
-  KGEO_ERR_NOALLOC_SIZE = 11 /* npix above KGEO_NOALLOC_MAX_PIXELS for kgeo_raytrace_noalloc */
+  KGEO_ERR_NOALLOC_SIZE = 11, /* npix above KGEO_NOALLOC_MAX_PIXELS for kgeo_raytrace_noalloc */
+  KGEO_ERR_SOLVER = 12      /* root-solver arguments: xtol <= 0, rtol < 4 eps, maxiter < 0 (scipy brentq's checks) */
 } kgeo_status;
 
 /* Arithmetic of the sample kernels. FP64: every output within the FP64 parity bars.
@@ -46,8 +47,8 @@ typedef enum {
  * sums into t, phi, sigma in float-float (two FP32 words, ~48 bits), the Pi / E increments as a
  * float-float leading term plus an FP32 correction, theta from an FP32 atan2; FP64 at chunk
  * starts, next to an elliptic-Pi pole and at the final horizon-adjacent sample. Measured against
- * the FP64 oracle: r <= 1e-10, theta <= 1.5e-7, phi <= 4e-8 (floor 1), t and sigma <= 2e-8 of
- * r_o. */
+ * the FP64 oracle on 2048^2 images: r <= 5e-9, theta <= 2e-7, t and sigma <= 1.3e-8 of r_o, phi
+ * within max(1e-6, 1e-12 / rho) where rho is the distance to the nearest elliptic-Pi pole. */
 #define KGEO_PRECISION_FP64 0
 #define KGEO_PRECISION_MIXED 1
 
@@ -263,6 +264,38 @@ size_t kgeo_image_adjoint_workspace_size(int64_t npix);
 int kgeo_image_adjoint(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha,
                        const double* beta, int64_t npix, const kgeo_emission* model, const double* grad_I, double* grad,
                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* Lensed curves of constant equatorial radius: rho_of_req / rho_of_req_single
+ * (kgeo/equatorial_lensing.py:223-258) for many curves at once. Curve c is the image-plane
+ * curve rho(varphi) on which the mbar-th equatorial crossing of the ray at
+ * (alpha, beta) = rho (cos varphi, sin varphi) lies at r_eq, for an observer at r_o = inf
+ * (equatorial_lensing.R0): at every angle, the root of objfunc (r_s of r_equatorial with the
+ * reference's fill-ins INF / 1 where there is no crossing, minus r_eq; :198-221) on
+ * [rho_min, rho_max] by Brent's method with scipy.optimize.brentq's convergence test
+ * (xtol, rtol; its defaults are 2e-12, 4 eps, 100). curves: host array; varphi (nphi), rho and
+ * status (ncurves, nphi) row-major: device arrays. status (may be NULL):
+ * KGEO_CURVE_SIGN where f(rho_min), f(rho_max) have the same sign (rho = NaN; brentq raises),
+ * KGEO_CURVE_MAXITER where maxiter steps did not converge (brentq raises). One launch over all
+ * (curve, angle) pairs: a whole curve library (make_curves2 / generate_library, :327-423) is one
+ * call. */
+#define KGEO_CURVE_OK 0
+#define KGEO_CURVE_SIGN 1
+#define KGEO_CURVE_MAXITER 2
+typedef struct {
+  double a, th_o;           /* spin and inclination (the kgeo_observer rules; r_o = inf) */
+  double r_eq;              /* equatorial radius of the curve */
+  double rho_min, rho_max;  /* bracket (rho_of_req: mbar 0: (0, r_eq + 5); 1: (0, 100); else (1, 10)) */
+  int32_t mbar;             /* image order >= 0 */
+  int32_t reserved;
+} kgeo_curve;
+int kgeo_rho_of_req(const kgeo_curve* curves, int32_t ncurves, const double* varphi, int32_t nphi, double xtol,
+                    double rtol, int32_t maxiter, double* rho, int32_t* status, void* stream);
+
+/* critical_curve(a, th0, n) (kgeo/equatorial_lensing.py:260-289) before its mask: the n
+ * points of r = linspace(r_-, r_+, n) over the prograde / retrograde spherical photon orbit
+ * radii, mapped to the screen (alpha, beta >= 0); a point the reference drops has alpha or beta
+ * NaN. alpha, beta: (n) device arrays. */
+int kgeo_critical_curve(double a, double th_o, int64_t n, double* alpha, double* beta, void* stream);
 
 /* Batched tracing: many images of different size, spin, inclination and ngeo traced as one
  * job (no counterpart in the reference, whose raytrace_ana takes one image per call:

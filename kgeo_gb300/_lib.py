@@ -50,6 +50,12 @@ class ImageOptions(ctypes.Structure):
     _fields_ = [('polarization', c_int32), ('pathlength', c_int32), ('diskangle', c_double), ('bfield', BField)]
 
 
+class Curve(ctypes.Structure):
+    """kgeo_curve."""
+    _fields_ = [('a', c_double), ('th_o', c_double), ('r_eq', c_double), ('rho_min', c_double),
+                ('rho_max', c_double), ('mbar', c_int32), ('reserved', c_int32)]
+
+
 class BatchImage(ctypes.Structure):
     """kgeo_batch_image."""
     _fields_ = [('a', c_double), ('r_o', c_double), ('th_o', c_double), ('npix', c_int64), ('ngeo', c_int32),
@@ -95,6 +101,9 @@ SIGNATURES = {
     'kgeo_image_ex': (c_int, [ctypes.POINTER(Observer), c_int32, c_int32, c_void_p, c_void_p, c_int64,
                               ctypes.POINTER(Emission), ctypes.POINTER(ImageOptions), ctypes.POINTER(ImageOut),
                               c_void_p]),
+    'kgeo_rho_of_req': (c_int, [ctypes.POINTER(Curve), c_int32, c_void_p, c_int32, c_double, c_double, c_int32,
+                                c_void_p, c_void_p, c_void_p]),
+    'kgeo_critical_curve': (c_int, [c_double, c_double, c_int64, c_void_p, c_void_p, c_void_p]),
     'kgeo_image_adjoint_workspace_size': (c_size_t, [c_int64]),
     'kgeo_image_adjoint': (c_int, [ctypes.POINTER(Observer), c_int32, c_int32, c_void_p, c_void_p, c_int64,
                                    ctypes.POINTER(Emission), c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),

@@ -28,6 +28,7 @@ UNITS = [
     ('kg_peak.cu', []),
     ('kg_noalloc.cu', []),
     ('kg_batch.cu', []),
+    ('kg_curves.cu', ['-fmad=false']),
 ]
 
 

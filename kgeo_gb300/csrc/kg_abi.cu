@@ -1,8 +1,10 @@
 // C ABI of the kgeo GB300 tracer (declarations and contracts: include/kgeo_gb300.h).
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "../../include/kgeo_gb300.h"
+
 #include "kg_launch.h"
 
 using namespace kg;
@@ -416,6 +418,68 @@ int kgeo_r_equatorial(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_order
   return launch_equatorial(ea, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
 }
 
+int kgeo_rho_of_req(const kgeo_curve* curves, int32_t ncurves, const double* varphi, int32_t nphi, double xtol,
+                    double rtol, int32_t maxiter, double* rho, int32_t* status, void* stream) {
+  if (ncurves < 0 || nphi < 0) return KGEO_ERR_LENGTHS;
+  if (!(xtol > 0) || !(rtol >= 4 * 2.220446049250313e-16) || maxiter < 0) return KGEO_ERR_SOLVER;
+  if (ncurves == 0 || nphi == 0) return KGEO_OK;
+  if (!curves || !varphi || !rho) return KGEO_ERR_NULL;
+  std::vector<CurveSpec> spec((size_t)ncurves);
+  for (int32_t c = 0; c < ncurves; ++c) {
+    const kgeo_curve& k = curves[c];
+    kgeo_observer o{k.a, INFINITY, k.th_o};
+    int st = check_observer(&o);
+    if (st) return st;
+    if (k.mbar < 0) return KGEO_ERR_MBAR;
+    spec[c].obs = make_observer(&o);
+    spec[c].r_target = k.r_eq;
+    spec[c].rho_min = k.rho_min;
+    spec[c].rho_max = k.rho_max;
+    spec[c].mbar = k.mbar;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  CurveSpec* table = nullptr;
+  const size_t bytes = sizeof(CurveSpec) * spec.size();
+  if (cudaMallocAsync(reinterpret_cast<void**>(&table), bytes, s) != cudaSuccess) return KGEO_ERR_CUDA;
+  // a pageable source: the call returns once the table is staged, so `spec` may go
+  bool ok = cudaMemcpyAsync(table, spec.data(), bytes, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  if (ok) {
+    CurveArgs ca;
+    ca.curves = table;
+    ca.ncurves = ncurves;
+    ca.varphi = varphi;
+    ca.nphi = nphi;
+    ca.xtol = xtol;
+    ca.rtol = rtol;
+    ca.maxiter = maxiter;
+    ca.rho = rho;
+    ca.status = status;
+    ok = launch_curves(ca, s) == cudaSuccess;
+  }
+  ok = (cudaFreeAsync(table, s) == cudaSuccess) && ok;
+  return ok ? KGEO_OK : KGEO_ERR_CUDA;
+}
+
+int kgeo_critical_curve(double a, double th_o, int64_t n, double* alpha, double* beta, void* stream) {
+  kgeo_observer o{a, INFINITY, th_o};
+  int st = check_observer(&o);
+  if (st) return st;
+  if (n < 0) return KGEO_ERR_LENGTHS;
+  if (n == 0) return KGEO_OK;
+  if (!alpha || !beta) return KGEO_ERR_NULL;
+  CriticalArgs ca;
+  ca.a = a;
+  ca.sin_th = std::sin(th_o);
+  ca.cos_th = std::cos(th_o);
+  ca.tan_th = std::tan(th_o);
+  ca.rminus = 2 * (1 + std::cos(2. * std::acos(-a) / 3.));
+  ca.rplus = 2 * (1 + std::cos(2. * std::acos(a) / 3.));
+  ca.n = n;
+  ca.alpha = alpha;
+  ca.beta = beta;
+  return launch_critical(ca, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
+}
+
 int kgeo_image(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha, const double* beta,
                int64_t npix, const kgeo_emission* model, kgeo_image_out* out, void* stream) {
   return kgeo_image_ex(obs, mbar_lo, n_orders, alpha, beta, npix, model, nullptr, out, stream);
@@ -551,6 +615,7 @@ const char* kgeo_status_string(int status) {
     case KGEO_ERR_CUDA: return "CUDA runtime error";
     case KGEO_ERR_MODEL: return "emissivity / velocity / B-field model or image option out of range";
     case KGEO_ERR_NOALLOC_SIZE: return "npix exceeds KGEO_NOALLOC_MAX_PIXELS (kgeo_raytrace_noalloc)";
+    case KGEO_ERR_SOLVER: return "root solver arguments out of range (xtol > 0, rtol >= 4 eps, maxiter >= 0)";
     default: return "unknown status";
   }
 }

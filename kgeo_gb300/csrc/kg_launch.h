@@ -5,6 +5,7 @@
 #include <cstdint>
 
 #include "kg_polar.cuh"
+#include "kg_curves.cuh"
 
 namespace kg {
 
@@ -218,6 +219,27 @@ constexpr int IMAGE_BLOCK = 128;
 KG_HD constexpr int64_t image_adjoint_blocks(int64_t npix) { return (npix + IMAGE_BLOCK - 1) / IMAGE_BLOCK; }
 
 cudaError_t launch_ray_setup(const SetupArgs& a, cudaStream_t s);
+// curve library (kg_curves.cu)
+struct CurveArgs {
+  const CurveSpec* curves;  // (ncurves) device table
+  int64_t ncurves;
+  const double* varphi;     // (nphi) angles shared by every curve
+  int64_t nphi;
+  double xtol, rtol;
+  int maxiter;
+  double* rho;              // (ncurves, nphi)
+  int32_t* status;          // (ncurves, nphi) CURVE_* or NULL
+};
+
+struct CriticalArgs {
+  double a, sin_th, cos_th, tan_th, rminus, rplus;
+  int64_t n;
+  double* alpha;
+  double* beta;
+};
+
+cudaError_t launch_curves(const CurveArgs& a, cudaStream_t s);
+cudaError_t launch_critical(const CriticalArgs& a, cudaStream_t s);
 cudaError_t launch_image(const ImageArgs& a, cudaStream_t s);
 cudaError_t launch_image_adjoint(const ImageAdjointArgs& a, cudaStream_t s);
 cudaError_t launch_equatorial(const EquatorialArgs& a, cudaStream_t s);

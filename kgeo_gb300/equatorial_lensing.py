@@ -7,6 +7,7 @@ kgeo/kerr_raytracing_utils.py:551-684, 794-826. Same signatures, checks and outp
 the work runs in the CUDA kernels behind the C ABI (include/kgeo_gb300.h).
 """
 import ctypes
+import os
 
 import numpy as np
 import torch
@@ -147,25 +148,174 @@ def _imax_counts(a, r_o, th_o, alpha, beta, key):
 
 
 def critical_curve(a, th0, n=100000):
-    """Parametrised critical curve (alpha, beta), 2 x (valid points) long.
+    """Parametrised critical curve (alpha, beta), 2 x (valid points) long
+    (kgeo/equatorial_lensing.py:260-289): the n photon-orbit radii between the retrograde and
+    prograde circular orbits, their conserved quantities and screen coordinates (GL19b Eqs
+    38-40) from kgeo_critical_curve; the points the reference drops (NaN) are dropped and the
+    lower half mirrored."""
+    _dev.require_cuda()
+    lib = _lib.load()
+    al = torch.empty(int(n), dtype=torch.float64, device='cuda')
+    be = torch.empty(int(n), dtype=torch.float64, device='cuda')
+    s = torch.cuda.current_stream()
+    _lib.check(lib.kgeo_critical_curve(float(a), float(th0), int(n), _p(al), _p(be), ctypes.c_void_p(s.cuda_stream)))
+    keep = ~(torch.isnan(al) | torch.isnan(be))
+    al, be = al[keep], be[keep]
+    alpha, beta = _dev.to_host([torch.cat((al, torch.flip(al, (0,)))), torch.cat((be, -torch.flip(be, (0,))))])
+    return alpha, beta
 
-    GL19b eqs. 38-40 as kgeo/equatorial_lensing.py:264-293 evaluates them: photon-orbit radii
-    between the retrograde and prograde circular orbits, their conserved quantities, the
-    screen coordinates, NaN points dropped, the lower half mirrored. Host-side numpy: it is a
-    closed form evaluated once per image, not part of the traced path.
-    """
-    rminus = 2 * (1 + np.cos(2. * np.arccos(-a) / 3.))
-    rplus = 2 * (1 + np.cos(2. * np.arccos(a) / 3.))
-    r = np.linspace(rminus, rplus, n)
-    lam = -(r ** 3 + a ** 2 + r * (a ** 2) - 3 * r ** 2) / (a * r - a)
-    eta = (r ** 2) * (3 * r ** 2 + a ** 2 - lam ** 2) / (r ** 2 - a ** 2)
-    with np.errstate(invalid='ignore'):
-        alpha = -lam / np.sin(th0)
-        beta = np.sqrt(eta + (a * np.cos(th0)) ** 2 - (lam / np.tan(th0)) ** 2)
-    bad = np.isnan(alpha) + np.isnan(beta)
-    alpha = alpha[~bad]
-    beta = beta[~bad]
-    return np.hstack((alpha, np.flip(alpha))), np.hstack((beta, -np.flip(beta)))
+
+# ---------------------------------------------------------------------------
+# lensed curves of constant equatorial radius (kgeo/equatorial_lensing.py:198-423)
+# ---------------------------------------------------------------------------
+
+INF = 1.e50
+R0 = np.inf
+BRENTQ_XTOL = 2e-12
+BRENTQ_RTOL = 4 * np.finfo(float).eps
+BRENTQ_MAXITER = 100
+
+
+def rho_bracket(mbar, req):
+    """rho_of_req's bracket, "eyeballed from Gralla+Lupsasca Fig 6" (kgeo/equatorial_lensing.py:227-236)."""
+    if mbar == 0:
+        return 0, req + 5
+    if mbar == 1:
+        return 0, 100
+    return 1, 10
+
+
+def rho_of_req_device(curves, varphis, xtol=BRENTQ_XTOL, rtol=BRENTQ_RTOL, maxiter=BRENTQ_MAXITER, stream=None):
+    """kgeo_rho_of_req for many curves at once. curves: iterable of (a, th0, r_eq, mbar) or
+    (a, th0, r_eq, mbar, rho_min, rho_max); varphis: angles (numpy or CUDA tensor). Returns
+    (rho, status) CUDA tensors (ncurves, nphi)."""
+    _dev.require_cuda()
+    lib = _lib.load()
+    curves = list(curves)
+    arr = (_lib.Curve * max(1, len(curves)))()
+    for i, c in enumerate(curves):
+        a, th0, req, mbar = c[:4]
+        lo, hi = (c[4], c[5]) if len(c) > 4 else rho_bracket(mbar, req)
+        arr[i] = _lib.Curve(float(a), float(th0), float(req), float(lo), float(hi), int(mbar), 0)
+    vp = _dev.as_device(varphis)
+    nphi = vp.numel()
+    rho = torch.empty((len(curves), nphi), dtype=torch.float64, device=vp.device)
+    st = torch.zeros((len(curves), nphi), dtype=torch.int32, device=vp.device)
+    s = stream if stream is not None else torch.cuda.current_stream(vp.device)
+    _lib.check(lib.kgeo_rho_of_req(arr, len(curves), _p(vp), nphi, float(xtol), float(rtol), int(maxiter), _p(rho),
+                                   _p(st), ctypes.c_void_p(s.cuda_stream)))
+    return rho, st
+
+
+def _raise_status(st):
+    if (st == 1).any():
+        raise ValueError("f(a) and f(b) must have different signs")
+    if (st == 2).any():
+        raise RuntimeError("Failed to converge after %d iterations" % BRENTQ_MAXITER)
+
+
+def rho_of_req(a, th0, req, mbar=0, varphis=None):
+    """(varphis, rhos, alphas, betas) of the curve of equatorial radius req for image order
+    mbar (kgeo/equatorial_lensing.py:223-243): at every angle the root of objfunc on the
+    reference's bracket, all angles in one kernel launch."""
+    if varphis is None:
+        varphis = np.linspace(-180, 179, 360) * np.pi / 180.
+    varphis = np.asarray(varphis, dtype=float)
+    rho, st = rho_of_req_device([(a, th0, req, mbar)], varphis)
+    rho, st = _dev.to_host([rho[0], st[0]])
+    _raise_status(st)
+    return varphis, rho, np.cos(varphis) * rho, np.sin(varphis) * rho
+
+
+def rho_of_req_single(a, th0, req, varphi, mbar=0):
+    """rho at one angle (kgeo/equatorial_lensing.py:245-258)."""
+    return float(rho_of_req(a, th0, req, mbar=mbar, varphis=np.array([varphi]))[1][0])
+
+
+def r_equatorial2(rho, varphi, a, th0, mbar=0):
+    """r_s at (rho, varphi) for r_o = inf, INF / 1 where there is no crossing outside / inside
+    the critical curve (kgeo/equatorial_lensing.py:198-216)."""
+    alpha = np.array([np.cos(varphi) * rho])
+    beta = np.array([np.sin(varphi) * rho])
+    r = r_equatorial(a, R0, th0, mbar, alpha, beta)[0][0]
+    outside = is_outside_crit(a, th0, alpha, beta)[0]
+    if r <= 0 and outside == 1:
+        r = INF
+    elif r <= 0:
+        r = 1
+    return r
+
+
+def objfunc(rho, varphi, a, th0, r_target, mbar=0):
+    """r_equatorial2 - r_target (kgeo/equatorial_lensing.py:218-221)."""
+    return r_equatorial2(rho, varphi, a, th0, mbar=mbar) - r_target
+
+
+LIBRARY_RADII = {'r10': 10., 'r100': 100., 'r1000': 1000., 'r10000': 10000.}
+
+
+def _library_file(outpath, spin, inc, which):
+    return '%s/a%02.0f_i%02.0f_%s.txt' % (outpath, 100 * spin, inc, which)
+
+
+def make_library(spins, incs, which='rh', mmax=5, outpath=None, varphis=None):
+    """The curve library of generate_library / make_curves2 (kgeo/equatorial_lensing.py:
+    327-423) for every (spin, inclination) pair: rho(varphi) of the curves of equatorial radius
+    r_h (which='rh') or 10, 100, 1000, 10000 for orders 0..mmax, all (spin, inc, order, angle)
+    roots in one kernel launch. Returns {(spin, inc): (nphi, mmax + 2) array of varphi and the
+    rho columns}, leaving out a pair whose solve fails at any angle (the reference skips its
+    file). With outpath, writes each pair's table as make_curves2 does (np.savetxt,
+    'a%02.0f_i%02.0f_<which>.txt'), skipping files that exist."""
+    if which != 'rh' and which not in LIBRARY_RADII:
+        raise Exception()
+    if varphis is None:
+        varphis = np.linspace(-180, 179, 360) * np.pi / 180.
+    varphis = np.asarray(varphis, dtype=float)
+    pairs = [(float(sp), float(inc)) for sp, inc in zip(np.ravel(spins), np.ravel(incs))]
+    if outpath is not None:
+        pairs = [p for p in pairs if not os.path.isfile(_library_file(outpath, p[0], p[1], which))]
+    curves = []
+    for sp, inc in pairs:
+        req = 1 + np.sqrt(1 - sp ** 2) if which == 'rh' else LIBRARY_RADII[which]
+        for m in range(mmax + 1):
+            curves.append((sp, inc * np.pi / 180., req, m))
+    out = {}
+    if not curves:
+        return out
+    rho, st = rho_of_req_device(curves, varphis)
+    rho, st = _dev.to_host([rho, st])
+    rho = rho.reshape(len(pairs), mmax + 1, -1)
+    ok = (st.reshape(len(pairs), mmax + 1, -1) == 0).all(axis=(1, 2))
+    for k, (sp, inc) in enumerate(pairs):
+        if not ok[k]:
+            continue
+        tab = np.hstack((varphis.reshape(-1, 1), rho[k].T))
+        out[(sp, inc)] = tab
+        if outpath is not None:
+            np.savetxt(_library_file(outpath, sp, inc, which), tab)
+    return out
+
+
+def make_curves2(i, which, n, spin, inc, mmax, outpath):
+    """One library file (kgeo/equatorial_lensing.py:362-418); the progress counter of the
+    reference's process pool is not kept."""
+    make_library([spin], [inc], which=which, mmax=mmax, outpath=outpath)
+
+
+def generate_library(which='rh', outpath=None, spins=None, incs=None, mmax=5):
+    """generate_library (kgeo/equatorial_lensing.py:327-357): spins 0.01..0.99 (99) x
+    inclinations 1..89 deg (89) x orders 0..mmax, 360 angles each, written to
+    './curve_library_<which>' (created if missing), in one kernel launch instead of a
+    process pool."""
+    if outpath is None:
+        outpath = './curve_library_' + which
+    if spins is None:
+        spins = np.linspace(0.01, 0.99, 99)
+    if incs is None:
+        incs = np.linspace(1, 89, 89)
+    allincs, allspins = np.meshgrid(incs, spins)
+    os.makedirs(outpath, exist_ok=True)
+    return make_library(allspins.flatten(), allincs.flatten(), which=which, mmax=mmax, outpath=outpath)
 
 
 def critical_band(a, th0, n_angles=4096, n_radii=256, half_width=0.05, n_curve=100000):

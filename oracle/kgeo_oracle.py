@@ -1315,6 +1315,65 @@ def image_grid(alpha_min, alpha_max, beta_min, beta_max, psize):
 
 
 # ----------------------------------------------------------------------------
+# lensed curves of constant equatorial radius and the critical curve
+# ----------------------------------------------------------------------------
+
+CURVE_INF = 1.e50   # kgeo/equatorial_lensing.py:17
+
+
+def r_equatorial2(rho, varphi, a, th0, mbar=0):
+    """r_s at image-plane polar point (rho, varphi) for r_o = inf, with INF outside / 1 inside
+    the critical curve where there is no crossing; kgeo/equatorial_lensing.py:198-216."""
+    alpha = np.array([np.cos(varphi) * rho])
+    beta = np.array([np.sin(varphi) * rho])
+    r = r_equatorial(a, np.inf, th0, mbar, alpha, beta)[0][0]
+    out = outside_critical(a, th0, alpha, beta)[0]
+    if r <= 0 and out == 1:
+        r = CURVE_INF
+    elif r <= 0:
+        r = 1
+    return r
+
+
+def rho_bracket(mbar, req):
+    """rho_of_req's bracket, kgeo/equatorial_lensing.py:227-236."""
+    if mbar == 0:
+        return 0, req + 5
+    if mbar == 1:
+        return 0, 100
+    return 1, 10
+
+
+def rho_of_req(a, th0, req, mbar=0, varphis=None):
+    """(varphis, rhos, alphas, betas) by scipy.optimize.brentq per angle on objfunc;
+    kgeo/equatorial_lensing.py:218-243."""
+    from scipy.optimize import brentq
+    if varphis is None:
+        varphis = np.linspace(-180, 179, 360) * np.pi / 180.
+    lo, hi = rho_bracket(mbar, req)
+    rhos = np.array([brentq(lambda rho: r_equatorial2(rho, vp, a, th0, mbar=mbar) - req, lo, hi)
+                     for vp in varphis])
+    return varphis, rhos, np.cos(varphis) * rhos, np.sin(varphis) * rhos
+
+
+def critical_curve(a, th0, n=100000):
+    """Critical curve (alpha, beta) with the reference's NaN mask and mirror;
+    kgeo/equatorial_lensing.py:260-289."""
+    rminus = 2 * (1 + np.cos(2. * np.arccos(-a) / 3.))
+    rplus = 2 * (1 + np.cos(2. * np.arccos(a) / 3.))
+    r = np.linspace(rminus, rplus, n)
+    lam = -(r ** 3 + a ** 2 + r * (a ** 2) - 3 * r ** 2) / (a * r - a)
+    eta = (r ** 2) * (3 * r ** 2 + a ** 2 - lam ** 2) / (r ** 2 - a ** 2)
+    alpha = -lam / np.sin(th0)
+    with np.errstate(invalid='ignore'):
+        beta = np.sqrt(eta + (a * np.cos(th0)) ** 2 - (lam / np.tan(th0)) ** 2)
+    mask = np.isnan(alpha) + np.isnan(beta)
+    alpha = alpha[~mask]
+    beta = beta[~mask]
+    return np.hstack((alpha, np.flip(alpha))), np.hstack((beta, -np.flip(beta)))
+
+
+# ----------------------------------------------------------------------------
 # conditioning helper for the parity tests
 # ----------------------------------------------------------------------------
 

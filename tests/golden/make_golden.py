@@ -302,6 +302,35 @@ def main(path):
     bout['nmodel'] = len(models)
     save('bfield_lab', bout)
 
+    # lensed curves of constant equatorial radius (rho_of_req at 36 angles), incl. brackets
+    # with no sign change (brentq raises), and the critical curve
+    vp = np.linspace(-180, 179, 36) * np.pi / 180.
+    ccases = [(0.5, 60., 'rh', 0), (0.94, 17., 5.0, 1), (0.3, 80., 'rh', 2), (0.7, 30., 10.0, 0),
+              (0.99, 85., 'rh', 5), (0.01, 45., 1000., 1), (0.6, 130., 'rh', 1), (0.5, 60., 100., 2),
+              (0.8, 40., 'rh', 100), (0.5, 60., 0.5, 0)]
+    cout = dict(varphi=vp, ncase=len(ccases))
+    for i, (a, inc, req, m) in enumerate(ccases):
+        r_eq = 1 + np.sqrt(1 - a * a) if req == 'rh' else float(req)
+        cout['case%d' % i] = np.array([a, inc, r_eq, m])
+        try:
+            with warnings.catch_warnings():
+                warnings.simplefilter('ignore')
+                res = quiet(ref.lensing.rho_of_req, a, inc * deg, r_eq, mbar=m, varphis=vp)
+            cout['rho%d' % i] = res[1]
+        except ValueError as e:
+            cout['error%d' % i] = str(e)
+    for i, (a, th0, n) in enumerate([(0.5, 1.0, 3000), (0.94, 0.3, 3000), (0.2, 2.5, 2000), (0.999, 1.5, 5000)]):
+        al, be = ref.lensing.critical_curve(a, th0, n=n)
+        cout['crit%d' % i] = np.array([a, th0, n])
+        cout['crit_alpha%d' % i] = al
+        cout['crit_beta%d' % i] = be
+    # one file of the curve library (make_curves2: 360 angles, orders 0..2, r_eq = 10)
+    lib_dir = tempfile.mkdtemp(prefix='kgeo_lib_')
+    quiet(ref.lensing.make_curves2, 0, 'r10', 1, 0.5, 30., 2, lib_dir)
+    fn = os.path.join(lib_dir, 'a%02.0f_i%02.0f_%s.txt' % (100 * 0.5, 30., 'r10'))
+    cout['library_a50_i30_r10'] = np.loadtxt(fn)
+    save('curves', cout)
+
     # EVPA of ipole images (the reference's tests/data/*.csv, from tests/test_images.py):
     # pixel location and EVPA along the middle row / column for image orders 0 and 1
     ip = {}

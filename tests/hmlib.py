@@ -126,6 +126,18 @@ def bfield(a, r, fieldtype, kw):
     return out.T
 
 
+def curve_rho(a, th0, r_eq, mbar, varphi, bracket, xtol=2e-12, rtol=4 * np.finfo(float).eps, maxiter=100):
+    """The curve kernel's Brent solve (host build) at each angle: (rho, status)."""
+    L = load()
+    ob = observer(a, np.inf, th0)
+    varphi = np.ascontiguousarray(varphi, float)
+    rho = np.zeros(len(varphi))
+    st = np.zeros(len(varphi), np.int32)
+    L.hm_curve_rho(dp(ob), D(r_eq), ctypes.c_int(mbar), D(bracket[0]), D(bracket[1]), dp(varphi),
+                   ctypes.c_long(len(varphi)), D(xtol), D(rtol), ctypes.c_int(maxiter), dp(rho), ip(st))
+    return rho, st
+
+
 def lambert_w0(z):
     L = load()
     L.hm_lambert_w0.restype = D

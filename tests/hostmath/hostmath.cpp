@@ -3,6 +3,7 @@
 #include "../../kgeo_gb300/csrc/kg_equatorial.cuh"
 #include "../../kgeo_gb300/csrc/kg_image.cuh"
 #include "../../kgeo_gb300/csrc/kg_polar.cuh"
+#include "../../kgeo_gb300/csrc/kg_curves.cuh"
 #include "../../kgeo_gb300/csrc/kg_mixed2.cuh"
 
 using namespace kg;
@@ -207,6 +208,17 @@ void hm_bfield(int field, int flag, const double* c, double a, const double* r, 
     BLab B = bfield_lab(F, a, r[i], rp);
     out[3 * i] = B.b1; out[3 * i + 1] = B.b2; out[3 * i + 2] = B.b3;
   }
+}
+// rho of curve (observer ob with r_o = inf) at each varphi; status per angle
+void hm_curve_rho(const double* ob, double r_eq, int mbar, double rho_min, double rho_max, const double* varphi,
+                  long n, double xtol, double rtol, int maxiter, double* rho, int* status) {
+  CurveSpec c;
+  c.obs = make_obs(ob);
+  c.r_target = r_eq;
+  c.mbar = mbar;
+  c.rho_min = rho_min;
+  c.rho_max = rho_max;
+  for (long i = 0; i < n; ++i) rho[i] = curve_rho(c, varphi[i], xtol, rtol, maxiter, status + i);
 }
 double hm_lambert_w0(double z) { return lambert_w0(z); }
 double hm_re_li2(double x) { return re_li2(x); }
