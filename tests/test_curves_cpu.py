@@ -3,10 +3,13 @@ against the reference's fixtures (bit-equal), and the curve kernel's Brent solve
 headers built for the host) against the same fixtures.
 
 Bar for the roots: |rho - rho_ref| <= 1e-8 rho, and rho a root of the oracle's objective to
-1e-9 (the objective changes sign across rho (1 -+ 1e-9)). The curves of r_eq = r_h are the
-edges of the m-th image where the crossing count Nmax steps: the objective jumps there and the
-jump's position rests on a floor() of a ratio that varies slowly with rho, so two exact
-implementations may place it up to ~1e-9 apart; elsewhere the roots agree to ~1e-11."""
+1e-8 (the objective takes both signs on [rho (1 - 1e-8), rho (1 + 1e-8)]). The curves of
+r_eq = r_h are the edges of the m-th image where the crossing count Nmax steps: there the
+objective jumps between r_s - r_h ~ +1e-8 and 1 - r_h, and inside a band of a few 1e-9 in
+rho the floor() that decides Nmax flips back and forth with the rounding of its argument
+(measured for a = 0.6, 130 deg, m = 1), so every point of the band is a root of the
+reference's own objective and the reference's brentq returns one of them; elsewhere the roots
+agree to ~1e-11."""
 import warnings
 
 import numpy as np
@@ -23,14 +26,18 @@ def curve_cases(g):
         yield i, float(a), float(inc) * DEG, float(req), int(m)
 
 
-def is_root(a, th0, req, m, varphi, rho, rel=1e-9):
-    """The oracle's objective changes sign (or vanishes) across rho (1 -+ rel)."""
+def is_root(a, th0, req, m, varphi, rho, rel=1e-8, n=21):
+    """The oracle's objective takes both signs (or vanishes) on [rho (1 - rel), rho (1 + rel)]:
+    the two ends first, then n points across (the Nmax band of the r_h curves)."""
     d = rel * max(abs(rho), 1.0)
     with warnings.catch_warnings():
         warnings.simplefilter('ignore')
-        f0 = ko.r_equatorial2(rho - d, varphi, a, th0, mbar=m) - req
-        f1 = ko.r_equatorial2(rho + d, varphi, a, th0, mbar=m) - req
-    return f0 * f1 <= 0
+        f = lambda x: ko.r_equatorial2(x, varphi, a, th0, mbar=m) - req  # noqa: E731
+        f0, f1 = f(rho - d), f(rho + d)
+        if f0 * f1 <= 0:
+            return True
+        vals = [f(x) for x in np.linspace(rho - d, rho + d, n)]
+    return min(vals) <= 0 <= max(vals)
 
 
 def check_roots(rho, g, i, a, th0, req, m, vp):
