@@ -167,6 +167,13 @@ int kgeo_equatorial_crossings(const kgeo_observer* obs, const double* alpha, con
                               const double* tau, int32_t ntau, double* n_eq, double* n_pol,
                               double* outside_crit, void* stream);
 
+/* n_angular_turnings (kgeo/kerr_raytracing_utils.py:686-792): the fractional number of
+ * angular turning points passed by Mino time tau (ntau, npix), n_turn (ntau, npix), including
+ * the reference's provisional rule for vortical rays. Its check: 0 <= th_o <= pi/2
+ * (KGEO_ERR_TH_O otherwise; r_o is not used). */
+int kgeo_angular_turnings(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                          const double* tau, int32_t ntau, double* n_turn, void* stream);
+
 /* Emission model of an unpolarised equatorial image: Emissivity(emistype, **kwargs)
  * (kgeo/emissivities.py:38-72) and Velocity(veltype, **kwargs) (kgeo/velocities.py:23-67)
  * restricted to the models below, plus Iobs' specind and sin(theta_B)

@@ -101,6 +101,8 @@ SIGNATURES = {
     'kgeo_image_ex': (c_int, [ctypes.POINTER(Observer), c_int32, c_int32, c_void_p, c_void_p, c_int64,
                               ctypes.POINTER(Emission), ctypes.POINTER(ImageOptions), ctypes.POINTER(ImageOut),
                               c_void_p]),
+    'kgeo_angular_turnings': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_void_p, c_int32,
+                                      c_void_p, c_void_p]),
     'kgeo_rho_of_req': (c_int, [ctypes.POINTER(Curve), c_int32, c_void_p, c_int32, c_double, c_double, c_int32,
                                 c_void_p, c_void_p, c_void_p]),
     'kgeo_critical_curve': (c_int, [c_double, c_double, c_int64, c_void_p, c_void_p, c_void_p]),

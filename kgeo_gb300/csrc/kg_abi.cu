@@ -569,6 +569,29 @@ int kgeo_equatorial_crossings(const kgeo_observer* obs, const double* alpha, con
   ca.n_eq = n_eq;
   ca.n_pol = n_pol;
   ca.outside = outside_crit;
+  ca.n_turn = nullptr;
+  return launch_crossings(ca, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
+}
+
+int kgeo_angular_turnings(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                          const double* tau, int32_t ntau, double* n_turn, void* stream) {
+  if (!obs) return KGEO_ERR_NULL;
+  if (!(std::fabs(obs->a) >= 0 && std::fabs(obs->a) < 1)) return KGEO_ERR_SPIN;
+  if (!(obs->th_o >= 0 && obs->th_o <= 0.5 * PI)) return KGEO_ERR_TH_O;
+  if (npix < 0) return KGEO_ERR_LENGTHS;
+  if (ntau < 0) return KGEO_ERR_NGEO;
+  if (npix > 0 && ntau > 0 && (!alpha || !beta || !tau || !n_turn)) return KGEO_ERR_NULL;
+  CrossingArgs ca;
+  ca.obs = make_observer(obs);
+  ca.alpha = alpha;
+  ca.beta = beta;
+  ca.npix = npix;
+  ca.tau = tau;
+  ca.ntau = ntau;
+  ca.n_eq = nullptr;
+  ca.n_pol = nullptr;
+  ca.outside = nullptr;
+  ca.n_turn = n_turn;
   return launch_crossings(ca, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
 }
 

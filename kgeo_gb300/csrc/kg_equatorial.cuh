@@ -115,6 +115,45 @@ KG_HD double n_pol_at(const EqConsts& c, double Kc, double tau) {
   return (sqrt(-c.a2um) * tau) / (4 * Kc);
 }
 
+// Constants of n_angular_turnings (kgeo/kerr_raytracing_utils.py:686-792): ordinary rays
+// (eta > 0) as the crossing counts; vortical rays (eta <= 0) through the vortical amplitude
+// Nu = asin(sqrt((cos^2 th_o - u_-) / (u_+ - u_-))) and parameter 1 - u_+/u_- (GL19b Eqs 56,
+// 60), as the reference evaluates them.
+struct TurnConsts {
+  bool vort;
+  double sq, F0, K;
+};
+
+KG_HD TurnConsts turn_consts(const Observer& o, double lam, double eta) {
+  TurnConsts c;
+  c.vort = eta <= 0;
+  Turning U = u_turning(o, lam, eta);
+  double ratio, a2um;
+  u_ratio(o, lam, eta, U, &ratio, &a2um);
+  if (!c.vort) {
+    c.F0 = ellip_f(asin(o.cos_th / sqrt(U.up)), ratio);
+    c.K = ellip_f(0.5 * PI, ratio);
+    c.sq = sqrt(-a2um);
+  } else {
+    const double nu = asin(sqrt((o.cos2 - U.um) / (U.up - U.um)));
+    c.F0 = ellip_f(nu, 1 - ratio);
+    c.K = ellip_f(0.5 * PI, 1 - ratio);
+    c.sq = sqrt(a2um);
+  }
+  return c;
+}
+
+// Fractional number of angular turnings at Mino time tau (kgeo/kerr_raytracing_utils.py:
+// 742-787, including its vortical rule: beta <= 0 counts above 1/2 gain another 1/2).
+KG_HD double n_turn_at(const TurnConsts& c, double beta, double tau) {
+  if (beta <= 0) {
+    double n = (tau * c.sq - c.F0) / (2 * c.K) + 0.5;
+    if (c.vort && n > 0.5) n += 0.5;
+    return n;
+  }
+  return (tau * c.sq + c.F0) / (2 * c.K) + 0.5;
+}
+
 // is_outside_crit (kgeo/kerr_raytracing_utils.py:816-826): real r4 > r_h and eta >= 0.
 KG_HD double outside_crit(const Observer& o, double lam, double eta) {
   Roots R = radial_roots(o, lam, eta);

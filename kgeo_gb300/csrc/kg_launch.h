@@ -112,6 +112,7 @@ struct CrossingArgs {
   double* n_eq;       // (ntau, npix)
   double* n_pol;      // (ntau, npix)
   double* outside;    // (npix) is_outside_crit
+  double* n_turn;     // (ntau, npix) n_angular_turnings
 };
 
 // Default and largest samples per thread of the stepped kernel (longer recurrence chains

@@ -88,6 +88,10 @@ __global__ void __launch_bounds__(128) crossings_kernel(CrossingArgs a) {
   double lam = -alpha * o.sin_th;
   double eta = (alpha * alpha - o.a2) * o.cos2 + beta * beta;
   if (a.outside) a.outside[i] = outside_crit(o, lam, eta);
+  if (a.ntau > 0 && a.n_turn) {
+    const TurnConsts tc = turn_consts(o, lam, eta);
+    for (int64_t g = 0; g < a.ntau; ++g) a.n_turn[g * a.npix + i] = n_turn_at(tc, beta, a.tau[g * a.npix + i]);
+  }
   if (a.ntau <= 0 || (!a.n_eq && !a.n_pol)) return;
   EqConsts c = eq_consts(o, lam, eta);
   double Kc = c.vort ? 0.0 : ellip_k(c.ratio);

@@ -114,6 +114,63 @@ def n_poloidal_orbits(a, th_o, alpha, beta, tau):
     return _crossings(a, th_o, alpha, beta, tau, ('n_pol',))['n_pol']
 
 
+def n_angular_turnings(a, th_o, alpha, beta, tau):
+    """Fractional number of angular turnings at Mino times tau (ntau, npix) or (npix)
+    (kgeo/kerr_raytracing_utils.py:686-792), through kgeo_angular_turnings."""
+    _check(a)
+    if not (isinstance(th_o, float) and (0 <= th_o <= np.pi / 2.)):
+        raise Exception("th_o should be a float in range (0,pi/2]")
+    if not isinstance(alpha, np.ndarray):
+        alpha = np.array([alpha]).flatten()
+    if not isinstance(beta, np.ndarray):
+        beta = np.array([beta]).flatten()
+    if len(alpha) != len(beta):
+        raise Exception("alpha, beta are different lengths!")
+    tau = np.asarray(tau, dtype=float) if not isinstance(tau, torch.Tensor) else tau
+    one = len(tau.shape) == 1
+    if one:
+        tau = tau.reshape(1, tau.shape[0])
+    if not (tau.shape[1] == len(alpha)):
+        raise Exception("tau has incompatible shape in n_poloidal_orbits!")
+    _dev.require_cuda()
+    lib = _lib.load()
+    al, be, tt = _dev.as_device(alpha), _dev.as_device(beta), _dev.as_device(tau)
+    out = torch.empty(tuple(tt.shape), dtype=torch.float64, device=al.device)
+    ob = _lib.Observer(float(a), 1.e4, float(th_o))
+    s = torch.cuda.current_stream(al.device)
+    _lib.check(lib.kgeo_angular_turnings(ctypes.byref(ob), _p(al), _p(be), al.numel(), _p(tt), tt.shape[0], _p(out),
+                                         ctypes.c_void_p(s.cuda_stream)))
+    res = out.cpu().numpy()
+    return res[0] if one else res
+
+
+def equatorial_consistency(a, r_o, th_o, alpha, beta, mbar_max=1, raise_on_failure=True):
+    """The consistency check of the reference's scripts/calc_t_equatorial.py:50-71 on the GPU:
+    for each order m <= mbar_max, the coordinates of the geodesics at the crossing Mino times
+    Ir of r_equatorial must lie on the equator (|1 - theta / (pi/2)| <= 1e-14) at the source
+    radius (|1 - r / r_s| <= 1e-12) on every pixel with Nmax >= m. Returns
+    {m: (max theta deviation, max r deviation)}; raises as the script does when a bound fails."""
+    _check(a, r_o, th_o)
+    alpha, beta = _pixels(alpha, beta)
+    al, be = _dev.as_device(alpha), _dev.as_device(beta)
+    out = {}
+    r_s, Ir, Imax, Nmax = r_equatorial_device(a, r_o, th_o, list(range(mbar_max + 1)), al, be)
+    rays = _dev.PreparedRays(a, r_o, th_o, al, be)
+    for m in range(mbar_max + 1):
+        ring = Nmax >= m
+        res = rays.samples(rays.alloc(nsamp=1, keys=('r', 'th')), tau=Ir[m:m + 1].contiguous(), do_phi_and_t=True)
+        th = res['th'][0][ring]
+        r = res['r'][0][ring]
+        dth = float(torch.max(torch.abs(1 - th / (0.5 * np.pi)))) if th.numel() else 0.0
+        dr = float(torch.max(torch.abs(1 - r / r_s[m][ring]))) if r.numel() else 0.0
+        out[m] = (dth, dr)
+        if raise_on_failure and dth > 1.e-14:
+            raise Exception("raytrace_ana not finding eqauatorial crossings for mbar=%i!" % m)
+        if raise_on_failure and dr > 1.e-12:
+            raise Exception("raytrace_ana not finding consistent r_s for mbar=%i!" % m)
+    return out
+
+
 def is_outside_crit(a, th_o, alpha, beta):
     """kgeo/kerr_raytracing_utils.py:794-826."""
     _check(a)

@@ -723,6 +723,48 @@ def n_poloidal_orbits(a, th_o, alpha, beta, tau):
     return out[0] if one else out
 
 
+def n_angular_turnings(a, th_o, alpha, beta, tau):
+    """Fractional number of angular turnings; kgeo/kerr_raytracing_utils.py:686-792 (ordinary
+    rays as the crossing counts, vortical rays by GL19b Eqs 56, 60 with the reference's
+    provisional +1/2 for beta <= 0 counts above 1/2)."""
+    one = tau.ndim == 1
+    if one:
+        tau = tau.reshape(1, tau.shape[0])
+    lam = -alpha * np.sin(th_o)
+    eta = (alpha ** 2 - a ** 2) * np.cos(th_o) ** 2 + beta ** 2
+    out = np.empty(tau.shape)
+    vort = eta <= 0
+    out[:, vort] = 0
+    if np.any(~vort):
+        up, um, ratio, a2um = u_roots(a, th_o, lam[~vort], eta[~vort])
+        F0 = sp.ellipkinc(np.arcsin(np.cos(th_o) / np.sqrt(up)), ratio)
+        K = sp.ellipkinc(0.5 * np.pi, ratio)
+        b = beta[~vort]
+        tr = tau[:, ~vort]
+        res = np.empty(tr.shape)
+        lo = b <= 0
+        res[:, lo] = ((tr * np.sqrt(-a2um) - F0) / (2 * K))[:, lo] + 0.5
+        res[:, ~lo] = ((tr * np.sqrt(-a2um) + F0) / (2 * K))[:, ~lo] + 0.5
+        out[:, ~vort] = res
+    if np.any(vort):
+        up, um, ratio, a2um = u_roots(a, th_o, lam[vort], eta[vort])
+        Nu = np.arcsin(np.sqrt((np.cos(th_o) ** 2 - um) / (up - um)))
+        F0 = sp.ellipkinc(Nu, 1 - ratio)
+        K = sp.ellipkinc(0.5 * np.pi, 1 - ratio)
+        b = beta[vort]
+        tv = tau[:, vort]
+        res = np.empty(tv.shape)
+        lo = b <= 0
+        if np.any(lo):
+            norbit = ((tv * np.sqrt(a2um) - F0) / (2 * K))[:, lo] + 0.5
+            norbit[norbit > 0.5] += 0.5
+            res[:, lo] = norbit
+        if np.any(~lo):
+            res[:, ~lo] = ((tv * np.sqrt(a2um) + F0) / (2 * K))[:, ~lo] + 0.5
+        out[:, vort] = res
+    return out[0] if one else out
+
+
 def outside_critical(a, th_o, alpha, beta):
     """1 where real r4 > r_h and eta >= 0, else 0; kgeo/kerr_raytracing_utils.py:794-826."""
     rh = 1 + np.sqrt(1 - a ** 2)

@@ -331,6 +331,22 @@ def main(path):
     cout['library_a50_i30_r10'] = np.loadtxt(fn)
     save('curves', cout)
 
+    # n_angular_turnings (th_o <= pi/2 only, its check): ordinary and vortical rays, both
+    # signs of beta, a MINSPIN spin, a 2-d tau and a 1-d tau
+    tout = {}
+    rng = np.random.default_rng(5)
+    for i, (a, th) in enumerate([(0.94, 17.), (0.5, 80.), (0.99, 45.), (5e-5, 30.), (0.7, 90.)]):
+        A = np.concatenate([rng.uniform(-8, 8, 300), rng.uniform(-0.3, 0.3, 100)])
+        B = np.concatenate([rng.uniform(-8, 8, 300), rng.uniform(-0.3, 0.3, 100)])
+        tau = np.abs(rng.uniform(0, 3, (5, A.size)))
+        with warnings.catch_warnings():
+            warnings.simplefilter('ignore')
+            nt = ref.utils.n_angular_turnings(a, th * deg, A, B, tau)
+            nt1 = ref.utils.n_angular_turnings(a, th * deg, A, B, tau[2])
+        tout.update({'par%d' % i: np.array([a, th]), 'alpha%d' % i: A, 'beta%d' % i: B, 'tau%d' % i: tau,
+                     'n%d' % i: nt, 'n1_%d' % i: nt1})
+    save('angular_turnings', tout)
+
     # EVPA of ipole images (the reference's tests/data/*.csv, from tests/test_images.py):
     # pixel location and EVPA along the middle row / column for image orders 0 and 1
     ip = {}

@@ -128,3 +128,16 @@ def test_midplane_known_answers(golden):
             x, y, z = x[::-1], y[::-1], z[::-1]
         assert np.isclose(np.interp(0, z, x), g['x0'][i], rtol=1e-12, atol=1e-12)
         assert np.isclose(np.interp(0, z, y), g['y0'][i], rtol=1e-12, atol=1e-12)
+
+
+def test_oracle_n_angular_turnings(golden):
+    """n_angular_turnings (kgeo/kerr_raytracing_utils.py:686-792) against the reference:
+    ordinary and vortical rays, both signs of beta, a spin below MINSPIN, 1-d and 2-d tau."""
+    g = golden('angular_turnings')
+    for i in range(5):
+        a, th = g['par%d' % i]
+        A, B, tau = g['alpha%d' % i], g['beta%d' % i], g['tau%d' % i]
+        n = ko.n_angular_turnings(float(a), float(th) * np.pi / 180, A, B, tau)
+        n1 = ko.n_angular_turnings(float(a), float(th) * np.pi / 180, A, B, tau[2])
+        assert np.array_equal(n, g['n%d' % i], equal_nan=True), i
+        assert np.array_equal(n1, g['n1_%d' % i], equal_nan=True), i
