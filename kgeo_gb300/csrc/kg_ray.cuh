@@ -713,13 +713,22 @@ KG_HD JacobiW jacobi_add(double snu, double cnu, double dnu, double snv, double 
 }
 
 // Distance rho = 1 - n sn^2 to a pole (n > 1) or near-pole (n slightly below 1, at a
-// turning point close to the polar axis) of a Pi integrand below which a sample is not
-// produced by the recurrence: there the recurrence state's rounding is amplified by 1/rho,
-// so that sample and the one after it are evaluated directly and the recurrence is
-// re-seeded from them.
+// turning point close to the polar axis) of a Pi integrand. Within rho < POLE_RHO_PI of any
+// characteristic, at the previous or the new sample, the recurrence state's rounding is
+// amplified by 1/rho: that sample and the one after it are evaluated directly and the
+// recurrence is re-seeded from them. The radial characteristic n0 is also the pole of the r
+// formula (r ~ 1 / (1 - n0 sn^2)), so r carries the recurrence's drift of sn amplified by
+// 1 / rho over the wider zone rho < POLE_RHO_R: there the step keeps its integrals but takes
+// sn, cn, dn from a direct Jacobi evaluation. (FP64 parity within the conditioning bar
+// max(1e-10, 10 eps / rho), measured over seeded 512x512-range draws.) POLE_RHO is the
+// float-float path's zone (kg_mixed.cuh, kg_mixed2.cuh).
 constexpr double POLE_RHO = 2.0e-2;
+constexpr double POLE_RHO_R = 5.0e-3;
+constexpr double POLE_RHO_PI = 1.0e-3;
 
-KG_HD bool near_pi_pole(double n, double sn) { return n > 0.0 && fabs(1.0 - n * (sn * sn)) < POLE_RHO; }
+KG_HD bool near_pi_pole(double n, double sn, double rho_max = POLE_RHO) {
+  return n > 0.0 && fabs(1.0 - n * (sn * sn)) < rho_max;
+}
 
 // Pi(n; am(u+v)) - Pi(n; am u) - Pi(n; am v) for parameter m, c = n (m - n)(1 - n):
 //   n S3 sgn(X) R_C(X^2, X^2 - c S3^2)
@@ -829,7 +838,7 @@ KG_HD bool theta_step(const FV& f, ThetaState* st) {
   const double snv = -f[S_TSN], cnv = f[S_TCN], dnv = f[S_TDN];
   JacobiW w = jacobi_add(st->sn, st->cn, st->dn, snv, cnv, dnv, kk);
   double S3 = st->sn * snv * w.sn;
-  if (near_pi_pole(n, st->sn) || near_pi_pole(n, w.sn)) return false;
+  if (near_pi_pole(n, st->sn, POLE_RHO_PI) || near_pi_pole(n, w.sn, POLE_RHO_PI)) return false;
   double pi = st->pi - f[S_TPI] + pi_add_term(n, f[S_TC], st->sn, snv, w);
   st->e = st->e - f[S_TE] - kk * S3;
   st->pi = pi;
@@ -898,12 +907,20 @@ KG_HD bool radial_step(const FV& f, RadialState* st, double Xnew) {
   const double k = f[R_M];
   const double snv = -f[S_RSN], cnv = f[S_RCN], dnv = f[S_RDN];
   JacobiW w = jacobi_add(st->sn, st->cn, st->dn, snv, cnv, dnv, k);
-  double S3 = st->sn * snv * w.sn;
   const double n0 = f[R_N0], n1 = f[R_N1], n2 = f[R_N2];
   // reject when the previous sample or this one is next to a pole of a Pi integrand
-  if (near_pi_pole(n0, st->sn) || near_pi_pole(n1, st->sn) || near_pi_pole(n2, st->sn) ||
-      near_pi_pole(n0, w.sn) || near_pi_pole(n1, w.sn) || near_pi_pole(n2, w.sn))
+  if (near_pi_pole(n0, st->sn, POLE_RHO_PI) || near_pi_pole(n0, w.sn, POLE_RHO_PI) ||
+      near_pi_pole(n1, st->sn, POLE_RHO_PI) || near_pi_pole(n2, st->sn, POLE_RHO_PI) ||
+      near_pi_pole(n1, w.sn, POLE_RHO_PI) || near_pi_pole(n2, w.sn, POLE_RHO_PI))
     return false;
+  // next to the pole of the r formula: fresh sn, cn, dn at the new argument
+  if (near_pi_pole(n0, st->sn, POLE_RHO_R) || near_pi_pole(n0, w.sn, POLE_RHO_R)) {
+    const RadialState d = radial_state_direct(f, 0, Xnew, false);
+    w.sn = d.sn;
+    w.cn = d.cn;
+    w.dn = d.dn;
+  }
+  double S3 = st->sn * snv * w.sn;
   double p0 = st->P[0] - f[S_RP0] + pi_add_term(n0, f[S_RC0], st->sn, snv, w);
   double p1 = st->P[1] - f[S_RP1] + pi_add_term(n1, f[S_RC1], st->sn, snv, w);
   double p2 = st->P[2] - f[S_RP2] + pi_add_term(n2, f[S_RC2], st->sn, snv, w);
