@@ -40,10 +40,12 @@ CPU_SAMPLE_RAYS = 16384      # rays of the bounded CPU sample (every 16th pixel 
 # FP64 floating-point work of the sample kernel (addition-theorem recurrence, chunks of 50)
 # per geodesic point on this workload, from the ncu capture summarised in
 # profiles/geo_samples_fp64_config2.md: (dadd + dmul + 2 dfma thread instructions) / points.
-# Used for roofline.achieved.
-FP64_FLOP_PER_POINT = 1179
+# Used for roofline.achieved. FP64_INST_PER_POINT: FP64 pipe instructions (dadd + dmul +
+# dfma) per point, against the pipe's rate (fp64_peak / 2 instructions per second).
+FP64_FLOP_PER_POINT = 758
+FP64_INST_PER_POINT = 483
 # DRAM bytes per point of the same capture (dram__bytes_read + dram__bytes_write) / points
-DRAM_BYTES_PER_POINT = 54.3
+DRAM_BYTES_PER_POINT = 54.2
 BYTES_PER_POINT = 48          # t, r, theta, phi, sigma, Mino tau written per point (8 B each)
 L2_FLUSH_BYTES = 256 << 20
 
@@ -270,7 +272,8 @@ def run_ours(args):
             'traffic_source': 'ncu dram__bytes_read+write of a 128x128 capture, scaled by points'}
     if FP64_FLOP_PER_POINT:
         ach = FP64_FLOP_PER_POINT * points / (samp_ms * 1e-3) / 1e12
-        roof.update({'achieved': ach, 'frac': ach / fp64_peak, 'fp64_flop_per_point': FP64_FLOP_PER_POINT})
+        roof.update({'achieved': ach, 'frac': ach / fp64_peak, 'fp64_flop_per_point': FP64_FLOP_PER_POINT,
+                     'fp64_pipe_frac': FP64_INST_PER_POINT * points / (samp_ms * 1e-3) / (fp64_peak * 1e12 / 2)})
     else:
         roof.update({'achieved': None, 'frac': None})
     hbm = BYTES_PER_POINT * points / (samp_ms * 1e-3) / 1e9
