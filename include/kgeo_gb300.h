@@ -304,6 +304,46 @@ int kgeo_rho_of_req(const kgeo_curve* curves, int32_t ncurves, const double* var
  * NaN. alpha, beta: (n) device arrays. */
 int kgeo_critical_curve(double a, double th_o, int64_t n, double* alpha, double* beta, void* stream);
 
+/* Crossings of the geodesics with a jet field line psi(r, theta) = psi_target
+ * (kgeo/solver.py:14-207; the solver of the off-equatorial model, kgeo/off_eq.py:124-172).
+ * Field lines: KGEO_JET_PARA psi_BZ_para (the BZ paraboloid), KGEO_JET_MONO psi_BZ_mono,
+ * KGEO_JET_POWER r^p (1 - |cos theta|). */
+#define KGEO_JET_PARA 0
+#define KGEO_JET_MONO 1
+#define KGEO_JET_POWER 2
+typedef struct {
+  int32_t model;     /* KGEO_JET_* */
+  int32_t reserved;
+  double psitarget;  /* psi of the field line */
+  double pval;       /* power: p */
+} kgeo_jet_field;
+
+/* getguesses (kgeo/solver.py:97-134) on a sampled geodesic set: r, th, mino (ngeo, npix)
+ * device arrays (kgeo_raytrace's outputs) and the pixels alpha, beta. count (npix, may be
+ * NULL): the number of Mino-time guesses of each pixel (the sign changes of psi - psi_target
+ * before the search bound of get_maxtau_forwardjet, endpoints excluded; 2 for the flat-space
+ * guesses of a nearly face-on view at impact parameter > 100; 1 (the guess -1) when there is
+ * none). guesses (nguess, npix, may be NULL): the guesses padded with -1 (pixels with more than
+ * nguess are all -1: size nguess from max(count)). taumax (npix, may be NULL): the bound
+ * (get_maxtau_forwardjet, :57-87); with r == NULL only taumax is computed. neqmax <= 0: no
+ * bound but the total Mino time. */
+int kgeo_jet_guesses(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                     const double* r, const double* th, const double* mino, int32_t ngeo,
+                     const kgeo_jet_field* field, int32_t neqmax, double* taumax, int32_t* count, double* guesses,
+                     int32_t nguess, void* stream);
+
+/* findroot (kgeo/solver.py:136-207): from each guess (nguess, npix), the Mino time tau of the
+ * crossing by the secant iteration of scipy.optimize.newton (tol on the step, maxiter steps),
+ * the coordinates r, th there, the signs of p_r and p_theta (from the coordinates at
+ * tau (1 + 1e-5)) and neq, the equatorial crossings before tau (getneq, :40-55). Entries of a
+ * -1 guess are 0 but neq. Every output is (nguess, npix), device memory; any but tau may be
+ * NULL; status (may be NULL): 0 converged, 1 not within maxiter (scipy warns). workspace: device
+ * scratch of kgeo_workspace_size(npix) bytes or NULL. */
+int kgeo_jet_findroot(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                      const double* guesses, int32_t nguess, const kgeo_jet_field* field, double tol, int32_t maxiter,
+                      void* workspace, size_t workspace_bytes, double* tau, double* r, double* th, double* signpr,
+                      double* signpth, double* neq, int32_t* status, void* stream);
+
 /* Batched tracing: many images of different size, spin, inclination and ngeo traced as one
  * job (no counterpart in the reference, whose raytrace_ana takes one image per call:
  * kgeo/kerr_raytracing_ana.py:46). A plan describes the images; kgeo_batch_bind attaches the

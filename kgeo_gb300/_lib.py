@@ -56,6 +56,11 @@ class Curve(ctypes.Structure):
                 ('rho_max', c_double), ('mbar', c_int32), ('reserved', c_int32)]
 
 
+class JetField(ctypes.Structure):
+    """kgeo_jet_field."""
+    _fields_ = [('model', c_int32), ('reserved', c_int32), ('psitarget', c_double), ('pval', c_double)]
+
+
 class BatchImage(ctypes.Structure):
     """kgeo_batch_image."""
     _fields_ = [('a', c_double), ('r_o', c_double), ('th_o', c_double), ('npix', c_int64), ('ngeo', c_int32),
@@ -69,6 +74,7 @@ class BatchConfig(ctypes.Structure):
 
 EMIS = {'bpl': 0, 'constant': 1, 'glm': 2, 'ring': 3}
 VEL = {'zamo': 0, 'infall': 1, 'kep': 2, 'cunningham': 2, 'subkep': 3, 'cunningham_subkep': 3, 'general': 4}
+JET = {'para': 0, 'mono': 1, 'power': 2}
 BFIELD = {'simple': 0, 'rad': 0, 'vert': 0, 'tor': 0, 'simple_rm1': 1, 'monopoleA': 2, 'bz_guess': 3,
           'bz_monopole': 4, 'bz_para': 5, 'power': 6, 'gen_power': 7}
 N_IMAGE_PARAMS = 7  # a, th_o, emis_p[0..1], vel_p[0..2]
@@ -103,6 +109,12 @@ SIGNATURES = {
                               c_void_p]),
     'kgeo_angular_turnings': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_void_p, c_int32,
                                       c_void_p, c_void_p]),
+    'kgeo_jet_guesses': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p,
+                                 c_int32, ctypes.POINTER(JetField), c_int32, c_void_p, c_void_p, c_void_p, c_int32,
+                                 c_void_p]),
+    'kgeo_jet_findroot': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_void_p, c_int32,
+                                  ctypes.POINTER(JetField), c_double, c_int32, c_void_p, c_size_t, c_void_p, c_void_p,
+                                  c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     'kgeo_rho_of_req': (c_int, [ctypes.POINTER(Curve), c_int32, c_void_p, c_int32, c_double, c_double, c_int32,
                                 c_void_p, c_void_p, c_void_p]),
     'kgeo_critical_curve': (c_int, [c_double, c_double, c_int64, c_void_p, c_void_p, c_void_p]),

@@ -29,6 +29,7 @@ UNITS = [
     ('kg_noalloc.cu', []),
     ('kg_batch.cu', []),
     ('kg_curves.cu', ['-fmad=false']),
+    ('kg_jet.cu', ['-fmad=false']),
 ]
 
 

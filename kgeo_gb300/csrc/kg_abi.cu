@@ -460,6 +460,89 @@ int kgeo_rho_of_req(const kgeo_curve* curves, int32_t ncurves, const double* var
   return ok ? KGEO_OK : KGEO_ERR_CUDA;
 }
 
+namespace {
+int make_jet_field(const kgeo_jet_field* j, double a, JetField* out) {
+  if (!j) return KGEO_ERR_NULL;
+  if (j->model < KGEO_JET_PARA || j->model > KGEO_JET_POWER) return KGEO_ERR_MODEL;
+  if (!std::isfinite(j->psitarget) || !std::isfinite(j->pval)) return KGEO_ERR_MODEL;
+  out->model = j->model;
+  out->psitarget = j->psitarget;
+  out->pval = j->pval;
+  out->rp = 1 + std::sqrt(1 - a * a);
+  return KGEO_OK;
+}
+}  // namespace
+
+int kgeo_jet_guesses(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                     const double* r, const double* th, const double* mino, int32_t ngeo,
+                     const kgeo_jet_field* field, int32_t neqmax, double* taumax, int32_t* count, double* guesses,
+                     int32_t nguess, void* stream) {
+  int st = check_observer(obs);
+  if (st) return st;
+  if (npix < 0) return KGEO_ERR_LENGTHS;
+  if (ngeo < 0 || nguess < 0) return KGEO_ERR_NGEO;
+  JetGuessArgs ga;
+  st = make_jet_field(field, obs->a, &ga.field);
+  if (st) return st;
+  if (npix > 0 && (!alpha || !beta)) return KGEO_ERR_NULL;
+  if (npix > 0 && r && (!th || !mino)) return KGEO_ERR_NULL;
+  ga.obs = make_observer(obs);
+  ga.alpha = alpha;
+  ga.beta = beta;
+  ga.npix = npix;
+  ga.r = r;
+  ga.th = th;
+  ga.mino = mino;
+  ga.ngeo = ngeo;
+  ga.neqmax = neqmax;
+  ga.taumax = taumax;
+  ga.count = count;
+  ga.guesses = guesses;
+  ga.nguess = nguess;
+  return launch_jet_guesses(ga, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
+}
+
+int kgeo_jet_findroot(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                      const double* guesses, int32_t nguess, const kgeo_jet_field* field, double tol, int32_t maxiter,
+                      void* workspace, size_t workspace_bytes_, double* tau, double* r, double* th, double* signpr,
+                      double* signpth, double* neq, int32_t* status, void* stream) {
+  int st = check_observer(obs);
+  if (st) return st;
+  if (npix < 0) return KGEO_ERR_LENGTHS;
+  if (nguess < 0) return KGEO_ERR_NGEO;
+  if (!(tol > 0) || maxiter < 1) return KGEO_ERR_SOLVER;
+  JetSolveArgs ja;
+  st = make_jet_field(field, obs->a, &ja.field);
+  if (st) return st;
+  if (npix > 0 && nguess > 0 && (!alpha || !beta || !guesses || !tau)) return KGEO_ERR_NULL;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Scratch sc;
+  st = get_scratch(sc, workspace, workspace_bytes_, npix, s);
+  if (st) return st;
+  Workspace w = carve_workspace(sc.ptr, npix);
+  st = setup_common(obs, alpha, beta, npix, 0, 1.0 - 1.e-10, w, nullptr, s);
+  if (st) return st;
+  ja.obs = make_observer(obs);
+  ja.rec = w.rec;
+  ja.code = w.code;
+  ja.flags = w.flags;
+  ja.alpha = alpha;
+  ja.beta = beta;
+  ja.npix = npix;
+  ja.guesses = guesses;
+  ja.nguess = nguess;
+  ja.tol = tol;
+  ja.maxiter = maxiter;
+  ja.tau = tau;
+  ja.r = r;
+  ja.th = th;
+  ja.signpr = signpr;
+  ja.signpth = signpth;
+  ja.neq = neq;
+  ja.status = status;
+  return launch_jet_solve(ja, s) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
+}
+
 int kgeo_critical_curve(double a, double th_o, int64_t n, double* alpha, double* beta, void* stream) {
   kgeo_observer o{a, INFINITY, th_o};
   int st = check_observer(&o);

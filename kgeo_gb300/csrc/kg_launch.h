@@ -6,6 +6,7 @@
 
 #include "kg_polar.cuh"
 #include "kg_curves.cuh"
+#include "kg_jet.cuh"
 
 namespace kg {
 
@@ -239,6 +240,48 @@ struct CriticalArgs {
   double* beta;
 };
 
+// jet field-line crossings (kg_jet.cu)
+struct JetGuessArgs {
+  Observer obs;
+  JetField field;
+  const double* alpha;
+  const double* beta;
+  int64_t npix;
+  const double* r;      // (ngeo, npix) samples, or NULL: taumax only
+  const double* th;
+  const double* mino;
+  int64_t ngeo;
+  int neqmax;           // <= 0: no limit
+  double* taumax;       // (npix) or NULL
+  int32_t* count;       // (npix) or NULL
+  double* guesses;      // (nguess, npix) or NULL
+  int64_t nguess;
+};
+
+struct JetSolveArgs {
+  Observer obs;
+  JetField field;
+  const double* rec;
+  const int* code;
+  const uint32_t* flags;
+  const double* alpha;
+  const double* beta;
+  int64_t npix;
+  const double* guesses;  // (nguess, npix)
+  int64_t nguess;
+  double tol;
+  int maxiter;
+  double* tau;
+  double* r;
+  double* th;
+  double* signpr;
+  double* signpth;
+  double* neq;
+  int32_t* status;
+};
+
+cudaError_t launch_jet_guesses(const JetGuessArgs& a, cudaStream_t s);
+cudaError_t launch_jet_solve(const JetSolveArgs& a, cudaStream_t s);
 cudaError_t launch_curves(const CurveArgs& a, cudaStream_t s);
 cudaError_t launch_critical(const CriticalArgs& a, cudaStream_t s);
 cudaError_t launch_image(const ImageArgs& a, cudaStream_t s);

@@ -1416,6 +1416,122 @@ def critical_curve(a, th0, n=100000):
 
 
 # ----------------------------------------------------------------------------
+# off-equatorial jet: crossings of the geodesics with a field line psi = psi_target
+# ----------------------------------------------------------------------------
+
+JET_MAXTAUFRAC = 1. - 1.e-10   # kgeo/solver.py:12
+
+
+def psifunc(r, theta, a, model='para', pval=1):
+    """Stream function psi(r, theta) of the jet models; kgeo/solver.py:14-38."""
+    abscth = np.abs(np.cos(theta))
+    if model == 'para':
+        rp = 1 + np.sqrt(1 - a ** 2)
+        return r * (1 - abscth) + rp * (1 + abscth) * (1 - np.log(1 + abscth)) - 2 * rp * (1 - np.log(2))
+    if model == 'mono':
+        return 1 - abscth
+    if model == 'power':
+        return r ** pval * (1 - abscth)
+    return 0
+
+
+def get_maxtau_forwardjet(a, r_o, th_o, alpha, beta, neqmax=1):
+    """Mino time bound of the crossing search (the neqmax-th equatorial crossing, or the
+    total); kgeo/solver.py:57-87."""
+    lam = -alpha * np.sin(th_o)
+    eta = (alpha ** 2 - a ** 2) * np.cos(th_o) ** 2 + beta ** 2
+    r1, r2, r3, r4, _ = quartic_roots(a, lam, eta)
+    tau_tot2 = mino_total(a, r_o, eta, r1, r2, r3, r4) * JET_MAXTAUFRAC
+    if neqmax is None:
+        return tau_tot2
+    up, um, ratio, a2um = u_roots(a, th_o, lam, eta)
+    F0 = sp.ellipkinc(np.arcsin(np.cos(th_o) / np.sqrt(up)), ratio)
+    K = sp.ellipkinc(0.5 * np.pi, ratio)
+    mmax = (neqmax - 1) + np.heaviside(beta, 0)
+    taumax = (2 * mmax * K - np.sign(beta) * F0) / np.sqrt(-um * a ** 2)
+    taumax[eta <= 0] = tau_tot2[eta <= 0]
+    return np.min(np.array([taumax, tau_tot2]), axis=0)
+
+
+def getguesses(geo, a, rout, inc, alphas, betas, psitarget, ngeo, neqmax=1, model='para', pval=1):
+    """Mino-time guesses of the crossings: midpoints of the sampled geodesic's sign changes of
+    psi - psi_target before the search bound (endpoints excluded), or the flat-space guesses
+    of nearly face-on views at large impact parameter; padded with -1 to (guesses, npix).
+    kgeo/solver.py:97-134. geo: dict with 'r', 'th', 'mino_times' (ngeo, npix)."""
+    out = []
+    taumaxes = get_maxtau_forwardjet(a, rout, inc, alphas, betas, neqmax=neqmax)
+    psig = psifunc(geo['r'], geo['th'], a, model=model, pval=pval) - psitarget
+    for i in range(len(alphas)):
+        b = np.sqrt(alphas[i] ** 2 + betas[i] ** 2)
+        if np.abs(np.sin(inc)) < .1 and b > 100:
+            if model == 'power' and pval > 0:
+                rparam = (b ** 2 / (2 * psitarget)) ** (1 / (2 - pval))
+                out.append(np.array([1 / rparam, 2 / b - 1 / rparam]))
+                continue
+            elif model == 'para':
+                rparam = (b ** 2 + psitarget ** 2) / (2 * psitarget)
+                out.append(np.array([1 / rparam, 2 / b - 1 / rparam]))
+                continue
+        mf = np.roll(psig[:, i], -1) * psig[:, i]
+        indmax = np.argmin(np.abs(geo['mino_times'][:, i] - taumaxes[i]))
+        mf = mf[:indmax + 1][1:-2]
+        js = np.where(mf < 0)[0] + 1
+        if len(js) == 0:
+            out.append(np.array([-1]))
+            continue
+        out.append(np.array([(geo['mino_times'][j, i] + geo['mino_times'][j + 1, i]) / 2 for j in js]))
+    n = max(len(x) for x in out)
+    res = -np.ones((len(out), n))
+    for i, x in enumerate(out):
+        res[i, :len(x)] = x
+    return np.transpose(res)
+
+
+def getneq(a, tau, u_minus, u_plus, th_o, betas):
+    """Equatorial crossings before Mino time tau (GL19b Eqs 81-82); kgeo/solver.py:40-55."""
+    ratio = u_plus / u_minus
+    F0 = sp.ellipkinc(np.arcsin(np.cos(th_o) / np.sqrt(u_plus)), ratio)
+    K = sp.ellipkinc(0.5 * np.pi, ratio)
+    mval = (np.sqrt(-u_minus * a ** 2) * tau + np.sign(betas) * F0) / (2 * K)
+    return np.ceil(np.nan_to_num(mval - np.heaviside(betas, 0)))
+
+
+def findroot(geo, psitarget, alpha, beta, r_o, th_o, a, ngeo, model='para', neqmax=1, tol=1e-8, pval=1):
+    """(tau, r_s, th_s, sign p_r, sign p_theta, n_eq, guesses shape) of every crossing of the
+    geodesics with psi = psi_target: scipy.optimize.newton (secant) from getguesses' Mino times
+    on coords_at_tau; kgeo/solver.py:136-207."""
+    from scipy.optimize import newton
+    guesses = getguesses(geo, a, r_o, th_o, alpha, beta, psitarget, ngeo, neqmax=neqmax, model=model, pval=pval)
+    shape = guesses.shape
+    G = shape[0]
+    At = np.tile(alpha, G)
+    Bt = np.tile(beta, G)
+    g = guesses.flatten()
+
+    def f(tau):
+        _, (t, r, th, ph) = coords_at_tau(a, r_o, th_o, At, Bt, np.reshape(tau, (1, len(tau))))
+        v = psifunc(r[0], th[0], a, model=model, pval=pval) - psitarget
+        v[g == -1] = 0
+        return v
+
+    with np.errstate(all='ignore'):
+        root = newton(f, g, maxiter=500, tol=tol)
+        _, (t0, r0, th0, ph0) = coords_at_tau(a, r_o, th_o, At, Bt, root.reshape(1, -1))
+        _, (t1, r1, th1, ph1) = coords_at_tau(a, r_o, th_o, At, Bt, (root * (1 + 1e-5)).reshape(1, -1))
+    signpr = np.sign(r0 - r1)[0]
+    signpth = np.sign(th0 - th1)[0]
+    r_s = np.copy(r0[0])
+    th_s = np.copy(th0[0])
+    lam, eta = conserved(a, th_o, At, Bt)
+    up, um, _, _ = u_roots(a, th_o, lam, eta)
+    with np.errstate(all='ignore'):
+        neq = getneq(a, root, um, up, th_o, Bt)
+    none = g == -1
+    root[none] = r_s[none] = th_s[none] = signpr[none] = signpth[none] = 0
+    return root, r_s, th_s, signpr, signpth, neq, shape
+
+
+# ----------------------------------------------------------------------------
 # conditioning helper for the parity tests
 # ----------------------------------------------------------------------------
 

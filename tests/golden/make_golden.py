@@ -347,6 +347,27 @@ def main(path):
                      'n%d' % i: nt, 'n1_%d' % i: nt1})
     save('angular_turnings', tout)
 
+    # off-equatorial jet crossings (solver.findroot on a sampled geodesic set)
+    import kgeo.solver as solver
+    jcases = [(0.9, 17., 'para', 1.0, 1, 1, 24, 8.), (0.5, 60., 'mono', 0.3, 1, 2, 24, 8.),
+              (0.94, 163., 'power', 1.5, 0.75, 1, 24, 8.), (0.7, 3., 'para', 2.0, 1, 1, 12, 150.),
+              (0.3, 40., 'power', 0.8, 0.0, 2, 20, 10.)]
+    jout = dict(ncase=len(jcases))
+    for i, (a, inc, model, psit, pval, neqmax, nside, lim) in enumerate(jcases):
+        x = np.linspace(-lim, lim, nside)
+        A, B = (v.flatten() for v in np.meshgrid(x, x))
+        with warnings.catch_warnings():
+            warnings.simplefilter('ignore')
+            geo = quiet(ref.ana.raytrace_ana, a=a, observer_coords=[0, 1.e4, inc * deg, 0], image_coords=[A, B],
+                        ngeo=200, plotdata=False, savedata=False)
+            res = quiet(solver.findroot, geo, psit, A, B, 1.e4, inc * deg, a, 200, model=model, neqmax=neqmax,
+                        tol=1e-8, pval=pval)
+        jout['case%d' % i] = repr((a, inc, model, psit, pval, neqmax, nside, lim))
+        for k, v in zip(['tau', 'r', 'th', 'signpr', 'signpth', 'neq'], res[:6]):
+            jout['%s%d' % (k, i)] = np.asarray(v)
+        jout['shape%d' % i] = np.array(res[6])
+    save('jet_crossings', jout)
+
     # EVPA of ipole images (the reference's tests/data/*.csv, from tests/test_images.py):
     # pixel location and EVPA along the middle row / column for image orders 0 and 1
     ip = {}
