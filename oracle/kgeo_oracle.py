@@ -1496,10 +1496,12 @@ def getneq(a, tau, u_minus, u_plus, th_o, betas):
     return np.ceil(np.nan_to_num(mval - np.heaviside(betas, 0)))
 
 
-def findroot(geo, psitarget, alpha, beta, r_o, th_o, a, ngeo, model='para', neqmax=1, tol=1e-8, pval=1):
+def findroot(geo, psitarget, alpha, beta, r_o, th_o, a, ngeo, model='para', neqmax=1, tol=1e-8, pval=1,
+             converged=False):
     """(tau, r_s, th_s, sign p_r, sign p_theta, n_eq, guesses shape) of every crossing of the
     geodesics with psi = psi_target: scipy.optimize.newton (secant) from getguesses' Mino times
-    on coords_at_tau; kgeo/solver.py:136-207."""
+    on coords_at_tau; kgeo/solver.py:136-207. converged=True appends newton's per-guess
+    convergence flags."""
     from scipy.optimize import newton
     guesses = getguesses(geo, a, r_o, th_o, alpha, beta, psitarget, ngeo, neqmax=neqmax, model=model, pval=pval)
     shape = guesses.shape
@@ -1515,7 +1517,7 @@ def findroot(geo, psitarget, alpha, beta, r_o, th_o, a, ngeo, model='para', neqm
         return v
 
     with np.errstate(all='ignore'):
-        root = newton(f, g, maxiter=500, tol=tol)
+        root, conv, _ = newton(f, g, maxiter=500, tol=tol, full_output=True)[:3]
         _, (t0, r0, th0, ph0) = coords_at_tau(a, r_o, th_o, At, Bt, root.reshape(1, -1))
         _, (t1, r1, th1, ph1) = coords_at_tau(a, r_o, th_o, At, Bt, (root * (1 + 1e-5)).reshape(1, -1))
     signpr = np.sign(r0 - r1)[0]
@@ -1528,6 +1530,8 @@ def findroot(geo, psitarget, alpha, beta, r_o, th_o, a, ngeo, model='para', neqm
         neq = getneq(a, root, um, up, th_o, Bt)
     none = g == -1
     root[none] = r_s[none] = th_s[none] = signpr[none] = signpth[none] = 0
+    if converged:
+        return root, r_s, th_s, signpr, signpth, neq, shape, conv
     return root, r_s, th_s, signpr, signpth, neq, shape
 
 
