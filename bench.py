@@ -902,6 +902,105 @@ def run_library(args):
 
 
 # ---------------------------------------------------------------------------
+# jet field-line crossings (kgeo.solver.findroot) on a traced image
+# ---------------------------------------------------------------------------
+
+JET_GRID = 256
+JET_CASE = dict(a=0.9, inc=17.0, model='para', psitarget=1.0, ngeo=200, neqmax=1)
+CPU_JET_SAMPLE = 2048     # pixels of the bounded CPU sample
+
+
+def _cpu_jet_chunk(args):
+    A, B = args
+    from oracle import kgeo_oracle as ko
+    import warnings
+    warnings.filterwarnings('ignore')
+    c = JET_CASE
+    th = c['inc'] * np.pi / 180
+    geo = ko.raytrace(c['a'], R_O, th, A, B, c['ngeo'])
+    ko.findroot(geo, c['psitarget'], A, B, R_O, th, c['a'], c['ngeo'], model=c['model'], neqmax=c['neqmax'])
+    return len(A)
+
+
+def run_jet(args):
+    small = args.case == 'jet-small'
+    pool = cores = None
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()
+    import torch
+    from kgeo_gb300 import device as dev
+    from kgeo_gb300 import solver
+    from kgeo_gb300.kerr_raytracing_ana import raytrace_ana
+    c = JET_CASE
+    n = 64 if small else JET_GRID
+    x = np.linspace(-10, 10, n)
+    A, B = (v.flatten() for v in np.meshgrid(x, x))
+    th = c['inc'] * np.pi / 180
+    al, be = dev.as_device(A), dev.as_device(B)
+    res = dev.trace(c['a'], R_O, th, al, be, ngeo=c['ngeo'])
+
+    class Geo:
+        r_s, th_s, mino_times = res['r'], res['th'], res['mino']
+    g = solver.getguesses(Geo, c['a'], R_O, th, A, B, c['psitarget'], c['ngeo'], neqmax=c['neqmax'], model=c['model'])
+    gd = torch.from_numpy(g).cuda()
+    nsolve = int((g != -1).sum())
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    for _ in range(args.warmup):
+        solver.findroot_device(c['a'], R_O, th, al, be, gd, c['psitarget'], model=c['model'])
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(args.steps):
+        out = solver.findroot_device(c['a'], R_O, th, al, be, gd, c['psitarget'], model=c['model'])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    t_step = e0.elapsed_time(e1) / 1e3 / args.steps
+    conv = int(((out['status'] == 0) & (gd != -1)).sum())
+    # end to end: numpy pixels in -> raytrace_ana -> findroot -> numpy crossings out
+    geo = raytrace_ana(a=c['a'], observer_coords=[0, R_O, th, 0], image_coords=[A, B], ngeo=c['ngeo'], plotdata=False)
+    solver.findroot(geo, c['psitarget'], A, B, R_O, th, c['a'], c['ngeo'], model=c['model'], neqmax=c['neqmax'])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        geo = raytrace_ana(a=c['a'], observer_coords=[0, R_O, th, 0], image_coords=[A, B], ngeo=c['ngeo'],
+                           plotdata=False)
+        solver.findroot(geo, c['psitarget'], A, B, R_O, th, c['a'], c['ngeo'], model=c['model'], neqmax=c['neqmax'])
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    cpu = None
+    if pool is not None:
+        idx = np.arange(0, A.size, max(1, A.size // CPU_JET_SAMPLE))[:CPU_JET_SAMPLE]
+        chunks = np.array_split(idx, cores * 2)
+        t0 = time.time()
+        pool.map(_cpu_jet_chunk, [(A[k], B[k]) for k in chunks])
+        dt = time.time() - t0
+        cpu = {'value': idx.size / dt, 'unit': 'pixels/s (trace + findroot)', 'cores': cores, 'kind': 'port',
+               'sample': '%d pixels (every %dth of the %dx%d grid): oracle raytrace + findroot (scipy newton) on a '
+                         '%d-process pool, %.1f s wall' % (idx.size, A.size // idx.size, n, n, cores, dt)}
+        pool.close()
+    line = {
+        'metric': 'crossing solves/s: jet field-line crossings (findroot secant per guess)',
+        'value': nsolve / t_step, 'unit': 'solves/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': t_step * 1e3, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f64', 'data': 'synthetic: uniform image-plane grid over [-10, 10] M',
+        'config': {'workload': 'a=0.9, theta_o=17 deg, r_o=1e4, %dx%d, ngeo=200, BZ paraboloid psi=1, neqmax=1' % (n, n),
+                   'guesses': list(g.shape), 'solves': nsolve, 'converged': conv, 'case': args.case,
+                   'l2': 'compute-bound (per-ray records 584 B / pixel)'},
+        'roofline': {'bound': 'fp64', 'kernel': 'jet_solve_kernel', 'launch_ms': t_step * 1e3, 'achieved': None,
+                     'frac': None, 'traffic': None},
+        'cpu_baseline': cpu,
+        'e2e': {'value': A.size / t_e2e, 'unit': 'pixels/s (trace + findroot)', 'h2d_bytes_per_step': 16 * A.size,
+                'd2h_bytes_per_step': 48 * c['ngeo'] * A.size + 48 * g.size, 'ms_per_step': t_e2e * 1e3,
+                'path': 'raytrace_ana + kgeo_gb300.solver.findroot (numpy in/out)'},
+        'gpu_launches': args.steps, 'clocks': ck,
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
 # configuration 4: batched images (64 images, one persistent launch, CUDA graph)
 # ---------------------------------------------------------------------------
 
@@ -1063,7 +1162,8 @@ def main():
     p.add_argument('--warmup', type=int, default=3)
     p.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     p.add_argument('--case', choices=('full', 'small', 'mixed', 'mixed-small', 'image', 'image-small', 'batch',
-                                      'batch-small', 'polimage', 'polimage-small', 'library', 'library-small'),
+                                      'batch-small', 'polimage', 'polimage-small', 'library', 'library-small', 'jet',
+                                      'jet-small'),
                    default='full')
     p.add_argument('--no-cpu-baseline', action='store_true')
     args = p.parse_args()
@@ -1077,6 +1177,8 @@ def main():
         run_polimage(args)
     elif args.case.startswith('library'):
         run_library(args)
+    elif args.case.startswith('jet'):
+        run_jet(args)
     elif args.case.startswith('batch'):
         run_batch(args)
     else:
