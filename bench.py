@@ -798,6 +798,24 @@ def run_polimage(args):
 # ---------------------------------------------------------------------------
 
 CPU_LIB_SAMPLE = 600     # (curve, angle) roots of the bounded CPU sample
+# FP64 work of curve_kernel per root on the library-small capture (profiles/curve_library_jet.md):
+# (dadd + dmul + 2 dfma) thread instructions / roots, and FP64 pipe instructions / roots
+LIB_FLOP_PER_ROOT = 153960
+LIB_FP64_INST_PER_ROOT = 102000
+
+
+def roofline_fp64(kernel, t, units, flop_per_unit, inst_per_unit, unit):
+    """FP64 roofline object of a compute-bound kernel timed alone: achieved TFLOP/s from the
+    captured FLOP per unit, against the FP64 FMA peak measured live; the FP64 pipe's
+    instruction rate is fp64_peak / 2 per second."""
+    from kgeo_gb300 import device as dev
+    peak = dev.fp64_peak_tflops()
+    ach = flop_per_unit * units / t / 1e12
+    return {'bound': 'fp64', 'unit': 'TFLOP/s', 'kernel': kernel, 'launch_ms': t * 1e3, 'peak': peak,
+            'peak_source': 'FP64 FMA loop measured live by bench.py (kgeo_measure_fp64_peak)',
+            'achieved': ach, 'frac': ach / peak, 'fp64_flop_per_%s' % unit: flop_per_unit,
+            'fp64_pipe_frac': inst_per_unit * units / t / (peak * 1e12 / 2), 'traffic': None,
+            'traffic_note': 'compute-bound; inputs and outputs are a few bytes per unit'}
 
 
 def library_workload(small=False):
@@ -890,8 +908,8 @@ def run_library(args):
                    'curves': len(curves), 'roots': nroots, 'case': args.case,
                    'failed_roots': int((st != 0).sum()), 'l2': 'compute-bound; inputs and outputs < 160 MB'},
         'curves_per_s': len(curves) / t_step,
-        'roofline': {'bound': 'fp64', 'kernel': 'curve_kernel', 'launch_ms': t_step * 1e3, 'achieved': None,
-                     'frac': None, 'traffic': None},
+        'roofline': roofline_fp64('curve_kernel', t_step, nroots, LIB_FLOP_PER_ROOT, LIB_FP64_INST_PER_ROOT,
+                                  'root'),
         'cpu_baseline': cpu,
         'e2e': {'value': nroots / t_e2e, 'unit': 'roots/s', 'h2d_bytes_per_step': 8 * vp.size + 48 * len(curves),
                 'd2h_bytes_per_step': 12 * nroots, 'ms_per_step': t_e2e * 1e3,
@@ -908,6 +926,10 @@ def run_library(args):
 JET_GRID = 256
 JET_CASE = dict(a=0.9, inc=17.0, model='para', psitarget=1.0, ngeo=200, neqmax=1)
 CPU_JET_SAMPLE = 2048     # pixels of the bounded CPU sample
+# FP64 work of jet_solve_kernel per converged solve on the jet-small capture
+# (profiles/curve_library_jet.md), as for the curve kernel
+JET_FLOP_PER_SOLVE = 14310
+JET_FP64_INST_PER_SOLVE = 8973
 
 
 def _cpu_jet_chunk(args):
@@ -989,8 +1011,8 @@ def run_jet(args):
         'config': {'workload': 'a=0.9, theta_o=17 deg, r_o=1e4, %dx%d, ngeo=200, BZ paraboloid psi=1, neqmax=1' % (n, n),
                    'guesses': list(g.shape), 'solves': nsolve, 'converged': conv, 'case': args.case,
                    'l2': 'compute-bound (per-ray records 584 B / pixel)'},
-        'roofline': {'bound': 'fp64', 'kernel': 'jet_solve_kernel', 'launch_ms': t_step * 1e3, 'achieved': None,
-                     'frac': None, 'traffic': None},
+        'roofline': roofline_fp64('jet_solve_kernel', t_step, nsolve, JET_FLOP_PER_SOLVE, JET_FP64_INST_PER_SOLVE,
+                                  'solve'),
         'cpu_baseline': cpu,
         'e2e': {'value': A.size / t_e2e, 'unit': 'pixels/s (trace + findroot)', 'h2d_bytes_per_step': 16 * A.size,
                 'd2h_bytes_per_step': 48 * c['ngeo'] * A.size + 48 * g.size, 'ms_per_step': t_e2e * 1e3,
