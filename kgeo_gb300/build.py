@@ -23,6 +23,7 @@ COMMON = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-I', os.path
 UNITS = [
     ('kg_setup.cu', ['-fmad=false']),
     ('kg_image.cu', ['-fmad=false']),
+    ('kg_image_adj.cu', ['-fmad=false']),
     ('kg_samples.cu', []),
     ('kg_abi.cu', []),
     ('kg_peak.cu', []),

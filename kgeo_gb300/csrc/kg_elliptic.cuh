@@ -55,7 +55,7 @@ KG_HD double carlson_rc(double x, double y) {
 }
 
 KG_HD double carlson_rf(double x, double y, double z) {
-  const double x0 = x, y0 = y, z0 = z;
+  const double x0 = x, y0 = y;
   const double A0 = (x + y + z) / 3.0;
   const double Q = RF_Q * fmax(fmax(fabs(A0 - x), fabs(A0 - y)), fabs(A0 - z));
   double A = A0, f = 1.0;
@@ -79,7 +79,7 @@ KG_HD double carlson_rf(double x, double y, double z) {
 // R_F(x,y,z) and R_J(x,y,z,p[i]) for NP values p[i] > 0, sharing the x,y,z duplication.
 template <int NP>
 KG_HD void rj_multi(double x, double y, double z, const double* p_in, double* rj, double* rf) {
-  const double x0 = x, y0 = y, z0 = z;
+  const double x0 = x, y0 = y;
   const double Af0 = (x + y + z) / 3.0;
   const double Qf = RF_Q * fmax(fmax(fabs(Af0 - x), fabs(Af0 - y)), fabs(Af0 - z));
   double Af = Af0;
