@@ -79,7 +79,7 @@ KG_HD double carlson_rf(double x, double y, double z) {
 // R_F(x,y,z) and R_J(x,y,z,p[i]) for NP values p[i] > 0, sharing the x,y,z duplication.
 template <int NP>
 KG_HD void rj_multi(double x, double y, double z, const double* p_in, double* rj, double* rf) {
-  const double x0 = x, y0 = y;
+  const double x0 = x, y0 = y, z0 = z;
   const double Af0 = (x + y + z) / 3.0;
   const double Qf = RF_Q * fmax(fmax(fabs(Af0 - x), fabs(Af0 - y)), fabs(Af0 - z));
   double Af = Af0;
