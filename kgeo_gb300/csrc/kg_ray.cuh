@@ -716,7 +716,9 @@ KG_HD JacobiW jacobi_add(double snu, double cnu, double dnu, double snv, double 
 // turning point close to the polar axis) of a Pi integrand. Within rho < POLE_RHO_PI of any
 // characteristic, at the previous or the new sample, the recurrence state's rounding is
 // amplified by 1/rho: that sample and the one after it are evaluated directly and the
-// recurrence is re-seeded from them. The radial characteristic n0 is also the pole of the r
+// recurrence is re-seeded from them (in the radial state, with one characteristic near its
+// pole, only that Pi is re-evaluated, from fresh sn, cn, dn; E and the other Pi keep stepping).
+// The radial characteristic n0 is also the pole of the r
 // formula (r ~ 1 / (1 - n0 sn^2)), so r carries the recurrence's drift of sn amplified by
 // 1 / rho over the wider zone rho < POLE_RHO_R: there the step keeps its integrals but takes
 // sn, cn, dn from a direct Jacobi evaluation. (FP64 parity within the conditioning bar
@@ -907,23 +909,48 @@ KG_HD bool radial_step(const FV& f, RadialState* st, double Xnew) {
   const double k = f[R_M];
   const double snv = -f[S_RSN], cnv = f[S_RCN], dnv = f[S_RDN];
   JacobiW w = jacobi_add(st->sn, st->cn, st->dn, snv, cnv, dnv, k);
-  const double n0 = f[R_N0], n1 = f[R_N1], n2 = f[R_N2];
-  // reject when the previous sample or this one is next to a pole of a Pi integrand
-  if (near_pi_pole(n0, st->sn, POLE_RHO_PI) || near_pi_pole(n0, w.sn, POLE_RHO_PI) ||
-      near_pi_pole(n1, st->sn, POLE_RHO_PI) || near_pi_pole(n2, st->sn, POLE_RHO_PI) ||
-      near_pi_pole(n1, w.sn, POLE_RHO_PI) || near_pi_pole(n2, w.sn, POLE_RHO_PI))
-    return false;
-  // next to the pole of the r formula: fresh sn, cn, dn at the new argument
-  if (near_pi_pole(n0, st->sn, POLE_RHO_R) || near_pi_pole(n0, w.sn, POLE_RHO_R)) {
-    const RadialState d = radial_state_direct(f, 0, Xnew, false);
-    w.sn = d.sn;
-    w.cn = d.cn;
-    w.dn = d.dn;
+  const double nn[3] = {f[R_N0], f[R_N1], f[R_N2]};
+  // characteristics whose pole is within POLE_RHO_PI of the previous sample or this one
+  bool pole[3];
+  int npole = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    pole[i] = near_pi_pole(nn[i], st->sn, POLE_RHO_PI) || near_pi_pole(nn[i], w.sn, POLE_RHO_PI);
+    npole += pole[i] ? 1 : 0;
+  }
+  if (npole > 1) return false;
+  // next to the pole of the r formula or of a Pi: fresh sn, cn, dn at the new argument
+  int nr = 0;
+  double Jsn = 0.0, am = 0.0;
+  if (npole == 1 || near_pi_pole(nn[0], st->sn, POLE_RHO_R) || near_pi_pole(nn[0], w.sn, POLE_RHO_R)) {
+    double v;
+    nr = (int)reduce_half_period(Xnew, f[R_K2], &v);
+    const Jacobi J = jacobi_landen(v, k);
+    const double odd = (nr & 1) ? -1.0 : 1.0;
+    w.sn = odd * J.sn;
+    w.cn = odd * J.cn;
+    w.dn = J.dn;
+    Jsn = J.sn;
+    am = nr * PI + atan2(J.sn, J.cn);
   }
   double S3 = st->sn * snv * w.sn;
-  double p0 = st->P[0] - f[S_RP0] + pi_add_term(n0, f[S_RC0], st->sn, snv, w);
-  double p1 = st->P[1] - f[S_RP1] + pi_add_term(n1, f[S_RC1], st->sn, snv, w);
-  double p2 = st->P[2] - f[S_RP2] + pi_add_term(n2, f[S_RC2], st->sn, snv, w);
+  double pnew[3];
+  const double sp[3] = {f[S_RP0], f[S_RP1], f[S_RP2]};
+  const double sc[3] = {f[S_RC0], f[S_RC1], f[S_RC2]};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (pole[i]) {
+      // that Pi directly at the new amplitude (one Carlson set: R_F, R_D and its R_J)
+      const double rho = 1.0 - nn[i] * (Jsn * Jsn);
+      double rj, rd, rf;
+      carlson_set<1>(w.cn * w.cn, w.dn * w.dn, 1.0, &rho, &rj, &rd, &rf);
+      const double pic = i == 0 ? f[R_PIC0] : (i == 1 ? f[R_PIC1] : f[R_PIC2]);
+      pnew[i] = pi_assemble(nn[i], am, (double)nr, Jsn * rf + (nn[i] / 3.0) * (Jsn * Jsn * Jsn) * rj, pic, k);
+    } else {
+      pnew[i] = st->P[i] - sp[i] + pi_add_term(nn[i], sc[i], st->sn, snv, w);
+    }
+  }
+  double p0 = pnew[0], p1 = pnew[1], p2 = pnew[2];
   st->E = st->E - f[S_RE] - k * S3;
   st->P[0] = p0;
   st->P[1] = p1;
