@@ -37,7 +37,7 @@ NGEO = 400
 ORDERS = (0, 1, 2)
 R_O = 1.0e4
 CPU_SAMPLE_RAYS = 16384      # rays of the bounded CPU sample (every 16th pixel of the grid)
-# FP64 floating-point work of the sample kernel (addition-theorem recurrence, chunks of 50)
+# FP64 floating-point work of the sample kernel (addition-theorem recurrence, chunks of 64)
 # per geodesic point on this workload, from the ncu capture summarised in
 # profiles/geo_samples_fp64_config2.md: (dadd + dmul + 2 dfma thread instructions) / points.
 # Used for roofline.achieved. FP64_INST_PER_POINT: FP64 pipe instructions (dadd + dmul +

@@ -117,8 +117,10 @@ struct CrossingArgs {
 };
 
 // Default and largest samples per thread of the stepped kernel (longer recurrence chains
-// accumulate more rounding: 64 keeps every output within the FP64 parity bars).
-constexpr int DEFAULT_CHUNK = 50;
+// accumulate more rounding: 64 keeps every output within the FP64 parity bars, max error over
+// bar 0.62 on 12 seeded 48x48x400 draws; the chunk-start direct evaluation is amortised over
+// the whole chunk).
+constexpr int DEFAULT_CHUNK = 64;
 constexpr int MAX_CHUNK = 64;
 // The mixed recurrence accumulates FP32 increments into FP64 sums, so its chains may be
 // longer: the chunk-start evaluation is amortised over more samples.
