@@ -42,10 +42,10 @@ CPU_SAMPLE_RAYS = 16384      # rays of the bounded CPU sample (every 16th pixel 
 # profiles/geo_samples_fp64_config2.md: (dadd + dmul + 2 dfma thread instructions) / points.
 # Used for roofline.achieved. FP64_INST_PER_POINT: FP64 pipe instructions (dadd + dmul +
 # dfma) per point, against the pipe's rate (fp64_peak / 2 instructions per second).
-FP64_FLOP_PER_POINT = 760
-FP64_INST_PER_POINT = 488
+FP64_FLOP_PER_POINT = 748
+FP64_INST_PER_POINT = 480
 # DRAM bytes per point of the same capture (dram__bytes_read + dram__bytes_write) / points
-DRAM_BYTES_PER_POINT = 54.2
+DRAM_BYTES_PER_POINT = 53.6
 BYTES_PER_POINT = 48          # t, r, theta, phi, sigma, Mino tau written per point (8 B each)
 L2_FLUSH_BYTES = 256 << 20
 
