@@ -1001,6 +1001,24 @@ def emissivity(a, r, emistype, kw):
 # ----------------------------------------------------------------------------
 
 
+BZ_TABLE_N = 100000   # nodes of the reference's f(r) table generator (kgeo/bfields.py:16-20)
+
+
+def bz_f_table(r):
+    """f(r), f'(r) as the reference evaluates them: the linear interpolant of f on
+    linspace(1, 100, 100000) (UnivariateSpline(k=1, s=0)) and its piecewise-constant slope
+    (kgeo/bfields.py:23-31), with 1/(4r), -1/(4r^2) beyond r = 100. The node values here are the
+    closed form of bz_f."""
+    r = np.asarray(r, dtype=float)
+    nodes = np.linspace(1, 100, BZ_TABLE_N)
+    fn = bz_f(nodes)[0]
+    f = np.interp(r, nodes, fn)
+    k = np.clip(np.floor((r - 1.) / (nodes[1] - nodes[0])).astype(np.int64), 0, BZ_TABLE_N - 2)
+    fp = (fn[k + 1] - fn[k]) / (nodes[k + 1] - nodes[k])
+    big = r > 100.
+    return np.where(big, 1. / (4. * r), f), np.where(big, -1. / (4. * r * r), fp)
+
+
 def bz_f(r):
     """BZ monopole radial function f(r) (kgeo/bfields.py:7-13) and its derivative, in closed
     form: Re Li2(2/r) through scipy.special.spence (spence(z) = Li2(1 - z)). The reference
@@ -1071,7 +1089,7 @@ def bfield_lab(a, r, fieldtype, kw, th=np.pi / 2):
         Br = C / r2
         return Br, 0 * Br, (-1 * (OmegaH - OmegaBZ) * np.sqrt(Pi) / Delta) * Br
     if fieldtype == 'bz_monopole':
-        fr, frp = bz_f(r)
+        fr, frp = bz_f_table(r) if kw.get('table', False) else bz_f(r)
         f2 = (6 * np.pi * np.pi - 49.) / 72.
         omega2 = 1. / 32. - sth2 * (4 * f2 - 1) / 64.
         if kw.get('secondorder_only', False):
@@ -1125,7 +1143,7 @@ def bfield_lab(a, r, fieldtype, kw, th=np.pi / 2):
     raise ValueError(fieldtype)
 
 
-def pol_quantities(a, r, lam, eta, kr_sign, kth_sign, u, B, th=np.pi / 2):
+def pol_quantities(a, r, lam, eta, kr_sign, kth_sign, u, B, th=np.pi / 2, full=False):
     """(sinthb, kappa, cos2chi-free pieces) of calc_polquantities for a lab-frame field
     (kgeo/equatorial_images.py:336-487) with the tetrads of Velocity.tetrades
     (kgeo/velocities.py:124-176). u = (u0, u1, u2, u3), B = (B1, B2, B3). Returns
@@ -1172,6 +1190,14 @@ def pol_quantities(a, r, lam, eta, kr_sign, kth_sign, u, B, th=np.pi / 2):
     Bp_y = e0_y * b0_l + e1_y * b1_l + e2_y * b2_l + e3_y * b3_l
     Bp_z = e0_z * b0_l + e1_z * b1_l + e2_z * b2_l + e3_z * b3_l
     Bp_mag = np.sqrt(Bp_x ** 2 + Bp_y ** 2 + Bp_z ** 2)
+    # normal to the field surface in the comoving frame (kgeo/equatorial_images.py:390-393, 416-419)
+    gdet = Sigma * np.sqrt(sth2)
+    norm1_l = -B2 * gdet
+    norm2_l = B1 * gdet
+    norm_x = e1_x * norm1_l + e2_x * norm2_l
+    norm_y = e1_y * norm1_l + e2_y * norm2_l
+    norm_z = e1_z * norm1_l + e2_z * norm2_l
+    norm_mag = np.sqrt(norm_x ** 2 + norm_y ** 2 + norm_z ** 2)
     # photon wavevector (kgeo/equatorial_images.py:442-462)
     R = (r2 + a2 - a * lam) ** 2 - Delta * (eta + (lam - a) ** 2)
     TH = eta + a2 * cth2 - lam * lam * cth2 / sth2
@@ -1199,6 +1225,10 @@ def pol_quantities(a, r, lam, eta, kr_sign, kth_sign, u, B, th=np.pi / 2):
     A = k0 * f1 - k1 * f0 + a * sth2 * (k1 * f3 - k3 * f1)
     Bk = ((r2 + a2) * (k3 * f2 - k2 * f3) - a * (k0 * f2 - k2 * f0)) * np.sin(th)
     kappa = (r - 1j * a * np.cos(th)) * (A - 1j * Bk)
+    if full:
+        kdotnorm = kp_x * (norm_x / norm_mag) + kp_y * (norm_y / norm_mag) + kp_z * (norm_z / norm_mag)
+        pathlength = np.abs(kp_mag / kdotnorm)
+        return sinthb, kappa, pathlength, Bp_mag ** 2
     return sinthb, kappa
 
 
@@ -1533,6 +1563,181 @@ def findroot(geo, psitarget, alpha, beta, r_o, th_o, a, ngeo, model='para', neqm
     if converged:
         return root, r_s, th_s, signpr, signpth, neq, shape, conv
     return root, r_s, th_s, signpr, signpth, neq, shape
+
+
+# ----------------------------------------------------------------------------
+# off-equatorial jet emission (the monopole field-line model of getstokes)
+# ----------------------------------------------------------------------------
+
+
+def omega_field(a, r, th, fieldtype, kw):
+    """Field-line angular speed Omega_F (kgeo/bfields.py:175-196) of the models the
+    monopole jet uses: 'bz_monopole' (:590-593) and 'power' (:609-615)."""
+    sth2 = np.sin(th) ** 2
+    if fieldtype == 'bz_monopole':
+        f2 = (6 * np.pi * np.pi - 49.) / 72.
+        omega2 = 1. / 32. - sth2 * (4 * f2 - 1) / 64.
+        om = np.abs(a) / 8. + np.abs(a) ** 3 * omega2
+        return -om if a < 0 else om
+    if fieldtype == 'power':
+        p = kw.get('p', 1)
+        if kw.get('usemono', False) or p == 0:
+            return a / 8 + 0 * r
+        rp = 1 + np.sqrt(1 - a ** 2)
+        psi = r ** p * (1 - np.abs(np.cos(th)))
+        return a / (4 + 8 / (1 + (1 - psi * rp ** (-p))))
+    raise ValueError(fieldtype)
+
+
+def u_driftframe(a, r, th, fieldtype, kw, nu_parallel=0):
+    """Drift-frame four-velocity of the force-free field (kgeo/velocities.py:487-623) for a
+    numeric parallel boost and no Lorentz-factor cap."""
+    nu = nu_parallel * np.ones_like(r)
+    if np.any(np.logical_or(nu > 1, nu < -1)):
+        raise Exception("nu_parallel should be in the range (-1,1)")
+    a2 = a ** 2
+    r2 = r ** 2
+    cth2 = np.cos(th) ** 2
+    sth2 = np.sin(th) ** 2
+    Delta = r2 - 2 * r + a2
+    Sigma = r2 + a2 * cth2
+    Xi = (r2 + a2) ** 2 - Delta * a2 * sth2
+    omegaz = 2 * a * r / Xi
+    gdet = Sigma * np.sin(th)
+    g11 = Sigma / Delta
+    g22 = Sigma
+    g33 = Xi * sth2 / Sigma
+    alpha = np.sqrt(Delta * Sigma / Xi)
+    eta3 = 2 * a * r / np.sqrt(Delta * Sigma * Xi)
+    omegaf = omega_field(a, r, th, fieldtype, kw)
+    B1, B2, B3 = bfield_lab(a, r, fieldtype, kw, th=th)
+    E1 = (omegaf - omegaz) * Xi * np.sin(th) * B2 / Sigma
+    E2 = -(omegaf - omegaz) * Xi * np.sin(th) * B1 / (Sigma * Delta)
+    E3 = 0
+    Bsq = g11 * B1 * B1 + g22 * B2 * B2 + g33 * B3 * B3
+    Esq = g11 * E1 * E1 + g22 * E2 * E2 + g33 * E3 * E3
+    B1c, B2c, B3c = g11 * B1, g22 * B2, g33 * B3
+    E1c, E2c, E3c = g11 * E1, g22 * E2, g33 * E3
+    vperp1 = (alpha / (Bsq * gdet)) * (E2c * B3c - B2c * E3c)
+    vperp2 = (alpha / (Bsq * gdet)) * (E3c * B1c - B3c * E1c)
+    vperp3 = (alpha / (Bsq * gdet)) * (E1c * B2c - B1c * E2c)
+    vpar_max = np.sqrt(1 - Esq / Bsq)
+    v1 = vperp1 + nu * vpar_max * B1 / np.sqrt(Bsq)
+    v2 = vperp2 + nu * vpar_max * B2 / np.sqrt(Bsq)
+    v3 = vperp3 + nu * vpar_max * B3 / np.sqrt(Bsq)
+    vsq = g11 * v1 * v1 + g22 * v2 * v2 + g33 * v3 * v3
+    gamma = 1. / np.sqrt(1 - vsq)
+    return gamma / alpha, gamma * (v1 + 0), gamma * (v2 + 0), gamma * (v3 + eta3)
+
+
+def r0min_mono(theta, Omegaf, spin, M=1.0):
+    """Stagnation radius of the monopole outflow: a root of the quintic of
+    kgeo/ff_boost.py:7-18 (numpy's sorted roots, index 4)."""
+    theta = np.arccos(np.abs(np.cos(theta)))
+    c0 = -spin ** 2 / 2 * M * np.cos(theta) ** 2 * (2 - spin * Omegaf + spin * Omegaf * np.cos(2 * theta)) ** 2
+    c1 = -2 * spin ** 4 * Omegaf ** 2 * np.cos(theta) ** 4 * np.sin(theta) ** 2
+    c2 = M / 2 * (2 - spin * Omegaf + spin * Omegaf * np.cos(2 * theta)) ** 2
+    c3 = -spin ** 2 * Omegaf ** 2 * np.sin(2 * theta) ** 2
+    c5 = -2 * Omegaf ** 2 * np.sin(theta) ** 2
+    roots = np.polynomial.polynomial.Polynomial([c0, c1, c2, c3, 0.0, c5]).roots()
+    return np.real(roots[4])
+
+
+def eta_mono(r, theta, r0, spin, sigma):
+    """Mass loading of the monopole outflow, a Gaussian source of width sigma about the
+    stagnation radius integrated in closed form; kgeo/densityfuncs.py:32-44."""
+    if sigma == 0:
+        return np.sign(r - r0)
+    cth = np.cos(theta)
+    t1 = 2 * sigma * (2 * r0 - (r + r0) * np.exp(-(r - r0) ** 2 / (2 * sigma ** 2)))
+    t2 = np.sqrt(2 * np.pi) * sp.erf((r - r0) / (np.sqrt(2) * sigma)) * (r0 ** 2 + sigma ** 2 + spin ** 2 * cth ** 2)
+    den = 4 * r0 * sigma + np.sqrt(2 * np.pi) * sigma ** 2 + np.sqrt(2 * np.pi) * (r0 ** 2 + spin ** 2 * cth ** 2)
+    return (t1 + t2) / den
+
+
+def jet_stagnation(rvals, thvals, shape, spin):
+    """(r0, Omega) of density_mono_all (kgeo/densityfuncs.py:47-60): the first crossing of the
+    first guess row fixes the field line's Omega and stagnation radius."""
+    rnew = np.reshape(rvals, shape)
+    thnew = np.arccos(np.abs(np.cos(np.reshape(thvals, shape))))
+    i0 = np.where(rnew[0] != 0)[0][0]
+    om = omega_field(spin, rnew[0][i0], thnew[0][i0], 'bz_monopole', {})
+    return r0min_mono(thnew[0][i0], om, spin, 1.0), om
+
+
+def density_mono_all(rvals, thvals, shape, spin, nu_parallel, sigma, table=False):
+    """Continuity-equation density rho = eta B^r / u^r along the monopole field line at the
+    reflected crossings; kgeo/densityfuncs.py:47-78."""
+    r0, _ = jet_stagnation(rvals, thvals, shape, spin)
+    rr = np.reshape(rvals, shape)
+    tt = np.arccos(np.abs(np.cos(np.reshape(thvals, shape))))
+    out = []
+    for k in range(shape[0]):
+        B1 = bfield_lab(spin, rr[k], 'bz_monopole', {'C': 1, 'table': table}, th=tt[k])[0]
+        u1 = u_driftframe(spin, rr[k], tt[k], 'bz_monopole', {'C': 1, 'table': table}, nu_parallel)[1]
+        out.append(eta_mono(rr[k], tt[k], r0, spin, sigma) * B1 / u1)
+    return np.nan_to_num(np.array(out).flatten(), nan=0.0)
+
+
+def iobs_off(a, r_o, r_s, th_o, alpha, beta, kr, kth, field, nu_parallel, th_s, density, specind=1):
+    """(I, Q, U) of the off-equatorial crossings (kgeo/off_eq.py:15-119) for the constant
+    emissivity with a density, the drift-frame velocity and polarisation."""
+    lam = -alpha * np.sin(th_o)
+    eta = (alpha ** 2 - a ** 2) * np.cos(th_o) ** 2 + beta ** 2
+    rh = 1 + np.sqrt(1 - a ** 2)
+    u = u_driftframe(a, r_s, th_s, field[0], field[1], nu_parallel)
+    gg = redshift(a, r_s, lam, eta, kr, kth, *u, th=th_s)
+    B = bfield_lab(a, r_s, field[0], field[1], th=th_s)
+    sinthb, kappa, plen, bsq = pol_quantities(a, r_s, lam, eta, kr, kth, u, B, th=th_s, full=True)
+    c2, s2 = evpa(a, th_o, alpha, beta, kappa)
+    Iemis = np.ones(r_s.shape) * density
+    Iemis = Iemis * bsq ** ((1 + specind) / 2)
+    I = (gg ** 3) * (gg ** specind) * plen * Iemis * (sinthb ** (1 + specind))
+    Q = c2 * I
+    U = s2 * I
+    I[r_s <= rh] = Q[r_s <= rh] = U[r_s <= rh] = 0
+    return I, Q, U
+
+
+def sort_image(iobs, qobs, uobs, neqvals, shape, ashape, neqmax):
+    """Per-subring and total images (kgeo/geometry.py:38-61)."""
+    outs = ([], [], [])
+    for neq in np.arange(0, neqmax, 1):
+        for o, v in zip(outs, (iobs, qobs, uobs)):
+            h = np.copy(v)
+            h[neqvals != neq] = 0
+            o.append(np.reshape(np.sum(np.reshape(h, shape), axis=0), ashape))
+    for o, v in zip(outs, (iobs, qobs, uobs)):
+        o.append(np.reshape(np.sum(np.reshape(v, shape), axis=0), ashape))
+    return tuple(np.array(o) for o in outs)
+
+
+def getstokes_mono(psitarget, alphavals, betavals, r_o, th_o, a, ngeo, neqmax=1, model='mono', pval=0,
+                   nu_parallel=0, sigma=2, tol=1e-8, table=False):
+    """getstokes (kgeo/off_eq.py:124-233) of the monopole field-line model ('mono', or 'power'
+    with p = 0): crossings, densities, the emission of each crossing, the per-subring sums.
+    Returns (I, Q, U, evpa) of shape (neqmax + 1, ...) and the crossings (r, th). table=True
+    evaluates the BZ f(r) as the reference does (bz_f_table) instead of in closed form."""
+    ashape = alphavals.shape
+    A = alphavals.flatten()
+    B = betavals.flatten()
+    geo = raytrace(a, r_o, th_o, A, B, ngeo)
+    tau, rv, tv, spr, spt, neq, shape = findroot(geo, psitarget, A, B, r_o, th_o, a, ngeo, model=model,
+                                                 neqmax=neqmax, tol=tol, pval=pval)
+    At = np.tile(A, shape[0])
+    Bt = np.tile(B, shape[0])
+    dv = density_mono_all(rv, tv, shape, a, nu_parallel, sigma, table=table)
+    field = ('bz_monopole', {'C': 1, 'table': table}) if model == 'mono' else ('power', {'p': pval})
+    with np.errstate(all='ignore'):
+        I, Q, U = iobs_off(a, r_o, rv, th_o, At, Bt, spr, spt, field, nu_parallel, tv, dv)
+    I = np.copy(I)
+    Q = np.copy(Q)
+    U = np.copy(U)
+    I[rv == 0] = Q[rv == 0] = U[rv == 0] = 0
+    I, Q, U = (np.real(np.nan_to_num(np.array(x))) for x in (I, Q, U))
+    iv, qv, uv = sort_image(I, Q, U, neq, shape, ashape, neqmax)
+    ev = np.nan_to_num(0.5 * np.arctan2(uv, qv))
+    return iv, qv, uv, ev, np.nan_to_num(rv), np.nan_to_num(tv)
 
 
 # ----------------------------------------------------------------------------

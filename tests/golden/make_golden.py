@@ -368,6 +368,25 @@ def main(path):
         jout['shape%d' % i] = np.array(res[6])
     save('jet_crossings', jout)
 
+    # off-equatorial jet images of the monopole field-line model (off_eq.getstokes); the
+    # paraboloid and p > 0 power models of getstokes fail inside the reference with this
+    # numpy / scipy (an array reaches scipy.integrate.quad's bounds), so they have no fixture
+    import kgeo.off_eq as off_eq
+    scases = [('mono', 0.4, 0.5, 60., 1, 0.0, 1, 2.0), ('mono', 0.3, 0.9, 17., 1, 0.3, 2, 2.0),
+              ('power', 0.5, 0.7, 30., 0.0, -0.2, 1, 1.5), ('mono', 0.35, 0.7, 150., 1, 0.5, 2, 0.0)]
+    sout = dict(ncase=len(scases))
+    for i, (model, psit, a, inc, pval, nu, neqmax, sigma) in enumerate(scases):
+        x = np.linspace(-8, 8, 16)
+        A, B = np.meshgrid(x, x)
+        with warnings.catch_warnings():
+            warnings.simplefilter('ignore')
+            res = quiet(off_eq.getstokes, psit, A, B, 1.e4, inc * deg, a, 200, model=model, pval=pval, neqmax=neqmax,
+                        retvals=True, nu_parallel=nu, sigma=sigma)
+        sout['case%d' % i] = repr((model, psit, a, inc, pval, nu, neqmax, sigma))
+        for k, v in zip(['I', 'Q', 'U', 'evpa', 'r', 'th'], res):
+            sout['%s%d' % (k, i)] = np.asarray(v)
+    save('jet_stokes', sout)
+
     # EVPA of ipole images (the reference's tests/data/*.csv, from tests/test_images.py):
     # pixel location and EVPA along the middle row / column for image orders 0 and 1
     ip = {}

@@ -1,0 +1,62 @@
+"""The oracle's getstokes of the monopole field-line model against the reference's own outputs
+(tests/golden/jet_stokes.npz, made by tests/golden/make_golden.py from kgeo/off_eq.py:124-233).
+
+Bars: I, Q, U within 1e-10 of the image maximum; the EVPA within 1e-7 rad (mod pi) where the
+polarised flux is above 1e-6 of the maximum (the angle of a vanishing Q + iU is undefined);
+the crossing radii and angles within 1e-12.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+from oracle import kgeo_oracle as ko  # noqa: E402
+
+GOLD = np.load(os.path.join(HERE, 'golden', 'jet_stokes.npz'), allow_pickle=False)
+CASES = range(int(GOLD['ncase']))
+DEG = np.pi / 180
+
+
+def stokes_bars(I, Q, U, ev, ref):
+    Ir, Qr, Ur, er = ref
+    scale = np.max(np.abs(Ir))
+    assert scale > 0
+    for x, y in ((I, Ir), (Q, Qr), (U, Ur)):
+        assert np.max(np.abs(x - y)) <= 1e-10 * scale
+    pol = np.hypot(Qr, Ur) > 1e-6 * scale
+    d = np.abs(((ev - er) + np.pi / 2) % np.pi - np.pi / 2)
+    assert np.max(d[pol], initial=0.0) <= 1e-7
+
+
+@pytest.mark.parametrize('i', CASES)
+def test_oracle_getstokes_vs_reference(i):
+    model, psit, a, inc, pval, nu, neqmax, sigma = eval(str(GOLD['case%d' % i]))
+    x = np.linspace(-8, 8, 16)
+    A, B = np.meshgrid(x, x)
+    with np.errstate(all='ignore'):
+        I, Q, U, ev, r, th = ko.getstokes_mono(psit, A, B, 1.e4, inc * DEG, a, 200, neqmax=neqmax, model=model,
+                                               pval=pval, nu_parallel=nu, sigma=sigma, table=True)
+    g = lambda k: GOLD['%s%d' % (k, i)]  # noqa: E731
+    assert I.shape == g('I').shape
+    stokes_bars(I, Q, U, ev, (g('I'), g('Q'), g('U'), g('evpa')))
+    assert np.max(np.abs(r - g('r'))) <= 1e-12
+    assert np.max(np.abs(th - g('th'))) <= 1e-12
+
+
+def test_stagnation_radius_is_largest_real_root():
+    """r0min_mono keeps numpy's sorted root 4 of the quintic (kgeo/ff_boost.py:7-18): the
+    largest real part, which the CUDA path finds by Aberth iteration."""
+    for th, a in ((0.3, 0.5), (1.1, 0.9), (0.05, 0.2)):
+        om = ko.omega_field(a, 10., th, 'bz_monopole', {})
+        r0 = ko.r0min_mono(th, om, a)
+        c = np.cos(th)
+        s = np.sin(th)
+        k = 2 - a * om + a * om * np.cos(2 * th)
+        coef = [-a ** 2 / 2 * c ** 2 * k ** 2, -2 * a ** 4 * om ** 2 * c ** 4 * s ** 2, k ** 2 / 2,
+                -a ** 2 * om ** 2 * np.sin(2 * th) ** 2, 0.0, -2 * om ** 2 * s ** 2]
+        roots = np.roots(coef[::-1])
+        assert abs(r0 - np.max(roots.real)) <= 1e-9 * abs(r0)
