@@ -1023,6 +1023,123 @@ def run_jet(args):
 
 
 # ---------------------------------------------------------------------------
+# jet Stokes images (kgeo.off_eq.getstokes, the BZ monopole field line)
+# ---------------------------------------------------------------------------
+
+STOKES_GRID = 256
+STOKES_CASE = dict(a=0.5, inc=60.0, model='mono', psitarget=0.4, ngeo=200, neqmax=1, nu_parallel=0.0, sigma=2.0)
+CPU_STOKES_SAMPLE = 2048
+# FP64 work of jet_stokes_kernel per crossing row and pixel on the stokes-small capture
+# (profiles/jet_stokes.md); None until captured
+STOKES_FLOP_PER_CROSSING = None
+STOKES_FP64_INST_PER_CROSSING = None
+
+
+def _cpu_stokes_chunk(args):
+    A, B = args
+    from oracle import kgeo_oracle as ko
+    import warnings
+    warnings.filterwarnings('ignore')
+    c = STOKES_CASE
+    with np.errstate(all='ignore'):
+        ko.getstokes_mono(c['psitarget'], A, B, R_O, c['inc'] * np.pi / 180, c['a'], c['ngeo'], neqmax=c['neqmax'],
+                          model=c['model'], nu_parallel=c['nu_parallel'], sigma=c['sigma'], table=True)
+    return len(A)
+
+
+def run_stokes(args):
+    small = args.case == 'stokes-small'
+    pool = cores = None
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()
+    import torch
+    from kgeo_gb300 import device as dev
+    from kgeo_gb300 import off_eq, solver
+    c = STOKES_CASE
+    n = 64 if small else STOKES_GRID
+    x = np.linspace(-10, 10, n)
+    A2, B2 = np.meshgrid(x, x)
+    A, B = A2.flatten(), B2.flatten()
+    th = c['inc'] * np.pi / 180
+    al, be = dev.as_device(A), dev.as_device(B)
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def pipeline():
+        geo = dev.trace(c['a'], R_O, th, al, be, ngeo=c['ngeo'], outputs=('r', 'th', 'mino'), per_ray=())
+        cr, shape = solver.crossings_device(c['a'], R_O, th, al, be, geo['r'], geo['th'], geo['mino'],
+                                            c['psitarget'], model=c['model'], neqmax=c['neqmax'])
+        return cr, off_eq.stokes_device(c['a'], R_O, th, al, be, cr, neqmax=c['neqmax'], model=c['model'],
+                                        nu_parallel=c['nu_parallel'], sigma=c['sigma'])
+    for _ in range(args.warmup):
+        cr, st = pipeline()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(args.steps):
+        cr, st = pipeline()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    t_step = e0.elapsed_time(e1) / 1e3 / args.steps
+    G = cr['r'].shape[0]
+    # the emission kernel alone, on the step's crossings
+    e2, e3 = ev(), ev()
+    e2.record(stream)
+    for _ in range(args.steps):
+        off_eq.stokes_device(c['a'], R_O, th, al, be, cr, neqmax=c['neqmax'], model=c['model'],
+                             nu_parallel=c['nu_parallel'], sigma=c['sigma'])
+    e3.record(stream)
+    torch.cuda.synchronize()
+    t_kern = e2.elapsed_time(e3) / 1e3 / args.steps
+    ncross = int((cr['r'] != 0).sum())
+    # end to end: numpy pixels in -> getstokes -> numpy images out
+    kw = dict(model=c['model'], neqmax=c['neqmax'], nu_parallel=c['nu_parallel'], sigma=c['sigma'])
+    off_eq.getstokes(c['psitarget'], A2, B2, R_O, th, c['a'], c['ngeo'], **kw)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        off_eq.getstokes(c['psitarget'], A2, B2, R_O, th, c['a'], c['ngeo'], **kw)
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    cpu = None
+    if pool is not None:
+        idx = np.arange(0, A.size, max(1, A.size // CPU_STOKES_SAMPLE))[:CPU_STOKES_SAMPLE]
+        chunks = np.array_split(idx, cores * 2)
+        t0 = time.time()
+        pool.map(_cpu_stokes_chunk, [(A[k], B[k]) for k in chunks])
+        dt = time.time() - t0
+        cpu = {'value': idx.size / dt, 'unit': 'pixels/s (getstokes)', 'cores': cores, 'kind': 'port',
+               'sample': '%d pixels (every %dth of the %dx%d grid): oracle getstokes (raytrace, findroot, emission) '
+                         'on a %d-process pool, %.1f s wall' % (idx.size, A.size // idx.size, n, n, cores, dt)}
+        pool.close()
+    if STOKES_FLOP_PER_CROSSING:
+        roof = roofline_fp64('jet_stokes_kernel', t_kern, G * A.size, STOKES_FLOP_PER_CROSSING,
+                             STOKES_FP64_INST_PER_CROSSING, 'crossing_row')
+    else:
+        roof = {'kernel': 'jet_stokes_kernel', 'launch_ms': t_kern * 1e3, 'bound': 'fp64', 'achieved': None,
+                'frac': None, 'traffic': None, 'note': 'FP64 work per crossing not captured'}
+    line = {
+        'metric': 'pixels/s: jet Stokes images (getstokes: trace, field-line crossings, emission, subring sums)',
+        'value': A.size / t_step, 'unit': 'pixels/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': t_step * 1e3, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f64', 'data': 'synthetic: uniform image-plane grid over [-10, 10] M',
+        'config': {'workload': 'a=0.5, theta_o=60 deg, r_o=1e4, %dx%d, ngeo=200, BZ monopole psi=0.4, neqmax=1, '
+                               'nu_parallel=0, sigma=2' % (n, n),
+                   'guess_rows': G, 'crossings': ncross, 'case': args.case,
+                   'stokes_kernel_ms': t_kern * 1e3, 'l2': 'per-step buffers 24 B x ngeo x pixels'},
+        'roofline': roof,
+        'cpu_baseline': cpu,
+        'e2e': {'value': A.size / t_e2e, 'unit': 'pixels/s (getstokes)', 'h2d_bytes_per_step': 16 * A.size,
+                'd2h_bytes_per_step': 32 * (c['neqmax'] + 1) * A.size, 'ms_per_step': t_e2e * 1e3,
+                'path': 'kgeo_gb300.off_eq.getstokes (numpy in/out)'},
+        'gpu_launches': args.steps * 7, 'clocks': ck,
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
 # configuration 4: batched images (64 images, one persistent launch, CUDA graph)
 # ---------------------------------------------------------------------------
 
@@ -1185,7 +1302,7 @@ def main():
     p.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     p.add_argument('--case', choices=('full', 'small', 'mixed', 'mixed-small', 'image', 'image-small', 'batch',
                                       'batch-small', 'polimage', 'polimage-small', 'library', 'library-small', 'jet',
-                                      'jet-small'),
+                                      'jet-small', 'stokes', 'stokes-small'),
                    default='full')
     p.add_argument('--no-cpu-baseline', action='store_true')
     args = p.parse_args()
@@ -1201,6 +1318,8 @@ def main():
         run_library(args)
     elif args.case.startswith('jet'):
         run_jet(args)
+    elif args.case.startswith('stokes'):
+        run_stokes(args)
     elif args.case.startswith('batch'):
         run_batch(args)
     else:

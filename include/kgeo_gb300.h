@@ -344,6 +344,36 @@ int kgeo_jet_findroot(const kgeo_observer* obs, const double* alpha, const doubl
                       void* workspace, size_t workspace_bytes, double* tau, double* r, double* th, double* signpr,
                       double* signpth, double* neq, int32_t* status, void* stream);
 
+/* getstokes (kgeo/off_eq.py:124-233) after findroot, for the monopole field-line model:
+ * the Stokes I, Q, U of every crossing (Iobs_off, :15-119: constant emissivity times the
+ * continuity-equation density of kgeo/densityfuncs.py:47-78, the force-free drift-frame
+ * velocity of kgeo/velocities.py:487-623 with a numeric parallel boost, the polarisation of
+ * calc_polquantities with its path length and comoving b^2), summed over the guess rows into
+ * the images of neq = 0 .. neqmax - 1 and their total (sort_image, kgeo/geometry.py:38-61), and
+ * the EVPA 0.5 atan2(U, Q) of each. The density's stagnation radius comes from the first
+ * crossing of the first guess row (kgeo/densityfuncs.py:47-60, kgeo/ff_boost.py:7-18).
+ * r, th, signpr, signpth, neq: (nguess, npix) device arrays, kgeo_jet_findroot's outputs.
+ * I, Q, U, evpa: (neqmax + 1, npix) device outputs (evpa may be NULL); I_c, Q_c, U_c (may be
+ * NULL): (nguess, npix) per crossing; stagnation (may be NULL): device (2) r0, Omega_F;
+ * status (may be NULL): device (1), 0 ok, 1 no crossing in the first row, 2 or 3 no stagnation
+ * root (a = 0 or a crossing on the axis; the reference fails on both), with all images 0.
+ * The BZ f(r) is the linear interpolant of its values on linspace(1, 100, 100000) as the
+ * reference evaluates it (kgeo/bfields.py:16-31); the first call on a device builds that table
+ * (one synchronous kernel). */
+typedef struct {
+  int32_t model;       /* KGEO_JET_MONO, or KGEO_JET_POWER with pval == 0 */
+  int32_t neqmax;      /* >= 1 */
+  double pval;
+  double nu_parallel;  /* in [-1, 1] */
+  double sigma;        /* width of the mass-loading Gaussian (0: a step at r0) */
+  double specind;      /* spectral index */
+} kgeo_jet_emission;
+int kgeo_jet_stokes(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                    const double* r, const double* th, const double* signpr, const double* signpth,
+                    const double* neq, int32_t nguess, const kgeo_jet_emission* emission, double* I, double* Q,
+                    double* U, double* evpa, double* I_c, double* Q_c, double* U_c, double* stagnation,
+                    int32_t* status, void* stream);
+
 /* Batched tracing: many images of different size, spin, inclination and ngeo traced as one
  * job (no counterpart in the reference, whose raytrace_ana takes one image per call:
  * kgeo/kerr_raytracing_ana.py:46). A plan describes the images; kgeo_batch_bind attaches the
@@ -359,7 +389,8 @@ int kgeo_jet_findroot(const kgeo_observer* obs, const double* alpha, const doubl
  * kgeo_batch_autotune times the sample kernel's launch shapes (block size, CTAs per SM, tile
  * length, samples per work item) on a subset of the bound batch's tiles within about budget_ms
  * and keeps the fastest; results are cached per device, precision and image sizes (the cache
- * is the library's only global state, mutex-guarded), so a new plan for the same batch shape
+ * and the BZ f(r) tables of kgeo_jet_stokes are the library's only global state, both
+ * mutex-guarded), so a new plan for the same batch shape
  * starts tuned. kgeo_batch_graph_launch captures the whole run into a CUDA graph on first use
  * (and again after a bind or a configuration change) and replays it on `stream`. */
 #define KGEO_BATCH_MAX_IMAGES 4096

@@ -61,6 +61,12 @@ class JetField(ctypes.Structure):
     _fields_ = [('model', c_int32), ('reserved', c_int32), ('psitarget', c_double), ('pval', c_double)]
 
 
+class JetEmission(ctypes.Structure):
+    """kgeo_jet_emission."""
+    _fields_ = [('model', c_int32), ('neqmax', c_int32), ('pval', c_double), ('nu_parallel', c_double),
+                ('sigma', c_double), ('specind', c_double)]
+
+
 class BatchImage(ctypes.Structure):
     """kgeo_batch_image."""
     _fields_ = [('a', c_double), ('r_o', c_double), ('th_o', c_double), ('npix', c_int64), ('ngeo', c_int32),
@@ -115,6 +121,9 @@ SIGNATURES = {
     'kgeo_jet_findroot': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_void_p, c_int32,
                                   ctypes.POINTER(JetField), c_double, c_int32, c_void_p, c_size_t, c_void_p, c_void_p,
                                   c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    'kgeo_jet_stokes': (c_int, [ctypes.POINTER(Observer), c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p,
+                                c_void_p, c_void_p, c_int32, ctypes.POINTER(JetEmission), c_void_p, c_void_p, c_void_p,
+                                c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     'kgeo_rho_of_req': (c_int, [ctypes.POINTER(Curve), c_int32, c_void_p, c_int32, c_double, c_double, c_int32,
                                 c_void_p, c_void_p, c_void_p]),
     'kgeo_critical_curve': (c_int, [c_double, c_double, c_int64, c_void_p, c_void_p, c_void_p]),

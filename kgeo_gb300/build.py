@@ -31,6 +31,7 @@ UNITS = [
     ('kg_batch.cu', []),
     ('kg_curves.cu', ['-fmad=false']),
     ('kg_jet.cu', ['-fmad=false']),
+    ('kg_jetimg.cu', ['-fmad=false']),
 ]
 
 

@@ -543,6 +543,59 @@ int kgeo_jet_findroot(const kgeo_observer* obs, const double* alpha, const doubl
   return launch_jet_solve(ja, s) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
 }
 
+int kgeo_jet_stokes(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
+                    const double* r, const double* th, const double* signpr, const double* signpth,
+                    const double* neq, int32_t nguess, const kgeo_jet_emission* em, double* I, double* Q,
+                    double* U, double* evpa, double* I_c, double* Q_c, double* U_c, double* stagnation,
+                    int32_t* status, void* stream) {
+  int st = check_observer(obs);
+  if (st) return st;
+  if (npix < 0) return KGEO_ERR_LENGTHS;
+  if (nguess < 0) return KGEO_ERR_NGEO;
+  if (!em) return KGEO_ERR_NULL;
+  if (!(em->model == KGEO_JET_MONO || (em->model == KGEO_JET_POWER && em->pval == 0.0))) return KGEO_ERR_MODEL;
+  if (em->neqmax < 1 || !(em->nu_parallel >= -1.0 && em->nu_parallel <= 1.0) || !(em->sigma >= 0.0) ||
+      !std::isfinite(em->specind))
+    return KGEO_ERR_MODEL;
+  if (!I || !Q || !U) return KGEO_ERR_NULL;
+  if (npix > 0 && (!alpha || !beta)) return KGEO_ERR_NULL;
+  if (npix > 0 && nguess > 0 && (!r || !th || !signpr || !signpth || !neq)) return KGEO_ERR_NULL;
+  JetStokesArgs ja;
+  if (jet_bz_table(&ja.tab) != cudaSuccess) return KGEO_ERR_CUDA;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  double* par = nullptr;
+  if (cudaMallocAsync(&par, 4 * sizeof(double), s) != cudaSuccess) return KGEO_ERR_CUDA;
+  ja.obs = make_observer(obs);
+  ja.p.field = em->model == KGEO_JET_MONO ? JETF_MONO : JETF_POWER0;
+  ja.p.nu = em->nu_parallel;
+  ja.p.sigma = em->sigma;
+  ja.p.r0 = 0.0;
+  ja.p.specind = em->specind;
+  ja.alpha = alpha;
+  ja.beta = beta;
+  ja.npix = npix;
+  ja.r = r;
+  ja.th = th;
+  ja.signpr = signpr;
+  ja.signpth = signpth;
+  ja.neq = neq;
+  ja.nguess = nguess;
+  ja.neqmax = em->neqmax;
+  ja.par = par;
+  ja.I = I;
+  ja.Q = Q;
+  ja.U = U;
+  ja.evpa = evpa;
+  ja.Ic = I_c;
+  ja.Qc = Q_c;
+  ja.Uc = U_c;
+  ja.stagnation = stagnation;
+  ja.status = status;
+  const cudaError_t e = launch_jet_stokes(ja, s);
+  const cudaError_t f = cudaFreeAsync(par, s);
+  return (e == cudaSuccess && f == cudaSuccess) ? KGEO_OK : KGEO_ERR_CUDA;
+}
+
 int kgeo_critical_curve(double a, double th_o, int64_t n, double* alpha, double* beta, void* stream) {
   kgeo_observer o{a, INFINITY, th_o};
   int st = check_observer(&o);

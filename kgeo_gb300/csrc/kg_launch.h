@@ -7,6 +7,7 @@
 #include "kg_polar.cuh"
 #include "kg_curves.cuh"
 #include "kg_jet.cuh"
+#include "kg_jetimg.cuh"
 
 namespace kg {
 
@@ -281,6 +282,37 @@ struct JetSolveArgs {
   double* neq;
   int32_t* status;
 };
+
+// Stokes images of the off-equatorial crossings (kg_jetimg.cu).
+struct JetStokesArgs {
+  Observer obs;
+  JetImgParams p;          // r0 is found on the device from the first crossing row
+  const double* tab;       // BZ f(r) node values (BZ_TABLE_N)
+  const double* alpha;     // (npix)
+  const double* beta;
+  int64_t npix;
+  const double* r;         // (nguess, npix) crossings
+  const double* th;
+  const double* signpr;
+  const double* signpth;
+  const double* neq;
+  int64_t nguess;
+  int neqmax;
+  double* par;             // device scratch: r0, Omega, status
+  double* I;               // (neqmax + 1, npix) per-subring images, then the total
+  double* Q;
+  double* U;
+  double* evpa;
+  double* Ic;              // (nguess, npix) per crossing, or NULL
+  double* Qc;
+  double* Uc;
+  double* stagnation;      // (2) r0, Omega, or NULL
+  int32_t* status;         // (1) or NULL
+};
+
+// Device table of BZ f(r) node values, built once per device on first use (synchronously).
+cudaError_t jet_bz_table(const double** tab);
+cudaError_t launch_jet_stokes(const JetStokesArgs& a, cudaStream_t s);
 
 cudaError_t launch_jet_guesses(const JetGuessArgs& a, cudaStream_t s);
 cudaError_t launch_jet_solve(const JetSolveArgs& a, cudaStream_t s);

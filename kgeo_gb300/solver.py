@@ -143,21 +143,19 @@ def findroot_device(a, r_o, th_o, alpha, beta, guesses, psitarget, model='para',
     return out
 
 
-def findroot(outgeo, psitarget, alpha, beta, r_o, th_o, a, ngeo, model='para', neqmax=1, tol=1e-8, pval=1):
-    """(tau, r_s, th_s, sign p_r, sign p_theta, neq, guesses_shape) of every crossing of the
-    geodesics with psi = psi_target (kgeo/solver.py:136-207); arrays flattened guess-major like
-    the reference's. Warns as scipy does when some guesses did not converge and raises when
-    none did."""
+def crossings_device(a, r_o, th_o, alpha, beta, r, th, mino, psitarget, model='para', neqmax=1, tol=1e-8, pval=1):
+    """findroot's crossings on CUDA tensors: (dict of (nguess, npix) tensors tau, r, th, signpr,
+    signpth, neq, status; the guesses' shape). r, th, mino: the (ngeo, npix) samples. Warns as
+    scipy does when some guesses did not converge and raises when none did."""
     if model not in _lib.JET:
         raise NotImplementedError("jet model %r is not on the GPU path" % (model,))
     if np.abs(a) < MINSPIN:
-        lam = -np.asarray(alpha) * np.sin(th_o)
-        eta = (np.asarray(alpha) ** 2 - a ** 2) * np.cos(th_o) ** 2 + np.asarray(beta) ** 2
+        al = alpha.cpu().numpy() if isinstance(alpha, torch.Tensor) else np.asarray(alpha)
+        be = beta.cpu().numpy() if isinstance(beta, torch.Tensor) else np.asarray(beta)
+        eta = (al ** 2 - a ** 2) * np.cos(th_o) ** 2 + be ** 2
         if np.any(eta < 0):
             print("WARNING: there were eta<0 points for spin %f<MINSPIN!" % a)
-        del lam, eta
-    g = _guesses_device(a, r_o, th_o, alpha, beta, outgeo.r_s, outgeo.th_s, outgeo.mino_times, psitarget, neqmax,
-                        model, pval)
+    g = _guesses_device(a, r_o, th_o, alpha, beta, r, th, mino, psitarget, neqmax, model, pval)
     shape = tuple(g.shape)
     out = findroot_device(a, r_o, th_o, alpha, beta, g, psitarget, model=model, tol=tol, pval=pval)
     st = out['status']
@@ -166,10 +164,20 @@ def findroot(outgeo, psitarget, alpha, beta, r_o, th_o, a, ngeo, model='para', n
         msg = '%s failed to converge after %d iterations' % ('all' if bool((st != 0).all()) else 'some', 500)
         if bool((st != 0).all()):
             raise RuntimeError(msg)
-        warnings.warn(msg, RuntimeWarning, stacklevel=2)
+        warnings.warn(msg, RuntimeWarning, stacklevel=3)
+    return out, shape
+
+
+def findroot(outgeo, psitarget, alpha, beta, r_o, th_o, a, ngeo, model='para', neqmax=1, tol=1e-8, pval=1):
+    """(tau, r_s, th_s, sign p_r, sign p_theta, neq, guesses_shape) of every crossing of the
+    geodesics with psi = psi_target (kgeo/solver.py:136-207); arrays flattened guess-major like
+    the reference's. Warns as scipy does when some guesses did not converge and raises when
+    none did."""
+    out, shape = crossings_device(a, r_o, th_o, alpha, beta, outgeo.r_s, outgeo.th_s, outgeo.mino_times, psitarget,
+                                  model=model, neqmax=neqmax, tol=tol, pval=pval)
     res = _dev.to_host([out[k].reshape(-1) for k in ('tau', 'r', 'th', 'signpr', 'signpth', 'neq')])
     return tuple(res) + (shape,)
 
 
 __all__ = ['psi_BZ_para', 'psi_BZ_mono', 'psi_power', 'psifunc', 'getneq', 'get_maxtau_forwardjet', 'makegoodarray',
-           'getguesses', 'findroot', 'findroot_device', 'EP']
+           'getguesses', 'findroot', 'findroot_device', 'crossings_device', 'EP']

@@ -161,3 +161,23 @@ def image_jac(a, r_o, th_o, alpha, beta, nord, mi, md):
     L.hm_image_jac(dp(ob), ip(mi), dp(md), dp(alpha), dp(beta), ctypes.c_long(n), ctypes.c_int(nord), dp(jac),
                    dp(rsd))
     return jac, rsd
+
+
+def jet_stagnation(a, th):
+    """(status, r0, Omega_F) of the stagnation solve (host build)."""
+    L = load()
+    out = np.zeros(2)
+    st = L.hm_jet_stagnation(D(a), D(th), dp(out))
+    return st, out[0], out[1]
+
+
+def jet_stokes(a, r_o, th_o, field, nu, sigma, r0, specind, alpha, beta, r, th, kr, kth):
+    """Per crossing (I, Q, U) of the jet emission kernel (host build); field 0 monopole, 1 power p = 0."""
+    L = load()
+    ob = observer(a, r_o, th_o)
+    par = np.array([field, nu, sigma, r0, specind], float)
+    arrs = [np.ascontiguousarray(x, float) for x in (alpha, beta, r, th, kr, kth)]
+    n = len(arrs[0])
+    out = np.zeros((n, 3))
+    L.hm_jet_stokes(dp(ob), dp(par), *[dp(x) for x in arrs], ctypes.c_long(n), dp(out))
+    return out.T

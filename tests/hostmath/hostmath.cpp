@@ -5,6 +5,7 @@
 #include "../../kgeo_gb300/csrc/kg_polar.cuh"
 #include "../../kgeo_gb300/csrc/kg_curves.cuh"
 #include "../../kgeo_gb300/csrc/kg_mixed2.cuh"
+#include "../../kgeo_gb300/csrc/kg_jetimg.cuh"
 
 using namespace kg;
 
@@ -219,6 +220,30 @@ void hm_curve_rho(const double* ob, double r_eq, int mbar, double rho_min, doubl
   c.rho_min = rho_min;
   c.rho_max = rho_max;
   for (long i = 0; i < n; ++i) rho[i] = curve_rho(c, varphi[i], xtol, rtol, maxiter, status + i);
+}
+// stagnation radius r0 and Omega_F of the field line through theta; returns the status
+int hm_jet_stagnation(double a, double th, double* out) { return jet_stagnation(a, th, out, out + 1); }
+// per crossing (I, Q, U) of the jet emission; par = (field, nu, sigma, r0, specind), with the BZ
+// f(r) table built here from the closed form
+void hm_jet_stokes(const double* ob, const double* par, const double* alpha, const double* beta, const double* r,
+                   const double* th, const double* kr, const double* kth, long n, double* out) {
+  static double* tab = nullptr;
+  if (!tab) {
+    tab = new double[BZ_TABLE_N];
+    for (int64_t k = 0; k < BZ_TABLE_N; ++k) {
+      double f, fp;
+      bz_f(bz_node(k), &f, &fp);
+      tab[k] = f;
+    }
+  }
+  Observer o = make_obs(ob);
+  JetImgParams P{(int)par[0], par[1], par[2], par[3], par[4]};
+  for (long i = 0; i < n; ++i) {
+    Stokes S = jet_stokes(P, tab, o, alpha[i], beta[i], r[i], th[i], kr[i], kth[i]);
+    out[3 * i] = S.I;
+    out[3 * i + 1] = S.Q;
+    out[3 * i + 2] = S.U;
+  }
 }
 double hm_lambert_w0(double z) { return lambert_w0(z); }
 double hm_re_li2(double x) { return re_li2(x); }

@@ -60,3 +60,45 @@ def test_stagnation_radius_is_largest_real_root():
                 -a ** 2 * om ** 2 * np.sin(2 * th) ** 2, 0.0, -2 * om ** 2 * s ** 2]
         roots = np.roots(coef[::-1])
         assert abs(r0 - np.max(roots.real)) <= 1e-9 * abs(r0)
+
+
+def test_host_stagnation_matches_numpy_roots():
+    """The kernel's Aberth solve of the stagnation quintic (host build) against the oracle's
+    numpy root 4, and its refusal of a = 0 (the reference's root 4 does not exist there)."""
+    import hmlib
+    for th in (0.05, 0.3, 0.7, 1.2, 1.5, 2.0, 3.0):
+        for a in (0.1, 0.5, 0.94, -0.6):
+            st, r0, om = hmlib.jet_stagnation(a, th)
+            thn = np.arccos(np.abs(np.cos(th)))
+            om_ref = ko.omega_field(a, 10., thn, 'bz_monopole', {})
+            assert st == 0
+            assert abs(om - om_ref) <= 1e-15
+            assert abs(r0 - ko.r0min_mono(th, om_ref, a)) <= 1e-11 * abs(r0)
+    assert hmlib.jet_stagnation(0.0, 0.5)[0] == 2
+
+
+@pytest.mark.parametrize('i', CASES)
+def test_host_emission_matches_oracle(i):
+    """Per-crossing (I, Q, U) of the emission kernel (host build, same source as the CUDA
+    kernel) against the oracle's Iobs_off at the reference's crossings."""
+    import hmlib
+    model, psit, a, inc, pval, nu, neqmax, sigma = eval(str(GOLD['case%d' % i]))
+    x = np.linspace(-8, 8, 16)
+    A, B = np.meshgrid(x, x)
+    A, B = A.flatten(), B.flatten()
+    th_o = inc * DEG
+    geo = ko.raytrace(a, 1.e4, th_o, A, B, 200)
+    tau, rv, tv, spr, spt, neq, shape = ko.findroot(geo, psit, A, B, 1.e4, th_o, a, 200, model=model, neqmax=neqmax,
+                                                    pval=pval)
+    At, Bt = np.tile(A, shape[0]), np.tile(B, shape[0])
+    r0, _ = ko.jet_stagnation(rv, tv, shape, a)
+    with np.errstate(all='ignore'):
+        dv = ko.density_mono_all(rv, tv, shape, a, nu, sigma, table=True)
+        field = ('bz_monopole', {'C': 1, 'table': True}) if model == 'mono' else ('power', {'p': pval})
+        Io, Qo, Uo = ko.iobs_off(a, 1.e4, rv, th_o, At, Bt, spr, spt, field, nu, tv, dv)
+    Io, Qo, Uo = (np.nan_to_num(np.where(rv == 0, 0, v)) for v in (Io, Qo, Uo))
+    Ih, Qh, Uh = hmlib.jet_stokes(a, 1.e4, th_o, 0 if model == 'mono' else 1, nu, sigma, r0, 1.0, At, Bt, rv, tv,
+                                  spr, spt)
+    scale = np.max(np.abs(Io))
+    for h, o in ((Ih, Io), (Qh, Qo), (Uh, Uo)):
+        assert np.max(np.abs(h - o)) <= 1e-10 * scale

@@ -1,0 +1,117 @@
+"""kgeo_jet_stokes and the off_eq.getstokes drop-in on the GPU.
+
+1. Same crossings in, same emission out: the oracle's crossings (CPU findroot) through
+   stokes_device against the oracle's Iobs_off per crossing and its sort_image per subring,
+   within 1e-10 of the image maximum (EVPA within 1e-7 rad where the polarised flux is above
+   1e-6 of the maximum).
+2. The drop-in end to end against the reference's images (tests/golden/jet_stokes.npz): the GPU
+   crossings agree with the reference's to the root solver's 1e-9 where both reached the same
+   root, so the images are compared on the pixels whose every crossing matches, within 1e-7 of
+   the maximum, and those pixels are most of the image.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+pytestmark = pytest.mark.gpu
+
+DEG = np.pi / 180
+
+
+def gold():
+    return np.load(os.path.join(HERE, 'golden', 'jet_stokes.npz'), allow_pickle=False)
+
+
+def cases():
+    g = gold()
+    return [(i, eval(str(g['case%d' % i]))) for i in range(int(g['ncase']))]
+
+
+def grid():
+    x = np.linspace(-8, 8, 16)
+    A, B = np.meshgrid(x, x)
+    return A, B
+
+
+@pytest.mark.parametrize('i,case', cases())
+def test_stokes_kernel_vs_oracle_same_crossings(i, case):
+    import torch
+    from kgeo_gb300 import off_eq
+    from oracle import kgeo_oracle as ko
+    model, psit, a, inc, pval, nu, neqmax, sigma = case
+    A, B = grid()
+    A, B = A.flatten(), B.flatten()
+    th_o = inc * DEG
+    geo = ko.raytrace(a, 1.e4, th_o, A, B, 200)
+    tau, rv, tv, spr, spt, neq, shape = ko.findroot(geo, psit, A, B, 1.e4, th_o, a, 200, model=model, neqmax=neqmax,
+                                                    pval=pval)
+    G = shape[0]
+    cr = {k: torch.tensor(np.asarray(v, float).reshape(G, -1), device='cuda')
+          for k, v in (('r', rv), ('th', tv), ('signpr', spr), ('signpth', spt), ('neq', neq))}
+    out = off_eq.stokes_device(a, 1.e4, th_o, A, B, cr, neqmax=neqmax, model=model, pval=pval, nu_parallel=nu,
+                               sigma=sigma, per_crossing=True)
+    assert int(out['status'].item()) == 0
+    r0, om = ko.jet_stagnation(rv, tv, shape, a)
+    st = out['stagnation'].cpu().numpy()
+    assert abs(st[0] - r0) <= 1e-11 * abs(r0)
+    assert abs(st[1] - om) <= 1e-15
+    At, Bt = np.tile(A, G), np.tile(B, G)
+    with np.errstate(all='ignore'):
+        dv = ko.density_mono_all(rv, tv, shape, a, nu, sigma, table=True)
+        field = ('bz_monopole', {'C': 1, 'table': True}) if model == 'mono' else ('power', {'p': pval})
+        Io, Qo, Uo = ko.iobs_off(a, 1.e4, rv, th_o, At, Bt, spr, spt, field, nu, tv, dv)
+    Io, Qo, Uo = (np.real(np.nan_to_num(np.where(rv == 0, 0, v))) for v in (Io, Qo, Uo))
+    scale = np.max(np.abs(Io))
+    assert scale > 0
+    for k, ref in (('Ic', Io), ('Qc', Qo), ('Uc', Uo)):
+        got = out[k].cpu().numpy().reshape(-1)
+        assert np.max(np.abs(got - ref)) <= 1e-10 * scale, (k, np.max(np.abs(got - ref)) / scale)
+    iv, qv, uv = ko.sort_image(Io, Qo, Uo, neq, shape, (16, 16), neqmax)
+    ev = np.nan_to_num(0.5 * np.arctan2(uv, qv))
+    for k, ref in (('I', iv), ('Q', qv), ('U', uv)):
+        got = out[k].cpu().numpy().reshape(ref.shape)
+        assert np.max(np.abs(got - ref)) <= 1e-10 * scale, (k, np.max(np.abs(got - ref)) / scale)
+    pol = np.hypot(qv, uv) > 1e-6 * scale
+    d = np.abs(((out['evpa'].cpu().numpy().reshape(ev.shape) - ev) + np.pi / 2) % np.pi - np.pi / 2)
+    assert np.max(d[pol], initial=0.0) <= 1e-7
+
+
+@pytest.mark.parametrize('i,case', cases())
+def test_getstokes_dropin_vs_reference(i, case):
+    from kgeo_gb300 import off_eq
+    g = gold()
+    model, psit, a, inc, pval, nu, neqmax, sigma = case
+    A, B = grid()
+    I, Q, U, ev, r, th = off_eq.getstokes(psit, A, B, 1.e4, inc * DEG, a, 200, model=model, pval=pval, neqmax=neqmax,
+                                          retvals=True, nu_parallel=nu, sigma=sigma)
+    ref = [g['%s%d' % (k, i)] for k in ('I', 'Q', 'U', 'evpa', 'r', 'th')]
+    assert I.shape == ref[0].shape
+    if r.shape != ref[4].shape:
+        pytest.fail('guess rows differ: %s vs %s' % (r.shape, ref[4].shape))
+    npix = A.size
+    G = r.size // npix
+    close = lambda x, y: np.abs(x - y) <= 1e-9 * np.maximum(np.abs(y), 1e-12)  # noqa: E731
+    same = np.all((close(r, ref[4]) & close(th, ref[5])).reshape(G, npix), axis=0).reshape(A.shape)
+    assert same.mean() >= 0.75, same.mean()
+    scale = np.max(np.abs(ref[0]))
+    for x, y in zip((I, Q, U), ref[:3]):
+        assert np.max(np.abs(x - y)[:, same]) <= 1e-7 * scale, np.max(np.abs(x - y)[:, same]) / scale
+    pol = (np.hypot(ref[1], ref[2]) > 1e-4 * scale) & same[None]
+    d = np.abs(((ev - ref[3]) + np.pi / 2) % np.pi - np.pi / 2)
+    assert np.max(d[pol], initial=0.0) <= 1e-5
+
+
+def test_getstokes_unsupported_models_raise():
+    from kgeo_gb300 import off_eq
+    A, B = grid()
+    with pytest.raises(NotImplementedError):
+        off_eq.getstokes(0.5, A, B, 1.e4, 0.5, 0.5, 50, model='para')
+    with pytest.raises(NotImplementedError):
+        off_eq.getstokes(0.5, A, B, 1.e4, 0.5, 0.5, 50, model='power', pval=1.0)
+    with pytest.raises(NotImplementedError):
+        off_eq.getstokes(0.5, A, B, 1.e4, 0.5, 0.5, 50, model='mono', gammamax=5.0)
