@@ -1029,10 +1029,10 @@ def run_jet(args):
 STOKES_GRID = 256
 STOKES_CASE = dict(a=0.5, inc=60.0, model='mono', psitarget=0.4, ngeo=200, neqmax=1, nu_parallel=0.0, sigma=2.0)
 CPU_STOKES_SAMPLE = 2048
-# FP64 work of jet_stokes_kernel per crossing row and pixel on the stokes-small capture
-# (profiles/jet_stokes.md); None until captured
-STOKES_FLOP_PER_CROSSING = None
-STOKES_FP64_INST_PER_CROSSING = None
+# FP64 work of jet_stokes_kernel per crossing (r != 0) on the stokes-small capture
+# (profiles/jet_stokes.md): dadd + dmul + 2 dfma, and FP64 pipe instructions
+STOKES_FLOP_PER_CROSSING = 2940
+STOKES_FP64_INST_PER_CROSSING = 1901
 
 
 def _cpu_stokes_chunk(args):
@@ -1107,19 +1107,20 @@ def run_stokes(args):
     if pool is not None:
         idx = np.arange(0, A.size, max(1, A.size // CPU_STOKES_SAMPLE))[:CPU_STOKES_SAMPLE]
         chunks = np.array_split(idx, cores * 2)
+        # the density's stagnation radius comes from the first crossing of the first guess row:
+        # every chunk starts with the image's first crossing pixel so that it has one
+        i0 = int(torch.nonzero(cr['r'][0] != 0)[0, 0])
         t0 = time.time()
-        pool.map(_cpu_stokes_chunk, [(A[k], B[k]) for k in chunks])
+        pool.map(_cpu_stokes_chunk, [(np.r_[A[i0], A[k]], np.r_[B[i0], B[k]]) for k in chunks])
         dt = time.time() - t0
         cpu = {'value': idx.size / dt, 'unit': 'pixels/s (getstokes)', 'cores': cores, 'kind': 'port',
-               'sample': '%d pixels (every %dth of the %dx%d grid): oracle getstokes (raytrace, findroot, emission) '
-                         'on a %d-process pool, %.1f s wall' % (idx.size, A.size // idx.size, n, n, cores, dt)}
+               'sample': '%d pixels (every %dth of the %dx%d grid) in %d chunks, each led by the image\'s first '
+                         'crossing pixel: oracle getstokes (raytrace, findroot, emission) on a %d-process pool, '
+                         '%.1f s wall' % (idx.size, A.size // idx.size, n, n, len(chunks), cores, dt)}
         pool.close()
-    if STOKES_FLOP_PER_CROSSING:
-        roof = roofline_fp64('jet_stokes_kernel', t_kern, G * A.size, STOKES_FLOP_PER_CROSSING,
-                             STOKES_FP64_INST_PER_CROSSING, 'crossing_row')
-    else:
-        roof = {'kernel': 'jet_stokes_kernel', 'launch_ms': t_kern * 1e3, 'bound': 'fp64', 'achieved': None,
-                'frac': None, 'traffic': None, 'note': 'FP64 work per crossing not captured'}
+    roof = roofline_fp64('jet_stokes_kernel', t_kern, ncross, STOKES_FLOP_PER_CROSSING, STOKES_FP64_INST_PER_CROSSING,
+                         'crossing')
+    roof['timed'] = 'kgeo_jet_stokes: jet_stagnation_kernel (one block) + jet_stokes_kernel'
     line = {
         'metric': 'pixels/s: jet Stokes images (getstokes: trace, field-line crossings, emission, subring sums)',
         'value': A.size / t_step, 'unit': 'pixels/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
@@ -1134,7 +1135,7 @@ def run_stokes(args):
         'e2e': {'value': A.size / t_e2e, 'unit': 'pixels/s (getstokes)', 'h2d_bytes_per_step': 16 * A.size,
                 'd2h_bytes_per_step': 32 * (c['neqmax'] + 1) * A.size, 'ms_per_step': t_e2e * 1e3,
                 'path': 'kgeo_gb300.off_eq.getstokes (numpy in/out)'},
-        'gpu_launches': args.steps * 7, 'clocks': ck,
+        'gpu_launches': args.steps * 12, 'clocks': ck,
     }
     print(json.dumps(line))
 

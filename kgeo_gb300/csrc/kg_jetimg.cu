@@ -53,11 +53,16 @@ cudaError_t jet_bz_table(const double** tab) {
 }
 
 // One block: the first crossing of the first guess row (np.where(r[0] != 0)[0][0]), then the
-// stagnation radius of its field line. par = (r0, Omega, status): status 1 when the row has no
-// crossing (the reference's index lookup raises), 2 or 3 when the quintic has no root 4.
+// stagnation radius of its field line, the five Aberth roots iterated by lanes 0-4 of warp 0
+// (the same arithmetic as quintic_max_real_root). par = (r0, Omega, status): status 1 when the
+// row has no crossing (the reference's index lookup raises), 2 or 3 when the quintic has no
+// root 4.
 __global__ void __launch_bounds__(256) jet_stagnation_kernel(const double* r, const double* th, int64_t npix,
                                                              double a, double* par) {
   __shared__ unsigned long long first;
+  __shared__ double coef[6];
+  __shared__ Cplx z[5];
+  __shared__ int state;
   if (threadIdx.x == 0) first = ~0ull;
   __syncthreads();
   for (int64_t base = 0; base < npix; base += blockDim.x) {
@@ -66,18 +71,57 @@ __global__ void __launch_bounds__(256) jet_stagnation_kernel(const double* r, co
     if (hit) atomicMin(&first, (unsigned long long)i);
     if (__syncthreads_or(hit)) break;
   }
-  if (threadIdx.x != 0) return;
-  if (first == ~0ull) {
-    par[0] = 0.0;
-    par[1] = 0.0;
-    par[2] = 1.0;
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  if (lane == 0) {
+    state = 0;
+    if (first == ~0ull) {
+      state = 1;
+    } else {
+      double om = 0.0;
+      stagnation_quintic(a, th[first], coef, &om);
+      par[1] = om;
+      if (!(coef[5] != 0.0) || !kg_finite(coef[5])) state = 2;
+      else if (aberth_radius(coef) == 0.0) state = 3;
+    }
+  }
+  __syncwarp();
+  if (state != 0) {
+    if (lane == 0) {
+      par[0] = 0.0;
+      if (state == 1) par[1] = 0.0;
+      par[2] = (double)state;
+    }
     return;
   }
-  double r0 = 0.0, om = 0.0;
-  const int st = jet_stagnation(a, th[first], &r0, &om);
-  par[0] = r0;
-  par[1] = om;
-  par[2] = (double)st;
+  double c[6];
+  for (int k = 0; k < 6; ++k) c[k] = coef[k];
+  if (lane < 5) z[lane] = aberth_start(aberth_radius(c), lane);
+  __syncwarp();
+  for (int it = 0; it < ABERTH_MAXITER; ++it) {
+    Cplx zl[5];
+    for (int k = 0; k < 5; ++k) zl[k] = z[k];
+    double corr = 0.0;
+    Cplx zi{0.0, 0.0};
+    if (lane < 5) {
+      const Cplx w = aberth_correction(c, zl, lane);
+      zi = c_sub(zl[lane], w);
+      corr = c_abs(w) / fmax(c_abs(zi), 1e-300);
+    }
+    __syncwarp();
+    if (lane < 5) z[lane] = zi;
+    for (int o = 16; o > 0; o >>= 1) corr = fmax(corr, __shfl_xor_sync(0xffffffffu, corr, o));
+    __syncwarp();
+    if (corr < ABERTH_TOL) break;
+  }
+  if (lane == 0) {
+    Cplx zl[5];
+    for (int k = 0; k < 5; ++k) zl[k] = z[k];
+    double r0 = 0.0;
+    const int st = aberth_finish(c, zl, &r0);
+    par[0] = r0;
+    par[2] = (double)st;
+  }
 }
 
 __global__ void __launch_bounds__(128) jet_stokes_kernel(JetStokesArgs a) {

@@ -224,8 +224,8 @@ struct Cplx {
 KG_HD Cplx c_sub(Cplx x, Cplx y) { return Cplx{x.re - y.re, x.im - y.im}; }
 KG_HD Cplx c_mul(Cplx x, Cplx y) { return Cplx{x.re * y.re - x.im * y.im, x.re * y.im + x.im * y.re}; }
 KG_HD Cplx c_div(Cplx x, Cplx y) {
-  const double d = y.re * y.re + y.im * y.im;
-  return Cplx{(x.re * y.re + x.im * y.im) / d, (x.im * y.re - x.re * y.im) / d};
+  const double d = 1.0 / (y.re * y.re + y.im * y.im);
+  return Cplx{(x.re * y.re + x.im * y.im) * d, (x.im * y.re - x.re * y.im) * d};
 }
 KG_HD double c_abs(Cplx x) { return hypot(x.re, x.im); }
 KG_HD bool kg_finite(double x) { return x - x == 0.0; }
@@ -244,43 +244,45 @@ KG_HD void poly5(const double* c, Cplx z, Cplx* p, Cplx* dp) {
   *dp = d;
 }
 
-// Largest real part of the roots of c[0] + ... + c[5] z^5; 0 when found, 2 when c[5] == 0
-// (numpy trims the leading zero and the reference's root 4 does not exist), 3 without
-// convergence.
-KG_HD int quintic_max_real_root(const double* c, double* out) {
-  if (!(c[5] != 0.0) || !kg_finite(c[5])) return 2;
+// Aberth-Ehrlich correction of root i from the current roots z (the simultaneous form: every
+// root's correction uses the previous iterate of the others, so the five can run in parallel).
+KG_HD Cplx aberth_correction(const double* c, const Cplx* z, int i) {
+  Cplx p, dp;
+  poly5(c, z[i], &p, &dp);
+  if (p.re == 0.0 && p.im == 0.0) return Cplx{0.0, 0.0};
+  const Cplx ratio = c_div(p, dp);
+  Cplx sum{0.0, 0.0};
+  for (int j = 0; j < 5; ++j) {
+    if (j == i) continue;
+    const Cplx inv = c_div(Cplx{1.0, 0.0}, c_sub(z[i], z[j]));
+    sum.re += inv.re;
+    sum.im += inv.im;
+  }
+  const Cplx rs = c_mul(ratio, sum);
+  const Cplx w = c_div(ratio, Cplx{1.0 - rs.re, -rs.im});
+  if (!kg_finite(w.re) || !kg_finite(w.im)) return Cplx{0.0, 0.0};
+  return w;
+}
+
+// Start of the iteration: five points on a circle of twice the Fujiwara bound (> every root);
+// 0 when the start is unusable.
+KG_HD double aberth_radius(const double* c) {
   double rad = 0.0;
   for (int k = 0; k < 5; ++k) rad = fmax(rad, pow(fabs(c[k] / c[5]), 1.0 / (5 - k)));
   rad = 2.0 * rad;
-  if (!(rad > 0.0) || !kg_finite(rad)) return 3;
-  Cplx z[5];
-  for (int k = 0; k < 5; ++k) {
-    const double ang = 2.0 * PI * k / 5.0 + 0.4;
-    z[k] = Cplx{rad * cos(ang), rad * sin(ang)};
-  }
-  bool done = false;
-  for (int it = 0; it < 500 && !done; ++it) {
-    double corr = 0.0;
-    for (int i = 0; i < 5; ++i) {
-      Cplx p, dp;
-      poly5(c, z[i], &p, &dp);
-      if (p.re == 0.0 && p.im == 0.0) continue;
-      const Cplx ratio = c_div(p, dp);
-      Cplx sum{0.0, 0.0};
-      for (int j = 0; j < 5; ++j) {
-        if (j == i) continue;
-        const Cplx inv = c_div(Cplx{1.0, 0.0}, c_sub(z[i], z[j]));
-        sum.re += inv.re;
-        sum.im += inv.im;
-      }
-      const Cplx rs = c_mul(ratio, sum);
-      const Cplx w = c_div(ratio, Cplx{1.0 - rs.re, -rs.im});
-      if (!kg_finite(w.re) || !kg_finite(w.im)) continue;
-      z[i] = c_sub(z[i], w);
-      corr = fmax(corr, c_abs(w) / fmax(c_abs(z[i]), 1e-300));
-    }
-    done = corr < 1e-15;
-  }
+  return (rad > 0.0 && kg_finite(rad)) ? rad : 0.0;
+}
+
+KG_HD Cplx aberth_start(double rad, int k) {
+  const double ang = 2.0 * PI * k / 5.0 + 0.4;
+  return Cplx{rad * cos(ang), rad * sin(ang)};
+}
+
+constexpr int ABERTH_MAXITER = 200;
+constexpr double ABERTH_TOL = 1e-15;  // largest relative correction of the last iteration
+
+// The largest real part of the converged roots, after three Newton steps on that root.
+KG_HD int aberth_finish(const double* c, const Cplx* z, double* out) {
   int best = 0;
   for (int k = 1; k < 5; ++k)
     if (z[k].re > z[best].re) best = k;
@@ -297,9 +299,30 @@ KG_HD int quintic_max_real_root(const double* c, double* out) {
   return 0;
 }
 
-// r0 and Omega_F of the field line through the crossing (r, th): the BZ monopole's Omega at
-// the reflected angle and the quintic's root (kgeo/densityfuncs.py:47-60, kgeo/ff_boost.py).
-KG_HD int jet_stagnation(double a, double th, double* r0, double* omega) {
+// Largest real part of the roots of c[0] + ... + c[5] z^5 (serial form of the iteration that
+// jet_stagnation_kernel runs on five lanes); 0 when found, 2 when c[5] == 0 (numpy trims the
+// leading zero and the reference's root 4 does not exist), 3 without a usable start.
+KG_HD int quintic_max_real_root(const double* c, double* out) {
+  if (!(c[5] != 0.0) || !kg_finite(c[5])) return 2;
+  const double rad = aberth_radius(c);
+  if (rad == 0.0) return 3;
+  Cplx z[5], w[5];
+  for (int k = 0; k < 5; ++k) z[k] = aberth_start(rad, k);
+  for (int it = 0; it < ABERTH_MAXITER; ++it) {
+    double corr = 0.0;
+    for (int i = 0; i < 5; ++i) w[i] = aberth_correction(c, z, i);
+    for (int i = 0; i < 5; ++i) {
+      z[i] = c_sub(z[i], w[i]);
+      corr = fmax(corr, c_abs(w[i]) / fmax(c_abs(z[i]), 1e-300));
+    }
+    if (corr < ABERTH_TOL) break;
+  }
+  return aberth_finish(c, z, out);
+}
+
+// Coefficients of the stagnation quintic and Omega_F of the field line through theta
+// (kgeo/ff_boost.py:7-18 with M = 1; kgeo/bfields.py:590-593 at the reflected angle).
+KG_HD void stagnation_quintic(double a, double th, double* c, double* omega) {
   const double thn = acos(fabs(cos(th)));
   const Trig T = trig_of(thn);
   const double f2 = (6 * PI * PI - 49.) / 72.;
@@ -310,13 +333,19 @@ KG_HD int jet_stagnation(double a, double th, double* r0, double* omega) {
   *omega = om;
   const double k = 2 - a * om + a * om * T.c2th;
   const double s2t = sin(2 * thn);
-  double c[6];
   c[0] = -(a * a) / 2 * 1.0 * T.cth2 * (k * k);
   c[1] = -2 * pow(a, 4.0) * (om * om) * pow(T.cth, 4.0) * T.sth2;
   c[2] = 1.0 / 2 * (k * k);
   c[3] = -(a * a) * (om * om) * (s2t * s2t);
   c[4] = 0.0;
   c[5] = -2 * (om * om) * T.sth2;
+}
+
+// r0 and Omega_F of the field line through the crossing (r, th): the BZ monopole's Omega at
+// the reflected angle and the quintic's root (kgeo/densityfuncs.py:47-60, kgeo/ff_boost.py).
+KG_HD int jet_stagnation(double a, double th, double* r0, double* omega) {
+  double c[6];
+  stagnation_quintic(a, th, c, omega);
   return quintic_max_real_root(c, r0);
 }
 
