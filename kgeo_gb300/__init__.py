@@ -9,6 +9,7 @@ Drop-in modules (same names, signatures and outputs as kgeo's):
   equatorial_images     make_image, Iobs (unpolarised, polarised, with path length)
   emissivities, velocities, bfields   the emission, velocity and B-field models
   solver                jet field-line crossings (getguesses, findroot)
+  off_eq                getstokes: Stokes images of the monopole jet field line
 Beyond kgeo: image_grad (an adjoint-backed torch.autograd.Function) and batch (many images in
 one persistent launch, CUDA graph replay, autotuned shape). The compute path is the CUDA
 library libkgeo_gb300.so (C ABI: include/kgeo_gb300.h); there is no CPU path.
