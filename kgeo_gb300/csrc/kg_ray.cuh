@@ -1170,6 +1170,90 @@ KG_HD void ray_chunk(const Observer& ob, const FV& f, int code, int64_t g0, int6
   }
 }
 
+// ---- theta and r only ----------------------------------------------------------
+
+// sn, cn, dn of the theta amplitude at snarg (the Jacobi part of theta_state_direct).
+template <class FV>
+KG_HD ThetaState theta_sncd_direct(const FV& f, double snarg) {
+  double v;
+  const double nr = reduce_half_period(snarg / f[T_S1M], f[T_K2], &v);
+  const Jacobi J = jacobi_landen(v, f[T_M]);
+  const double odd = fmod(fabs(nr), 2.0) == 1.0 ? -1.0 : 1.0;
+  const double idn = 1.0 / J.dn;
+  ThetaState st;
+  st.sn = odd * (f[T_S1M] * J.sn) * idn;
+  st.cn = odd * J.cn * idn;
+  st.dn = idn;
+  st.e = st.pi = st.Phi = 0.0;
+  return st;
+}
+
+// theta from sn (theta_assemble's first line for each branch).
+template <class FV>
+KG_HD double theta_of_sn(const FV& f, int code, double sn) {
+  const double up = f[T_UP];
+  if (code_th(code) == TH_ORD) return acos(-f[F_S] * sqrt(up) * sn);
+  const double um = f[T_UM];
+  return acos(f[T_H] * sqrt(um + (up - um) * (sn * sn)));
+}
+
+// One radial step of sn, cn, dn alone; fresh Jacobi functions next to the pole of the r
+// formula (the n0 characteristic), as radial_step does.
+template <class FV>
+KG_HD void radial_sncd_step(const FV& f, RadialState* st, double Xnew) {
+  const double k = f[R_M];
+  JacobiW w = jacobi_add(st->sn, st->cn, st->dn, -f[S_RSN], f[S_RCN], f[S_RDN], k);
+  if (near_pi_pole(f[R_N0], st->sn, POLE_RHO_R) || near_pi_pole(f[R_N0], w.sn, POLE_RHO_R)) {
+    double v;
+    const int nr = (int)reduce_half_period(Xnew, f[R_K2], &v);
+    const Jacobi J = jacobi_landen(v, k);
+    const double odd = (nr & 1) ? -1.0 : 1.0;
+    w.sn = odd * J.sn;
+    w.cn = odd * J.cn;
+    w.dn = J.dn;
+  }
+  st->sn = w.sn;
+  st->cn = w.cn;
+  st->dn = w.dn;
+  st->X = Xnew;
+}
+
+// Samples g0 .. g1-1 of theta and r alone (t, phi and sigma not requested): ray_chunk's grid,
+// chunk starts and addition-theorem steps on the Jacobi functions only, with no E or Pi (and
+// so none of their pole re-seeds). emit(g, tau, r, theta) stores.
+template <class FV, class Emit>
+KG_HD void ray_chunk_rth(const FV& f, int code, int64_t g0, int64_t g1, int64_t G, bool ordinary_active,
+                         bool step_zero, Emit emit) {
+  const EvenGrid grid(f[F_TAUMAX], G, step_zero);
+  const bool thact = theta_active(f, code, ordinary_active);
+  const bool stepping = code_step(code);
+  const bool rdo = code_rcase(code) != RCASE_NONE;
+  ThetaState ts;
+  RadialState rs;
+  ts.sn = ts.cn = ts.dn = ts.e = ts.pi = ts.Phi = 0.0;
+  rs.X = rs.sn = rs.cn = rs.dn = rs.E = rs.am = 0.0;
+  rs.P[0] = rs.P[1] = rs.P[2] = 0.0;
+  for (int64_t g = g0; g < g1; ++g) {
+    const double tau = grid.at(g);
+    const double X = radial_X(f, tau);
+    if (g == g0 || g == G - 1 || !stepping) {
+      if (thact) ts = theta_sncd_direct(f, theta_snarg(f, tau));
+      if (rdo) rs = radial_state_direct(f, code, X, false);
+    } else {
+      if (thact) {
+        const JacobiW w = jacobi_add(ts.sn, ts.cn, ts.dn, -f[S_TSN], f[S_TCN], f[S_TDN], f[T_KK]);
+        ts.sn = w.sn;
+        ts.cn = w.cn;
+        ts.dn = w.dn;
+      }
+      if (rdo) radial_sncd_step(f, &rs, X);
+    }
+    const double th = thact ? theta_of_sn(f, code, ts.sn) : 0.0;
+    const double r = rdo ? radial_assemble(f, code, tau, rs, false).r : 0.0;
+    emit(g, tau, r, th);
+  }
+}
+
 struct GainArgs {
   double a, rp, rm, r_o;
 };

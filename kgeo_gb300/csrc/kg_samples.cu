@@ -48,7 +48,7 @@ extern __shared__ float kg_ffray_smem[];
 
 __device__ __forceinline__ FFRay* ffray_slot() { return reinterpret_cast<FFRay*>(kg_ffray_smem) + threadIdx.x; }
 
-template <bool MIXED>
+template <bool MIXED, bool RTH>
 __global__ void __launch_bounds__(256) stepped_kernel(SampleArgs a) {
   const uint32_t fl = *a.flags;
   const bool ordinary_active = (fl & FLAG_ANY_ETA_POS) != 0;
@@ -77,8 +77,19 @@ __global__ void __launch_bounds__(256) stepped_kernel(SampleArgs a) {
       if (a.sig) a.sig[o] = S.sig;
       if (a.mino) a.mino[o] = tau;
     };
-    if (MIXED) ray_chunk_ff(a.obs, f, code, g0, g1, a.nsamp, ordinary_active, step_zero, emit, ffray_slot());
-    else ray_chunk(a.obs, f, code, g0, g1, a.nsamp, ordinary_active, step_zero, emit);
+    if (MIXED) {
+      ray_chunk_ff(a.obs, f, code, g0, g1, a.nsamp, ordinary_active, step_zero, emit, ffray_slot());
+    } else if (RTH) {
+      ray_chunk_rth(f, code, g0, g1, a.nsamp, ordinary_active, step_zero,
+                    [&](int64_t g, double tau, double r, double th) {
+                      const int64_t o = (g - a.row0) * a.npix + p;
+                      if (a.r) a.r[o] = r;
+                      if (a.th) a.th[o] = th;
+                      if (a.mino) a.mino[o] = tau;
+                    });
+    } else {
+      ray_chunk(a.obs, f, code, g0, g1, a.nsamp, ordinary_active, step_zero, emit);
+    }
   }
 }
 
@@ -98,12 +109,15 @@ cudaError_t launch_samples(const SampleArgs& a, cudaStream_t s) {
     if (grid > cap) grid = cap;
     if (a.mixed) {
       const size_t smem = sizeof(FFRay) * block;
-      if (cudaFuncSetAttribute(stepped_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-          cudaSuccess)
+      if (cudaFuncSetAttribute(stepped_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem) != cudaSuccess)
         return cudaGetLastError();
-      stepped_kernel<true><<<(unsigned)grid, block, smem, s>>>(a);
+      stepped_kernel<true, false><<<(unsigned)grid, block, smem, s>>>(a);
+    } else if (!a.t && !a.ph && !a.sig) {
+      // theta and r only: the Jacobi recurrence without E and Pi
+      stepped_kernel<false, true><<<(unsigned)grid, block, 0, s>>>(a);
     } else {
-      stepped_kernel<false><<<(unsigned)grid, block, 0, s>>>(a);
+      stepped_kernel<false, false><<<(unsigned)grid, block, 0, s>>>(a);
     }
     return cudaGetLastError();
   }

@@ -86,6 +86,19 @@ void hm_samples_stepped(const double* ob, const double* rec, const int* code, lo
     }
   }
 }
+void hm_samples_rth(const double* ob, const double* rec, const int* code, long n, long G, long chunk,
+                    int ordinary_active, double* r, double* th, double* mino) {
+  (void)ob;
+  for (long i = 0; i < n; ++i) {
+    RecView f{rec + i, n};
+    for (long g0 = 0; g0 < G; g0 += chunk) {
+      long g1 = g0 + chunk < G ? g0 + chunk : G;
+      ray_chunk_rth(f, code[i], g0, g1, G, ordinary_active != 0, false, [&](long g, double tau, double rr, double tt) {
+        r[g * n + i] = rr; th[g * n + i] = tt; mino[g * n + i] = tau;
+      });
+    }
+  }
+}
 void hm_samples_mixed(const double* ob, const double* rec, const int* code, long n, long G, long chunk,
                    int ordinary_active, double* t, double* r, double* th, double* ph, double* sig, double* mino) {
   Observer o = make_obs(ob);

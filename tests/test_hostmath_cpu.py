@@ -86,6 +86,23 @@ def host_trace_stepped(L, a, r_o, th_o, alpha, beta, ngeo, chunk, maxtaufrac=1 -
     return dict(t=t, r=r, th=th, ph=ph, sig=sig, mino=mino)
 
 
+def host_trace_rth(L, a, r_o, th_o, alpha, beta, ngeo, chunk, maxtaufrac=1 - 1e-10):
+    n = len(alpha)
+    nf = L.hm_num_fields()
+    ob = observer(a, r_o, th_o)
+    rec = np.zeros(nf * n)
+    code, rc, tc = (np.zeros(n, np.int32) for _ in range(3))
+    alpha = np.ascontiguousarray(alpha, float)
+    beta = np.ascontiguousarray(beta, float)
+    flags = L.hm_setup(dp(ob), dp(alpha), dp(beta), ctypes.c_long(n), D(maxtaufrac), dp(rec), ip(code), ip(rc), ip(tc),
+                       ctypes.c_long(ngeo))
+    outs = [np.zeros((ngeo, n)) for _ in range(3)]
+    L.hm_samples_rth(dp(ob), dp(rec), ip(code), ctypes.c_long(n), ctypes.c_long(ngeo), ctypes.c_long(chunk),
+                     ctypes.c_int(flags & 1), *[dp(o) for o in outs])
+    r, th, mino = outs
+    return dict(r=r, th=th, mino=mino)
+
+
 def rel(a, b):
     return np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))
 
@@ -148,3 +165,10 @@ def test_host_trace_vs_reference_fixture(hm, golden, name):
         st = host_trace_stepped(hm, a, r_o, th_o, g['alpha'], g['beta'], int(g['ngeo']), 50)
         check_trace(st, dict(t=g['t'], r=g['r'], th=g['th'], ph=g['ph'], sig=g['sig']), r_o, g['rclass'],
                     name + '-recurrence', rho=rho)
+        # theta and r alone (the sample kernel's path when t, phi and sigma are not requested),
+        # against the same bars; the other three are taken from the fixture
+        rth = host_trace_rth(hm, a, r_o, th_o, g['alpha'], g['beta'], int(g['ngeo']), 64)
+        assert np.array_equal(rth['mino'], st['mino'])
+        check_trace(dict(r=rth['r'], th=rth['th'], t=g['t'], ph=g['ph'], sig=g['sig']),
+                    dict(t=g['t'], r=g['r'], th=g['th'], ph=g['ph'], sig=g['sig']), r_o, g['rclass'],
+                    name + '-rth', rho=rho)

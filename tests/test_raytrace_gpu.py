@@ -54,6 +54,29 @@ def test_trace_vs_reference_fixture(kg, golden, name):
     check_trace(got, ref, r_o, g['rclass'], name, rho=rho)
 
 
+@pytest.mark.parametrize('name', TRACES)
+def test_theta_r_only_trace_vs_reference_fixture(kg, golden, name):
+    """kgeo_raytrace with t, phi and sigma not requested runs the sample kernel's theta / r
+    path (the Jacobi recurrence without E and Pi): r and theta against the reference's within
+    the same bars, the Mino times identical to the full trace's."""
+    import torch
+    from kgeo_gb300 import device as dev
+    g = golden(name)
+    a, r_o, th_o = float(g['a']), float(g['r_o']), float(g['th_o'])
+    if not np.isfinite(r_o):
+        pytest.skip('r_o = inf: covered by the full trace test')
+    al, be = dev.as_device(g['alpha']), dev.as_device(g['beta'])
+    res = dev.trace(a, r_o, th_o, al, be, ngeo=int(g['ngeo']), outputs=('r', 'th', 'mino'), per_ray=())
+    torch.cuda.synchronize()
+    full = _run(kg, a, r_o, th_o, g['alpha'], g['beta'], int(g['ngeo']))
+    assert np.array_equal(res['mino'].cpu().numpy(), full['mino'])
+    from oracle import kgeo_oracle as ko
+    rho = ko.pole_distance(a, r_o, th_o, g['alpha'], g['beta'], g['mino'])
+    ref = dict(t=g['t'], r=g['r'], th=g['th'], ph=g['ph'], sig=g['sig'])
+    got = dict(ref, r=res['r'].cpu().numpy(), th=res['th'].cpu().numpy())
+    check_trace(got, ref, r_o, g['rclass'], name + '-rth', rho=rho)
+
+
 def test_config1_full_vs_oracle(kg):
     """a = 0.94, r_o = 1e4, theta_o = 20 deg, 64x64 over [-8, 8], ngeo = 100 (the reference's CPU case)."""
     from oracle import kgeo_oracle as ko
@@ -222,8 +245,14 @@ def test_config2_draws_vs_oracle(kg, seed):
     ref = ko.raytrace(a, 1.e4, th_o, A, B, 400)
     got = _run(kg, a, 1.e4, th_o, A, B, 400)
     rho = ko.pole_distance(a, 1.e4, th_o, A, B, ref['mino_times'])
-    check_trace(got, dict(t=ref['t'], r=ref['r'], th=ref['th'], ph=ref['ph'], sig=ref['affine_times']), 1.e4,
-                ref['rclass'], 'config2-%d' % seed, rho=rho)
+    refd = dict(t=ref['t'], r=ref['r'], th=ref['th'], ph=ref['ph'], sig=ref['affine_times'])
+    check_trace(got, refd, 1.e4, ref['rclass'], 'config2-%d' % seed, rho=rho)
+    # the theta / r only path on the same draws
+    from kgeo_gb300 import device as dev
+    res = dev.trace(a, 1.e4, th_o, dev.as_device(A), dev.as_device(B), ngeo=400, outputs=('r', 'th', 'mino'),
+                    per_ray=())
+    check_trace(dict(refd, r=res['r'].cpu().numpy(), th=res['th'].cpu().numpy()), refd, 1.e4, ref['rclass'],
+                'config2-rth-%d' % seed, rho=rho)
 
 
 @pytest.mark.parametrize('chunk', [1, 7, 50, 64])
