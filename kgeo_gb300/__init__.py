@@ -10,6 +10,8 @@ Drop-in modules (same names, signatures and outputs as kgeo's):
   emissivities, velocities, bfields   the emission, velocity and B-field models
   solver                jet field-line crossings (getguesses, findroot)
   off_eq                getstokes: Stokes images of the monopole jet field line
+The same functions as torch operators on CUDA tensors (torch.ops.kgeo.*, with fake
+implementations and the image's autograd): import kgeo_gb300.ops.
 Beyond kgeo: image_grad (an adjoint-backed torch.autograd.Function) and batch (many images in
 one persistent launch, CUDA graph replay, autotuned shape). The compute path is the CUDA
 library libkgeo_gb300.so (C ABI: include/kgeo_gb300.h); there is no CPU path.
