@@ -80,12 +80,20 @@ def cpu_sample(seed):
     return a, th_o, A[idx], B[idx]
 
 
+def _pool_warm(_):
+    from oracle import kgeo_oracle  # noqa: F401  (worker start-up and imports outside every timing)
+    time.sleep(0.3)
+    return 0
+
+
 def make_pool():
     import multiprocessing as mp
     cores = len(os.sched_getaffinity(0))
     os.environ.setdefault('OMP_NUM_THREADS', '1')
     os.environ.setdefault('OPENBLAS_NUM_THREADS', '1')
-    return mp.get_context('spawn').Pool(cores), cores
+    pool = mp.get_context('spawn').Pool(cores)
+    pool.map(_pool_warm, range(2 * cores), chunksize=1)
+    return pool, cores
 
 
 def cpu_run(pool, cores, seed):
@@ -168,9 +176,6 @@ def dist_env():
 
 def run_ours(args):
     rank, world, local = dist_env()
-    pool = cores = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        pool, cores = make_pool()  # spawn the CPU workers before any CUDA initialisation
     import torch
     torch.cuda.set_device(local)
     if world > 1:
@@ -286,7 +291,10 @@ def run_ours(args):
                          'frac': (hbm / pk['hbm_gbs']) if pk.get('hbm_gbs') else None,
                          'bytes_per_point': BYTES_PER_POINT}
     cpu = None
-    if pool is not None:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # spawned workers (no CUDA state inherited), started after the GPU timings so that no
+        # worker start-up overlaps them
+        pool, cores = make_pool()
         cpu_run(pool, cores, rank)  # warm the workers (imports)
         n, dt = cpu_run(pool, cores, rank)
         pool.close()
@@ -403,8 +411,6 @@ def error_stats(got, ref, rclass, torch, rho=None):
 def run_mixed(args):
     small = args.case == 'mixed-small'
     pool = cores = None
-    if not args.no_cpu_baseline:
-        pool, cores = make_pool()
     import torch
     from kgeo_gb300 import device as dev
     a, th_o, A, B, ngrid = mixed_workload(small)
@@ -450,7 +456,8 @@ def run_mixed(args):
     errs = error_stats(out_m, out_d, prep.rclass, torch)
     # FP64 kernel against the oracle on a seeded 1/64 subsample of the same rays
     orc = orc_m = None
-    if pool is not None:
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()  # spawned after the GPU timings
         rng = np.random.default_rng(0)
         sub = np.sort(rng.choice(npix, npix // 64, replace=False))
         chunks = np.array_split(sub, cores * 4)
@@ -548,8 +555,6 @@ def cpu_image_run(pool, cores):
 def run_image(args):
     small = args.case == 'image-small'
     pool = cores = None
-    if not args.no_cpu_baseline:
-        pool, cores = make_pool()
     import torch
     from kgeo_gb300.image_grad import config_params, equatorial_image
     grid = 128 if small else IMG_GRID
@@ -630,8 +635,10 @@ def run_image(args):
     if ADJ_FLOP_PER_PIXEL and fp64_peak:
         roof['achieved'] = ADJ_FLOP_PER_PIXEL * npix / t_adj / 1e12
         roof['frac'] = roof['achieved'] / fp64_peak
-    cpu = cpu_image_run(pool, cores) if pool is not None else None
-    if pool is not None:
+    cpu = None
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()  # spawned after the GPU timings
+        cpu = cpu_image_run(pool, cores)
         pool.close()
     line = {
         'metric': 'image+grad/s: configuration-5 equatorial image (512x512, n=0..2) + adjoint gradient wrt '
@@ -702,8 +709,6 @@ def _cpu_pol_chunk(args):
 def run_polimage(args):
     small = args.case == 'polimage-small'
     pool = cores = None
-    if not args.no_cpu_baseline:
-        pool, cores = make_pool()
     import torch
     from kgeo_gb300.equatorial_images import emission_model, image_device, image_options, make_image
     nx = 160 if small else POL_NX
@@ -765,7 +770,8 @@ def run_polimage(args):
         # like a dfma, so the pipe-instruction bound is fp64_peak / 2 instructions per second
         roof['fp64_pipe_frac'] = POL_FP64_INST_PER_PIXEL * npix / t_step / (fp64_peak * 1e12 / 2)
     cpu = None
-    if pool is not None:
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()  # spawned after the GPU timings
         idx = np.arange(0, npix, max(1, npix // CPU_POL_SAMPLE))[:CPU_POL_SAMPLE]
         chunks = np.array_split(idx, cores * 2)
         t0 = time.time()
@@ -855,8 +861,6 @@ def _cpu_lib_chunk(items):
 def run_library(args):
     small = args.case == 'library-small'
     pool = cores = None
-    if not args.no_cpu_baseline:
-        pool, cores = make_pool()
     import torch
     from kgeo_gb300.equatorial_lensing import rho_of_req_device
     curves, vp = library_workload(small)
@@ -890,7 +894,8 @@ def run_library(args):
         tabs = make_library(S.flatten(), I.flatten(), which='rh', mmax=5)
     t_e2e = (time.perf_counter() - t0) / args.steps
     cpu = None
-    if pool is not None:
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()  # spawned after the GPU timings
         rng = np.random.default_rng(0)
         pick = rng.choice(nroots, size=CPU_LIB_SAMPLE, replace=False)
         items = [curves[k // vp.size][:4] + (float(vp[k % vp.size]),) for k in pick]
@@ -952,8 +957,6 @@ def _cpu_jet_chunk(args):
 def run_jet(args):
     small = args.case == 'jet-small'
     pool = cores = None
-    if not args.no_cpu_baseline:
-        pool, cores = make_pool()
     import torch
     from kgeo_gb300 import device as dev
     from kgeo_gb300 import solver
@@ -998,7 +1001,8 @@ def run_jet(args):
         solver.findroot(geo, c['psitarget'], A, B, R_O, th, c['a'], c['ngeo'], model=c['model'], neqmax=c['neqmax'])
     t_e2e = (time.perf_counter() - t0) / args.steps
     cpu = None
-    if pool is not None:
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()  # spawned after the GPU timings
         idx = np.arange(0, A.size, max(1, A.size // CPU_JET_SAMPLE))[:CPU_JET_SAMPLE]
         chunks = np.array_split(idx, cores * 2)
         t0 = time.time()
@@ -1055,8 +1059,6 @@ def _cpu_stokes_chunk(args):
 def run_stokes(args):
     small = args.case == 'stokes-small'
     pool = cores = None
-    if not args.no_cpu_baseline:
-        pool, cores = make_pool()
     import torch
     from kgeo_gb300 import device as dev
     from kgeo_gb300 import off_eq, solver
@@ -1109,7 +1111,8 @@ def run_stokes(args):
         off_eq.getstokes(c['psitarget'], A2, B2, R_O, th, c['a'], c['ngeo'], **kw)
     t_e2e = (time.perf_counter() - t0) / args.steps
     cpu = None
-    if pool is not None:
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()  # spawned after the GPU timings
         idx = np.arange(0, A.size, max(1, A.size // CPU_STOKES_SAMPLE))[:CPU_STOKES_SAMPLE]
         chunks = np.array_split(idx, cores * 2)
         # the density's stagnation radius comes from the first crossing of the first guess row:
@@ -1184,8 +1187,6 @@ def _oracle_batch_chunk(args):
 def run_batch(args):
     small = args.case == 'batch-small'
     pool = cores = None
-    if not args.no_cpu_baseline:
-        pool, cores = make_pool()
     import torch
     from kgeo_gb300 import device as dev
     from kgeo_gb300.batch import BatchPlan
@@ -1262,7 +1263,8 @@ def run_batch(args):
     t_fp64 = e0.elapsed_time(e1) / 1e3
     plan_d.close()
     cpu = None
-    if pool is not None:
+    if not args.no_cpu_baseline:
+        pool, cores = make_pool()  # spawned after the GPU timings
         rng = np.random.default_rng(0)
         idx = np.sort(rng.choice(n_rays, n_rays // 256, replace=False))
         img_of = np.searchsorted(off, idx, side='right') - 1
