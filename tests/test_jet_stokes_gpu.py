@@ -115,3 +115,23 @@ def test_getstokes_unsupported_models_raise():
         off_eq.getstokes(0.5, A, B, 1.e4, 0.5, 0.5, 50, model='power', pval=1.0)
     with pytest.raises(NotImplementedError):
         off_eq.getstokes(0.5, A, B, 1.e4, 0.5, 0.5, 50, model='mono', gammamax=5.0)
+
+
+def test_getstokes_return_forms():
+    """retvals=False returns the four images; sumsubring=False the per-crossing Stokes, neq,
+    crossings and the guesses' shape, whose row sums are the total image."""
+    from kgeo_gb300 import off_eq
+    A, B = grid()
+    kw = dict(model='mono', neqmax=2, nu_parallel=0.2, sigma=2.0)
+    imgs = off_eq.getstokes(0.4, A, B, 1.e4, 60 * DEG, 0.5, 200, **kw)
+    assert len(imgs) == 4 and all(x.shape == (3, 16, 16) for x in imgs)
+    Ic, Qc, Uc, neq, r, th, shape = off_eq.getstokes(0.4, A, B, 1.e4, 60 * DEG, 0.5, 200, sumsubring=False, **kw)
+    G = shape[0]
+    assert Ic.shape == (G * A.size,) and neq.shape == r.shape == th.shape == Ic.shape
+    for c, img in zip((Ic, Qc, Uc), imgs[:3]):
+        tot = c.reshape(G, -1).sum(axis=0).reshape(A.shape)
+        assert np.allclose(tot, img[-1], rtol=1e-12, atol=1e-12 * np.max(np.abs(imgs[0])))
+        for n in range(2):
+            sub = np.where(neq == n, c, 0).reshape(G, -1).sum(axis=0).reshape(A.shape)
+            assert np.allclose(sub, img[n], rtol=1e-12, atol=1e-12 * np.max(np.abs(imgs[0])))
+    assert np.all(Ic[r == 0] == 0)
