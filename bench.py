@@ -1019,7 +1019,7 @@ def run_jet(args):
         'dtype': 'f64', 'data': 'synthetic: uniform image-plane grid over [-10, 10] M',
         'config': {'workload': 'a=0.9, theta_o=17 deg, r_o=1e4, %dx%d, ngeo=200, BZ paraboloid psi=1, neqmax=1' % (n, n),
                    'guesses': list(g.shape), 'solves': nsolve, 'converged': conv, 'case': args.case,
-                   'l2': 'compute-bound (per-ray records 584 B / pixel)'},
+                   'l2': 'compute-bound (per-ray records 624 B / pixel)'},
         'roofline': roofline_fp64('jet_solve_kernel', t_step, nsolve, JET_FLOP_PER_SOLVE, JET_FP64_INST_PER_SOLVE,
                                   'solve'),
         'cpu_baseline': cpu,

@@ -58,6 +58,8 @@ enum RecField : int {
   // radial, case-specific
   R_C0, R_C1, R_C2, R_C3, R_C4, R_C5, R_C6, R_C7, R_C8, R_C9, R_C10, R_C11, R_C12, R_C13,
   R_C14, R_C15, R_C16, R_C17, R_C18, R_C19,
+  // per-ray factors the sample kernels would otherwise recompute at every sample
+  R_C20, R_C21, R_C22, R_C23, R_C24,
   // one step of the even Mino grid: theta Jacobi values / integrals at the step, r ditto
   S_TSN, S_TCN, S_TDN, S_TE, S_TPI, S_TC,
   S_RSN, S_RCN, S_RDN, S_RE, S_RP0, S_RP1, S_RP2, S_RC0, S_RC1, S_RC2,
@@ -545,6 +547,14 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     f[R_C13] = aa1;
     f[R_C14] = g0 / (a2i - a2i * g0 * x4rp);
     f[R_C15] = g0 / (a2i - a2i * g0 * x4rm);
+    const double g4[3] = {g0, gp, gm};
+    for (int i = 0; i < 3; ++i) {  // p2 of S1_S2 for g0, gp, gm
+      const double gg = g4[i] * g4[i];
+      f[R_C20 + i] = sqrt((1 + gg) / (1 - k4 + gg));
+    }
+    const double g02 = g0 * g0, g02p1 = 1 + g02, g02j = 1 - k4 + g02;
+    f[R_C23] = -1.0 / (g02p1 * g02j);           // S2 = S2a f[R_C23] + S1_0 f[R_C24]
+    f[R_C24] = 1. / g02p1 + (1 - k4) / g02j;
   }
   if (c3) {
     rcase = RCASE_3;
@@ -606,7 +616,7 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     f[R_C17] = (BB * rrm2 + AA * rrm1);
     f[R_C18] = sqrt((a0s - 1) / (k3 + (1 - k3) * a0s));  // p1 of R1_R2 for al0, alp, alm
     f[R_C19] = sqrt((aps - 1) / (k3 + (1 - k3) * aps));
-    // p1 of alm is evaluated per sample (R_C slots are full)
+    f[R_C20] = sqrt((ams - 1) / (k3 + (1 - k3) * ams));
   }
   if (c2) {
     rcase = RCASE_2;
@@ -657,6 +667,8 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     f[R_C16] = rr31;
     f[R_C17] = rr41;
     f[R_C18] = rr43;
+    f[R_C20] = 1.0 / rrp3;
+    f[R_C21] = 1.0 / rrm3;
   }
   rec->code = rcase | (th << 4) | ((kk0 ? 1 : 0) << 8) | ((o.minspin ? 1 : 0) << 9);
   return flags;
@@ -989,8 +1001,8 @@ KG_HD RadialOut radial_assemble(const FV& f, int code, double tau, const RadialS
     double Pi_m = f[R_C11] * (st.P[2] - f[R_C7]);
     o.I1 = rr3 * (-tau) + rr43 * Pi_1;
     o.I2 = H - f[R_C15] * (-tau) - Eterm;
-    o.Ip = tau / f[R_C13] - Pi_p;
-    o.Im = tau / f[R_C14] - Pi_m;
+    o.Ip = tau * f[R_C20] - Pi_p;
+    o.Im = tau * f[R_C21] - Pi_m;
     return o;
   }
   if (rc == RCASE_3) {
@@ -1004,7 +1016,7 @@ KG_HD RadialOut radial_assemble(const FV& f, int code, double tau, const RadialS
     for (int i = 0; i < 3; ++i) {
       double a_ = al[i];
       double al2 = a_ * a_;
-      double p1 = (i == 0) ? f[R_C18] : (i == 1 ? f[R_C19] : sqrt((al2 - 1) / (k + (1 - k) * al2)));
+      double p1 = f[R_C18 + i];
       double f1 = 0.5 * p1 * log(fabs((p1 * dnX + snX) / (p1 * dnX - snX)));
       R1[i] = (st.P[i] - a_ * f1) / (1 - al2);
       (void)nn;
@@ -1040,15 +1052,14 @@ KG_HD RadialOut radial_assemble(const FV& f, int code, double tau, const RadialS
       double al = gs[i];
       double al2 = al * al;
       double al2p1 = 1 + al2;
-      double al2j = 1 - k + al2;
-      double p2 = sqrt(al2p1 / al2j);
+      double p2 = f[R_C20 + i];
       double f2 = 0.5 * p2 * log(fabs(((1 - p2) * (1 + p2 * dnX)) / ((1 + p2) * (1 - p2 * dnX))));
       S1[i] = (st.X + al2 * st.P[i] - al * f2) / al2p1;
     }
-    double al2 = g0 * g0, al2p1 = 1 + al2, al2j = 1 - k + al2;
+    double al2 = g0 * g0;
     double S2a = (1 - k) * st.X + al2 * st.E + al2 * dnX * (g0 - sc) / (1 + g0 * sc) - al2 * g0;
-    S2a = -S2a / (al2p1 * al2j);
-    double S2b = S1[0] * (1. / al2p1 + (1 - k) / al2j);
+    S2a = S2a * f[R_C23];
+    double S2b = S1[0] * f[R_C24];
     double S2 = S2a + S2b;
     double Pi_1 = f[R_C9] * (S1[0] - f[R_C5]);
     double Pi_2 = f[R_C10] * (S2 - f[R_C6]);
