@@ -102,3 +102,22 @@ def test_host_emission_matches_oracle(i):
     scale = np.max(np.abs(Io))
     for h, o in ((Ih, Io), (Qh, Qo), (Uh, Uo)):
         assert np.max(np.abs(h - o)) <= 1e-10 * scale
+
+
+def test_dropin_argument_handling_before_any_launch():
+    """off_eq.getstokes refuses what the GPU path does not cover, and raises the reference's
+    errors, before touching the GPU."""
+    from kgeo_gb300 import off_eq
+    x = np.linspace(-8, 8, 4)
+    A, B = np.meshgrid(x, x)
+    for kw in (dict(model='para'), dict(model='power', pval=0.5), dict(model='mono', gammamax=3.0),
+               dict(model='mono', retsin=True), dict(model='mono', nu_parallel='FF')):
+        with pytest.raises(NotImplementedError):
+            off_eq.getstokes(0.4, A, B, 1.e4, 1.0, 0.5, 50, **kw)
+    with pytest.raises(Exception, match=r"nu_parallel should be in the range \(-1,1\)"):
+        off_eq.getstokes(0.4, A, B, 1.e4, 1.0, 0.5, 50, model='mono', nu_parallel=1.5)
+    with pytest.raises(IndexError):
+        off_eq._stagnation_error(1)
+    with pytest.raises(np.linalg.LinAlgError):
+        off_eq._stagnation_error(2)
+    off_eq._stagnation_error(0)
