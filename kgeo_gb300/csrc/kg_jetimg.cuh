@@ -264,8 +264,8 @@ KG_HD Cplx aberth_correction(const double* c, const Cplx* z, int i) {
   return w;
 }
 
-// Start of the iteration: five points on a circle of twice the Fujiwara bound (> every root);
-// 0 when the start is unusable.
+// Start of the iteration: five points on a circle of radius 2 max_k |c_k / c_5|^(1 / (5 - k)),
+// the Fujiwara bound (>= every root's modulus); 0 when the start is unusable.
 KG_HD double aberth_radius(const double* c) {
   double rad = 0.0;
   for (int k = 0; k < 5; ++k) rad = fmax(rad, pow(fabs(c[k] / c[5]), 1.0 / (5 - k)));
