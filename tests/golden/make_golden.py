@@ -127,10 +127,58 @@ def grid(lo, hi, n):
     return A.flatten(), B.flatten()
 
 
-def main(path):
+BAND_SAMPLES = np.r_[0:256:8, 255]   # samples of the ngeo = 256 band traces kept in the fixture
+
+
+def band_rays(ref, a, th_o, n_angles, offsets, n_curve=100000):
+    """Pixels at the given radial offsets (M) from the critical curve at n_angles screen
+    angles, the construction of the 2048^2-plus-band workload's polar band; the curve is the
+    reference's critical_curve (kgeo/equatorial_lensing.py:260-289)."""
+    al, be = ref.lensing.critical_curve(a, th_o, n=n_curve)
+    ang = np.arctan2(be, al)
+    rad = np.hypot(al, be)
+    order = np.argsort(ang)
+    phis = np.linspace(-np.pi, np.pi, n_angles, endpoint=False)
+    rc = np.interp(phis, ang[order], rad[order], period=2 * np.pi)
+    R = rc[None, :] + np.asarray(offsets)[:, None]
+    return (R * np.cos(phis)[None, :]).flatten(), (R * np.sin(phis)[None, :]).flatten()
+
+
+def hot_path_edges(ref):
+    """Rays of the rarer radial and angular classes: radial region II (four real roots, the
+    ray ends on the horizon; kgeo/kerr_raytracing_utils.py:375, :485-515), the no-real-root
+    case 4 with vortical theta motion, and pixels next to the critical curve."""
+    deg = np.pi / 180.
+
+    def patch(a, th, alo, ahi, blo, bhi, n=12):
+        A, B = np.meshgrid(np.linspace(alo, ahi, n), np.linspace(blo, bhi, n))
+        return trace_case(ref, a, 1.e4, th * deg, A.flatten(), B.flatten(), 48)
+    save('trace_region2_a094_i81', patch(0.94, 81.3, -1.6, -1.1, -0.5, 0.5))
+    save('trace_region2_a099_i89', patch(0.99, 89.0, -1.9, -1.0, -0.9, 0.9))
+    save('trace_region2_a081_i99', patch(0.8116436987218719, 98.67750919956, -1.1, -0.95, -0.16, 0.16))
+    save('trace_case4_a094_i45', patch(0.94, 45.0, -1.2, 1.2, -1.2, 1.2))
+    save('trace_case4_a086_i4', patch(0.8556894680343942, 3.955530626880863, -1.6, 1.6, -1.6, 1.6))
+
+    # the critical-curve band of the mixed-precision workload (a = 0.94, theta_o = 17 deg,
+    # offsets from linspace(-0.05, 0.05, 256), the ones nearest the curve included), ngeo = 256,
+    # every 8th sample and the last one stored
+    offs = np.linspace(-0.05, 0.05, 256)[[0, 64, 120, 126, 127, 128, 129, 135, 191, 255]]
+    A, B = band_rays(ref, 0.94, 17 * deg, 32, offs)
+    d = trace_case(ref, 0.94, 1.e4, 17 * deg, A, B, 256)
+    for k in ('mino', 'sig', 't', 'r', 'th', 'ph'):
+        d[k] = d[k][BAND_SAMPLES]
+    d.update(samples=BAND_SAMPLES, offsets=offs, n_angles=32)
+    save('band_a094_i17', d)
+
+
+def main(path, only=None):
     warnings.filterwarnings('ignore')
     ref = import_reference(path)
     deg = np.pi / 180.
+    if only == 'edges':
+        hot_path_edges(ref)
+        return
+    hot_path_edges(ref)
 
     # configuration-1 geometry on a coarser grid
     A, B = grid(-8, 8, 16)
@@ -418,4 +466,6 @@ def main(path):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    # python tests/golden/make_golden.py [path-to-kgeo-checkout] [edges]
+    # ('edges' regenerates only the fixtures of hot_path_edges)
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference', sys.argv[2] if len(sys.argv) > 2 else None)

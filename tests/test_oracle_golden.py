@@ -141,3 +141,17 @@ def test_oracle_n_angular_turnings(golden):
         n1 = ko.n_angular_turnings(float(a), float(th) * np.pi / 180, A, B, tau[2])
         assert np.array_equal(n, g['n%d' % i], equal_nan=True), i
         assert np.array_equal(n1, g['n1_%d' % i], equal_nan=True), i
+
+
+def test_band_trace_matches_reference(golden):
+    """Rays 2e-4 to 5e-2 M from the critical curve (a = 0.94, theta_o = 17 deg, ngeo = 256): the
+    fixture keeps every 8th Mino sample and the last."""
+    g = golden('band_a094_i17')
+    a, r_o, th_o = float(g['a']), float(g['r_o']), float(g['th_o'])
+    out = ko.raytrace(a, r_o, th_o, g['alpha'], g['beta'], int(g['ngeo']))
+    assert np.array_equal(out['rclass'], g['rclass'])
+    assert np.array_equal(out['thclass'], g['thclass'])
+    idx = g['samples']
+    close(out['mino_times'][idx], g['mino'])
+    for k_ours, k_ref in [('t', 't'), ('r', 'r'), ('th', 'th'), ('ph', 'ph'), ('affine_times', 'sig')]:
+        close(out[k_ours][idx], g[k_ref])
