@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from parity import check_trace
+from parity import check_trace, lambda_eta_sensitivity
 
 pytestmark = pytest.mark.gpu
 
@@ -276,30 +276,95 @@ def test_recurrence_matches_independent_samples(kg, chunk):
     check_trace(h1, h0, 1.e4, prep.rclass.cpu().numpy(), 'chunk%d' % chunk, rho=rho)
 
 
-@pytest.mark.parametrize('geom', [(0.94, 17.0), (0.3, 70.0), (0.7, 5.0)])
+@pytest.mark.parametrize('geom', [(0.94, 17.0), (0.3, 70.0), (0.7, 5.0), 'band'])
 def test_mixed_precision_error_bars(kg, geom):
-    """Mixed-precision (float-float) recurrence against the FP64 oracle: r 1e-9, theta 5e-7,
-    phi 1e-6 (relative, floor 1), t and sigma 1e-7 of r_o; within rho = |1 - n sn^2| of an
-    elliptic-Pi pole the bar widens to 1e-12 / rho (the float-float state's rounding amplified by
-    the pole (~1e-12 after a 256-step chain), as the FP64 bars widen by 10 eps / rho); the last sample is
-    checked at the FP64 path's bar (it is evaluated in FP64)."""
+    """Mixed-precision (float-float) recurrence against the FP64 oracle: r 1e-8, theta 5e-7,
+    phi 1e-6 (relative, floor 1), t and sigma 1e-7 of r_o, on 40x40 grids and on rays of the
+    critical-curve band (0.94, 17 deg: 256 angles x the 16 offsets nearest the curve). Only the
+    FP64 path's pole rule widens a bar (10 eps / rho, rho = |1 - n sn^2| the distance to an
+    elliptic-Pi pole): within 1e-5 of a pole the mixed kernel re-seeds from the FP64 direct
+    evaluation, so no sample is left to the float-float state's pole-amplified rounding."""
     import torch
     from oracle import kgeo_oracle as ko
     from kgeo_gb300 import device as dev
-    from parity import rel_err
-    a, th = geom[0], geom[1] * np.pi / 180
-    x = np.linspace(-10, 10, 40)
-    A, B = (v.flatten() for v in np.meshgrid(x, x))
+    from parity import rel_err, EPS
+    if geom == 'band':
+        from kgeo_gb300.equatorial_lensing import critical_band
+        a, th = 0.94, 17 * np.pi / 180
+        A, B = critical_band(a, th, n_angles=256, n_radii=256)
+        A, B = (v.reshape(256, 256)[120:136].flatten() for v in (A, B))
+    else:
+        a, th = geom[0], geom[1] * np.pi / 180
+        x = np.linspace(-10, 10, 40)
+        A, B = (v.flatten() for v in np.meshgrid(x, x))
     ref = ko.raytrace(a, 1.e4, th, A, B, 256)
     prep = dev.PreparedRays(a, 1.e4, th, dev.as_device(A), dev.as_device(B), ngeo=256)
     out = prep.samples(prep.alloc(fill=float('nan')), mixed=True)
     torch.cuda.synchronize()
     got = {k: v.cpu().numpy() for k, v in out.items()}
     assert np.array_equal(np.isfinite(got['ph']), np.isfinite(ref['ph']))
-    last = np.zeros(ref['r'].shape, bool)
-    last[-1] = np.isin(ref['rclass'], (2, 3, 4))
     rho = ko.pole_distance(a, 1.e4, th, A, B, ref['mino_times'])
-    for k, rk, scale, bar in (('r', 'r', 1e-300, 1e-9), ('th', 'th', 1.0, 5e-7), ('ph', 'ph', 1.0, 1e-6),
+    for k, rk, scale, bar in (('r', 'r', 1e-300, 1e-8), ('th', 'th', 1.0, 5e-7), ('ph', 'ph', 1.0, 1e-6),
                               ('t', 't', 1.e4, 1e-7), ('sig', 'affine_times', 1.e4, 1e-7)):
-        e = rel_err(got[k], ref[rk], scale) / np.maximum(bar, 1e-12 / rho)
-        assert e[~last].max() <= 1.0, (k, e[~last].max())
+        e = rel_err(got[k], ref[rk], scale) / np.maximum(bar, 10 * EPS / rho)
+        assert e.max() <= 1.0, (k, e.max())
+
+
+def test_band_fixture_vs_reference(kg, golden):
+    """Rays 2e-4 to 5e-2 M from the critical curve (a = 0.94, theta_o = 17 deg, ngeo = 256),
+    against the reference's samples kept in the fixture (every 8th and the last)."""
+    from oracle import kgeo_oracle as ko
+    g = golden('band_a094_i17')
+    a, r_o, th_o = float(g['a']), float(g['r_o']), float(g['th_o'])
+    got = _run(kg, a, r_o, th_o, g['alpha'], g['beta'], int(g['ngeo']))
+    idx = g['samples']
+    np.testing.assert_allclose(got['mino'][idx], g['mino'], rtol=1e-12, atol=0)
+    full_tau = got['mino']
+    rho = ko.pole_distance(a, r_o, th_o, g['alpha'], g['beta'], full_tau)[idx]
+    sens = lambda_eta_sensitivity(a, r_o, th_o, g['alpha'], g['beta'], ngeo=int(g['ngeo']))
+    sub = lambda cols: {k: v[idx] for k, v in sens(cols).items()}  # noqa: E731
+    check_trace({k: got[k][idx] for k in ('t', 'r', 'th', 'ph', 'sig')},
+                dict(t=g['t'], r=g['r'], th=g['th'], ph=g['ph'], sig=g['sig']), r_o, g['rclass'], 'band-fixture',
+                rho=rho, sens=sub)
+
+
+def test_band_vs_oracle(kg):
+    """The critical-curve band of the 2048^2-plus-band workload (a = 0.94, theta_o = 17 deg,
+    ngeo = 256) at 256 screen angles and the 16 radial offsets of linspace(-0.05, 0.05, 256)
+    nearest the curve (|offset| 2e-4 to 3e-3 M), FP64 recurrence against the oracle."""
+    import torch
+    from oracle import kgeo_oracle as ko
+    from kgeo_gb300.equatorial_lensing import critical_band
+    A, B = critical_band(0.94, 17 * np.pi / 180, n_angles=256, n_radii=256)
+    A, B = (v.reshape(256, 256)[120:136].flatten() for v in (A, B))
+    a, r_o, th_o = 0.94, 1.e4, 17 * np.pi / 180
+    ref = ko.raytrace(a, r_o, th_o, A, B, 256)
+    got = _run(kg, a, r_o, th_o, A, B, 256)
+    torch.cuda.synchronize()
+    refd = dict(t=ref['t'], r=ref['r'], th=ref['th'], ph=ref['ph'], sig=ref['affine_times'])
+    rho = ko.pole_distance(a, r_o, th_o, A, B, ref['mino_times'])
+    check_trace(got, refd, r_o, ref['rclass'], 'band', rho=rho,
+                sens=lambda_eta_sensitivity(a, r_o, th_o, A, B, ngeo=256))
+
+
+@pytest.mark.parametrize('name', ['trace_region2_a094_i81', 'trace_region2_a099_i89', 'trace_region2_a081_i99'])
+def test_region2_r_equatorial_vs_oracle(kg, golden, name):
+    """Radial region II rays (four real roots, the ray ends on the horizon): r_s, Ir, Imax and
+    Nmax of orders 0..2 against the oracle on the fixture's pixels."""
+    from oracle import kgeo_oracle as ko
+    from kgeo_gb300 import equatorial_lensing as el
+    g = golden(name)
+    a, r_o, th_o = float(g['a']), float(g['r_o']), float(g['th_o'])
+    assert (g['rclass'] == 2).sum() >= 20
+    for m in range(3):
+        r_s, Ir, Imax, Nmax = el.r_equatorial(a, r_o, th_o, m, g['alpha'], g['beta'])
+        rr, ir, imax, nmax = ko.r_equatorial(a, r_o, th_o, m, g['alpha'], g['beta'])
+        assert np.array_equal(Nmax, nmax)
+        assert np.array_equal(r_s == 0, rr == 0)
+        np.testing.assert_allclose(r_s, rr, rtol=1e-10, atol=0)
+        np.testing.assert_allclose(Ir, ir, rtol=1e-10, atol=1e-12)
+        np.testing.assert_allclose(Imax, imax, rtol=1e-10, atol=1e-12)
+    # the fixture's Mino totals are the reference's Imax of these rays
+    got = kg.raytrace_ana(a=a, observer_coords=[0, r_o, th_o, 0], image_coords=[g['alpha'], g['beta']],
+                          ngeo=int(g['ngeo']), plotdata=False)
+    np.testing.assert_allclose(got.tautot, g['tau_tot'], rtol=1e-12, atol=0)
