@@ -59,6 +59,12 @@ typedef enum {
 /* |a| < 1e-4 and some pixel has eta == 0: the reference raises
  * "below MINSPIN but there are eta<0 points in th_integrate!" (kgeo/kerr_raytracing_ana.py:301-302) */
 #define KGEO_FLAG_MINSPIN_VORTICAL 8u
+/* An iterative loop of the elliptic arithmetic (Carlson duplication, descending Landen
+ * transformation) stopped at its iteration cap without meeting its convergence test; the
+ * affected samples may be inaccurate. The reference surfaces such failures as NaN or as an
+ * exception (kgeo/gsl_ellip_binding.py:92-136); the caps are far above FP64 convergence, so
+ * on finite inputs this bit is not expected. */
+#define KGEO_FLAG_LOOP_CAP 16u
 
 /* Observer: spin a (|a| < 1), radius r_o (>= 100, may be +inf), inclination th_o in (0, pi) minus pi/2. */
 typedef struct {
@@ -411,6 +417,8 @@ typedef struct kgeo_batch_plan kgeo_batch_plan;
 int kgeo_batch_create(const kgeo_batch_image* images, int32_t nimg, int32_t precision, kgeo_batch_plan** plan);
 void kgeo_batch_destroy(kgeo_batch_plan* plan);
 int kgeo_batch_sizes(const kgeo_batch_plan* plan, int64_t* n_rays, int64_t* n_samples, size_t* workspace_bytes);
+/* kgeo_batch_bind: out->flags, when not NULL, receives nimg words after each run (image i's
+ * KGEO_FLAG_* bits). */
 int kgeo_batch_bind(kgeo_batch_plan* plan, const double* alpha, const double* beta, kgeo_geodesics* out,
                     void* workspace, size_t workspace_bytes);
 int kgeo_batch_get_config(const kgeo_batch_plan* plan, kgeo_batch_config* cfg, int32_t* tuned);
@@ -435,6 +443,17 @@ int kgeo_batch_graph_launch(kgeo_batch_plan* plan, void* stream);
 #define KGEO_NOALLOC_MAX_PIXELS 16384
 int kgeo_raytrace_noalloc(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,
                           int32_t ngeo, double maxtaufrac, kgeo_geodesics* out, void* stream);
+
+/* ellip_pi_arr(n, phi, m) (kgeo/scipy_ellip_binding.py:87-237): the incomplete elliptic
+ * integral of the third kind Pi(n; phi | m) in Abramowitz & Stegun's convention, with the
+ * reference adapter's special cases (phi ~ 0, m < -1e14, 1 - m sin^2 < 0, |phi| > pi/2 with
+ * m >= 1 or n = 1, 1 - n sin^2 = 0, n = inf) and its periodic continuation, evaluated on the
+ * device exactly as the kernels evaluate it: `form` 0 = the per-ray setup's arithmetic
+ * (FMA contraction off), 1 = the direct sample evaluators' (contraction on), 2 = the
+ * standalone adapter kg::ellip_pi_ref. n, phi, m, out: N doubles (device memory); the
+ * caller broadcasts. Stream-ordered, allocates nothing. */
+int kgeo_ellip_pi(const double* n, const double* phi, const double* m, int64_t N, int32_t form, double* out,
+                  void* stream);
 
 /* Measurement helper (no counterpart in the reference): runs a fixed FP64 fused
  * multiply-add loop on every SM and returns the achieved FP64 rate in TFLOP/s (an FMA

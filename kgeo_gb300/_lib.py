@@ -140,6 +140,7 @@ SIGNATURES = {
     'kgeo_batch_autotune': (c_int, [c_void_p, c_int32, c_void_p, ctypes.POINTER(BatchConfig)]),
     'kgeo_batch_run': (c_int, [c_void_p, c_void_p]),
     'kgeo_batch_graph_launch': (c_int, [c_void_p, c_void_p]),
+    'kgeo_ellip_pi': (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p]),
     'kgeo_status_string': (ctypes.c_char_p, [c_int]),
     'kgeo_abi_version': (c_int, []),
 }
@@ -150,6 +151,7 @@ FLAG_ANY_ETA_POS = 1
 FLAG_ANY_ETA_NONPOS = 2
 FLAG_ANY_STEP_ZERO = 4
 FLAG_MINSPIN_VORTICAL = 8
+FLAG_LOOP_CAP = 16
 
 _lib = None
 

@@ -9,6 +9,8 @@
 
 using namespace kg;
 
+static_assert(KGEO_FLAG_LOOP_CAP == kg::FLAG_LOOP_CAP, "flag bit of the C ABI and the kernels differ");
+
 namespace {
 
 // Observer checks with the reference's rules (kgeo/kerr_raytracing_ana.py:59-65).
@@ -777,6 +779,17 @@ const char* kgeo_status_string(int status) {
     case KGEO_ERR_SOLVER: return "root solver arguments out of range (xtol > 0, rtol >= 4 eps, maxiter >= 0)";
     default: return "unknown status";
   }
+}
+
+int kgeo_ellip_pi(const double* n, const double* phi, const double* m, int64_t N, int32_t form, double* out,
+                  void* stream) {
+  if (N < 0) return KGEO_ERR_LENGTHS;
+  if (form < 0 || form > 2) return KGEO_ERR_MODEL;
+  if (N > 0 && (!n || !phi || !m || !out)) return KGEO_ERR_NULL;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = form == 0 ? launch_ellip_pi_setup(n, phi, m, N, out, s)
+                            : launch_ellip_pi_samples(n, phi, m, N, form, out, s);
+  return e == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
 }
 
 int kgeo_abi_version(void) { return KGEO_ABI_VERSION; }

@@ -82,7 +82,7 @@ struct SampleArgs {
   int64_t c_begin;      // recurrence kernel: chunks [c_begin, c_end) only (c_end < 0: to the last)
   int64_t c_end;
   int64_t row0;         // sample g is stored in row g - row0 of the outputs
-  const uint32_t* flags;
+  uint32_t* flags;      // launch flags: read at start; FLAG_LOOP_CAP is OR-ed in
   double* t;
   double* r;
   double* th;
@@ -323,5 +323,9 @@ cudaError_t launch_image_adjoint(const ImageAdjointArgs& a, cudaStream_t s);
 cudaError_t launch_equatorial(const EquatorialArgs& a, cudaStream_t s);
 cudaError_t launch_crossings(const CrossingArgs& a, cudaStream_t s);
 cudaError_t launch_samples(const SampleArgs& a, cudaStream_t s);
+cudaError_t launch_ellip_pi_setup(const double* n, const double* phi, const double* m, int64_t N, double* out,
+                                  cudaStream_t s);
+cudaError_t launch_ellip_pi_samples(const double* n, const double* phi, const double* m, int64_t N, int form,
+                                    double* out, cudaStream_t s);
 
 }  // namespace kg

@@ -8,6 +8,7 @@ namespace kg {
 
 __global__ void __launch_bounds__(256) samples_kernel(SampleArgs a) {
   const uint32_t fl = *a.flags;
+  loop_cap_begin();
   const bool ordinary_active = (fl & FLAG_ANY_ETA_POS) != 0;
   const bool step_zero = (fl & FLAG_ANY_STEP_ZERO) != 0;
   const int64_t total = a.npix * a.nsamp;
@@ -38,6 +39,7 @@ __global__ void __launch_bounds__(256) samples_kernel(SampleArgs a) {
     }
     if (a.mino) a.mino[o] = tau;
   }
+  loop_cap_end(a.flags);
 }
 
 // Even Mino grid: one thread per (pixel, chunk of `chunk` consecutive samples), items
@@ -51,6 +53,7 @@ __device__ __forceinline__ FFRay* ffray_slot() { return reinterpret_cast<FFRay*>
 template <bool MIXED, bool RTH>
 __global__ void __launch_bounds__(256) stepped_kernel(SampleArgs a) {
   const uint32_t fl = *a.flags;
+  loop_cap_begin();
   const bool ordinary_active = (fl & FLAG_ANY_ETA_POS) != 0;
   const bool step_zero = (fl & FLAG_ANY_STEP_ZERO) != 0;
   const int64_t chunk = a.chunk;
@@ -91,6 +94,32 @@ __global__ void __launch_bounds__(256) stepped_kernel(SampleArgs a) {
       ray_chunk(a.obs, f, code, g0, g1, a.nsamp, ordinary_active, step_zero, emit);
     }
   }
+  loop_cap_end(a.flags);
+}
+
+// Pi(n; phi | m) as the sample kernels' translation unit compiles it (FMA contraction on):
+// form 1 = ellip_set_at (the direct sample evaluators' path), form 2 = ellip_pi_ref.
+__global__ void __launch_bounds__(256) ellip_pi_samples_kernel(const double* n, const double* phi, const double* m,
+                                                               int64_t N, int form, double* out) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+    const double ni = n[i], mi = m[i];
+    if (form == 2) {
+      out[i] = ellip_pi_ref(ni, phi[i], mi);
+    } else {
+      const EllipSet<1> comp = ellip_set_at<1>(HALFPI, mi, &ni, nullptr);
+      out[i] = ellip_set_at<1>(phi[i], mi, &ni, &comp).P[0];
+    }
+  }
+}
+
+cudaError_t launch_ellip_pi_samples(const double* n, const double* phi, const double* m, int64_t N, int form,
+                                    double* out, cudaStream_t s) {
+  if (N <= 0) return cudaSuccess;
+  int64_t grid = (N + 255) / 256;
+  if (grid > 152 * 16) grid = 152 * 16;
+  ellip_pi_samples_kernel<<<(unsigned)grid, 256, 0, s>>>(n, phi, m, N, form, out);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_samples(const SampleArgs& a, cudaStream_t s) {
@@ -142,6 +171,7 @@ template <bool MIXED>
 __global__ void __launch_bounds__(256) batch_samples_kernel(BatchArgs a) {
   __shared__ long long tile_id;
   const int64_t total = a.item_off[a.nimg];
+  if (threadIdx.x == 0) kg_loop_cap_word = 0u;  // ordered by the first tile's barrier
   for (;;) {
     if (threadIdx.x == 0) tile_id = (long long)atomicAdd(a.work, 1ull);
     __syncthreads();
@@ -156,7 +186,7 @@ __global__ void __launch_bounds__(256) batch_samples_kernel(BatchArgs a) {
       const int64_t local = item - a.item_off[im];
       const int64_t c = local / B.npix;
       const int64_t p = __ldg(a.perm + B.pix_off + (local - c * B.npix));
-      const uint32_t fl = __ldg(a.flags + im);
+      const uint32_t fl = a.flags[im];  // plain load: other blocks may OR FLAG_LOOP_CAP in
       const bool ordinary_active = (fl & FLAG_ANY_ETA_POS) != 0;
       const bool step_zero = (fl & FLAG_ANY_STEP_ZERO) != 0;
       RecView f{a.rec + p, a.ntot};
@@ -176,6 +206,15 @@ __global__ void __launch_bounds__(256) batch_samples_kernel(BatchArgs a) {
       };
       if (MIXED) ray_chunk_ff(B.obs, f, code, g0, g1, B.ngeo, ordinary_active, step_zero, emit, ffray_slot());
       else ray_chunk(B.obs, f, code, g0, g1, B.ngeo, ordinary_active, step_zero, emit);
+    }
+    // a capped loop in this tile is charged to the images the tile spans (thread 0 clears the
+    // word before the next tile's first barrier)
+    __syncthreads();
+    if (threadIdx.x == 0 && kg_loop_cap_word) {
+      const int64_t last = base + a.tile - 1 < total ? base + a.tile - 1 : total - 1;
+      const int i0 = batch_find(a.item_off, a.nimg, base), i1 = batch_find(a.item_off, a.nimg, last);
+      for (int j = i0; j <= i1; ++j) atomicOr(a.flags + j, kg_loop_cap_word);
+      kg_loop_cap_word = 0u;
     }
   }
 }

@@ -7,6 +7,7 @@ namespace kg {
 __global__ void __launch_bounds__(128) ray_setup_kernel(SetupArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned fl = 0;
+  loop_cap_begin();
   if (i < a.npix) {
     RayRec R;
     int rc = 0, tc = 0;
@@ -27,6 +28,7 @@ __global__ void __launch_bounds__(128) ray_setup_kernel(SetupArgs a) {
   const int key = i < a.npix ? ray_bucket(a.code[i]) : -1;
   const unsigned grp = __match_any_sync(0xffffffffu, key);
   if (key >= 0 && (threadIdx.x & 31) == (unsigned)(__ffs(grp) - 1)) atomicAdd(a.counts + key, (uint32_t)__popc(grp));
+  loop_cap_end(a.flags);
 }
 
 // Exclusive scan of the bucket counts into the cursors (one warp).
@@ -130,6 +132,7 @@ __global__ void __launch_bounds__(128) batch_setup_kernel(BatchArgs a) {
   int key = -1;
   unsigned fl = 0;
   int im = 0;
+  loop_cap_begin();
   if (r < a.ntot) {
     im = batch_find(a.pix_off, a.nimg, r);
     const BatchImage& B = a.img[im];
@@ -164,6 +167,14 @@ __global__ void __launch_bounds__(128) batch_setup_kernel(BatchArgs a) {
   // bucket counts: one atomic per distinct (image, bucket) key of the warp
   const unsigned grp = __match_any_sync(0xffffffffu, key);
   if (key >= 0 && lane == __ffs(grp) - 1) atomicAdd(a.counts + key, (uint32_t)__popc(grp));
+  // a capped loop in this block is charged to the images of the block's first and last rays
+  __syncthreads();
+  if (threadIdx.x == 0 && kg_loop_cap_word) {
+    const int64_t r0 = (int64_t)blockIdx.x * blockDim.x;
+    const int64_t r1 = r0 + blockDim.x - 1 < a.ntot ? r0 + blockDim.x - 1 : a.ntot - 1;
+    const int i0 = batch_find(a.pix_off, a.nimg, r0), i1 = batch_find(a.pix_off, a.nimg, r1);
+    for (int j = i0; j <= i1; ++j) atomicOr(a.flags + j, kg_loop_cap_word);
+  }
 }
 
 // Per image: exclusive scan of its NBUCKET counts into cursors that start at its first ray.
@@ -199,6 +210,31 @@ cudaError_t launch_batch_setup(const BatchArgs& a, cudaStream_t s) {
     batch_scan_kernel<<<a.nimg, 32, 0, s>>>(a);
     batch_scatter_kernel<<<grid, block, 0, s>>>(a);
   }
+  return cudaGetLastError();
+}
+
+}  // namespace kg
+
+namespace kg {
+
+// Pi(n; phi | m) with the reference adapter's special cases, as the per-ray setup evaluates
+// it (ellip_set_at in this translation unit's no-contraction arithmetic), one value per thread.
+__global__ void __launch_bounds__(256) ellip_pi_setup_kernel(const double* n, const double* phi, const double* m,
+                                                             int64_t N, double* out) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+    const double ni = n[i], mi = m[i];
+    const EllipSet<1> comp = ellip_set_at<1>(HALFPI, mi, &ni, nullptr);
+    out[i] = ellip_set_at<1>(phi[i], mi, &ni, &comp).P[0];
+  }
+}
+
+cudaError_t launch_ellip_pi_setup(const double* n, const double* phi, const double* m, int64_t N, double* out,
+                                  cudaStream_t s) {
+  if (N <= 0) return cudaSuccess;
+  int64_t grid = (N + 255) / 256;
+  if (grid > 152 * 16) grid = 152 * 16;
+  ellip_pi_setup_kernel<<<(unsigned)grid, 256, 0, s>>>(n, phi, m, N, out);
   return cudaGetLastError();
 }
 
