@@ -49,6 +49,7 @@ class BatchPlan:
         self.tau_tot = torch.empty(self.n_rays, dtype=torch.float64, device=self.dev)
         self.rclass = torch.empty(self.n_rays, dtype=torch.int32, device=self.dev)
         self.thclass = torch.empty(self.n_rays, dtype=torch.int32, device=self.dev)
+        self.flags = torch.zeros(max(n, 1), dtype=torch.int32, device=self.dev)  # per image, after each run
         self.pix_off, self.out_off = [], []
         po = so = 0
         for im in images:
@@ -68,7 +69,7 @@ class BatchPlan:
         self.alpha = alpha.to(device=self.dev, dtype=torch.float64).contiguous()
         self.beta = beta.to(device=self.dev, dtype=torch.float64).contiguous()
         g = _lib.GeodesicsOut(*[_ptr(self.out.get(k)) for k in SAMPLE_KEYS], _ptr(self.tau_tot), _ptr(self.rclass),
-                              _ptr(self.thclass), None)
+                              _ptr(self.thclass), _ptr(self.flags))
         _lib.check(self.lib.kgeo_batch_bind(self.handle, _ptr(self.alpha), _ptr(self.beta), ctypes.byref(g),
                                             _ptr(self.ws), self.ws_bytes))
         return self
@@ -101,8 +102,18 @@ class BatchPlan:
         so, po = self.out_off[i], self.pix_off[i]
         res = {k: v[so:so + ngeo * npix].view(ngeo, npix) for k, v in self.out.items()}
         res.update(tau_tot=self.tau_tot[po:po + npix], rclass=self.rclass[po:po + npix],
-                   thclass=self.thclass[po:po + npix])
+                   thclass=self.thclass[po:po + npix], flags=self.flags[i:i + 1])
         return res
+
+    def check_flags(self):
+        """Host check of every image's flags word after a run (synchronises): warns when an
+        iterative loop stopped at its cap (KGEO_FLAG_LOOP_CAP)."""
+        from .kerr_raytracing_ana import warn_loop_cap
+        f = 0
+        for v in self.flags[:len(self.images)].tolist():
+            f |= int(v)
+        warn_loop_cap(f)
+        return f
 
     def close(self):
         if self.handle:

@@ -35,6 +35,33 @@ UNITS = [
 ]
 
 
+# Per-thread stack every kernel must fit: CUDA's default cudaLimitStackSize is 1024 bytes and the
+# library never raises it. A kernel whose call chain (ptxas' "cumulative stack size") grows past
+# it faults with an illegal address at launch, so the build refuses it, with a margin.
+STACK_BUDGET = 960
+
+
+def check_resources(log):
+    """Parse ptxas -v output: {kernel: (registers, cumulative stack bytes, spill store bytes)}."""
+    import re
+    out, entry, spill = {}, None, 0
+    for line in log.splitlines():
+        m = re.search(r"Compiling entry function '(\S+)'", line)
+        if m:
+            entry, spill = m.group(1), 0
+            continue
+        m = re.search(r'(\d+) bytes spill stores', line)
+        if m and entry:
+            spill = int(m.group(1))
+            continue
+        m = re.search(r'Used (\d+) registers', line)
+        if m and entry:
+            st = re.search(r'(\d+) bytes cumulative stack size', line)
+            out[entry] = (int(m.group(1)), int(st.group(1)) if st else 0, spill)
+            entry = None
+    return out
+
+
 def nvcc():
     for cand in (shutil.which('nvcc'), '/usr/local/cuda/bin/nvcc'):
         if cand and os.path.exists(cand):
@@ -45,12 +72,14 @@ def nvcc():
 def _compile(args):
     src, extra, verbose = args
     obj = os.path.join(BUILD, src.replace('.cu', '.o'))
-    cmd = [nvcc(), *ARCH, *COMMON, *extra, '-c', os.path.join(CSRC, src), '-o', obj]
-    if verbose:
-        cmd.insert(1, '-Xptxas=-v')
+    cmd = [nvcc(), '-Xptxas=-v', *ARCH, *COMMON, *extra, '-c', os.path.join(CSRC, src), '-o', obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError('nvcc failed for %s:\n%s\n%s' % (src, ' '.join(cmd), r.stderr))
+    over = {k: v for k, v in check_resources(r.stderr).items() if v[1] > STACK_BUDGET}
+    if over:
+        raise RuntimeError('%s: per-thread stack above %d bytes (CUDA default limit 1024): %s'
+                           % (src, STACK_BUDGET, over))
     return obj, r.stderr
 
 
@@ -63,6 +92,9 @@ def build(verbose=False, force=False):
         return LIB
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         results = list(ex.map(_compile, [(s, e, verbose) for s, e in UNITS]))
+    with open(os.path.join(BUILD, 'ptxas.log'), 'w') as f:
+        for obj, log in results:
+            f.write(log)
     if verbose:
         for obj, log in results:
             sys.stderr.write(log)

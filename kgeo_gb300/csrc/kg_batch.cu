@@ -27,6 +27,7 @@ struct kgeo_batch_plan {
   int64_t* d_pix_off = nullptr;
   // bound buffers (caller-owned)
   BatchArgs args{};
+  uint32_t* user_flags = nullptr;  // (nimg) per-image flags words of the caller, or NULL
   bool bound = false;
   // launch shape
   kgeo_batch_config cfg{};
@@ -136,9 +137,14 @@ int run_pipeline(kgeo_batch_plan* p, const kgeo_batch_config& c, int tile_skip, 
     b.ntot = 0;  // item offsets only
     if (launch_batch_setup(b, s) != cudaSuccess) return KGEO_ERR_CUDA;
   }
-  if (p->nsamp_tot == 0) return KGEO_OK;
-  const int grid = p->sms * c.ctas_per_sm;
-  return launch_batch_samples(a, c.block, grid, s) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
+  if (p->nsamp_tot > 0) {
+    const int grid = p->sms * c.ctas_per_sm;
+    if (launch_batch_samples(a, c.block, grid, s) != cudaSuccess) return KGEO_ERR_CUDA;
+  }
+  if (tile_skip == 1 && p->user_flags &&
+      cudaMemcpyAsync(p->user_flags, a.flags, sizeof(uint32_t) * p->nimg, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return KGEO_ERR_CUDA;
+  return KGEO_OK;
 }
 
 void drop_graph(kgeo_batch_plan* p) {
@@ -264,6 +270,7 @@ int kgeo_batch_bind(kgeo_batch_plan* p, const double* alpha, const double* beta,
   a.ph = out->ph;
   a.sig = out->sig;
   a.mino = out->mino;
+  p->user_flags = out->flags;
   p->bound = true;
   drop_graph(p);
   return KGEO_OK;

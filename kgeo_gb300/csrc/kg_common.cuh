@@ -65,4 +65,52 @@ KG_HD double cube_rn(double x) {
 // Python / numpy sign conventions.
 KG_HD double sign_of(double x) { return x > 0 ? 1.0 : (x < 0 ? -1.0 : 0.0); }
 
+// ---- iteration caps ---------------------------------------------------------
+// Every iterative loop of the elliptic arithmetic stops at a hard cap (Carlson duplication
+// KG_CARLSON_MAX_IT steps, descending Landen KG_LANDEN_MAX levels; both are far above what
+// FP64 convergence takes, 4-12 steps and 3-6 levels). A loop that reaches its cap without
+// meeting its convergence test calls note_loop_cap(). On the device the tracer's kernels keep
+// one shared word per block (loop_cap_begin at block start, loop_cap_end OR-s it into the
+// launch's flags word as FLAG_LOOP_CAP); kernels that do not collect it leave the word
+// unread. The host build keeps one process-wide word (host_loop_cap()).
+#ifndef KG_CARLSON_MAX_IT
+#define KG_CARLSON_MAX_IT 40
+#endif
+#ifndef KG_LANDEN_MAX
+#define KG_LANDEN_MAX 12
+#endif
+
+constexpr unsigned FLAG_LOOP_CAP = 16u;
+
+#if defined(__CUDACC__)
+static __shared__ unsigned kg_loop_cap_word;
+#endif
+
+inline unsigned& host_loop_cap() {
+  static unsigned word = 0;
+  return word;
+}
+
+KG_HD void note_loop_cap() {
+#if defined(__CUDA_ARCH__)
+  atomicOr_block(&kg_loop_cap_word, FLAG_LOOP_CAP);
+#else
+  host_loop_cap() |= FLAG_LOOP_CAP;
+#endif
+}
+
+#if defined(__CUDACC__)
+// Clear the block's word; every thread of the block must call it (it synchronises).
+__device__ __forceinline__ void loop_cap_begin() {
+  if (threadIdx.x == 0) kg_loop_cap_word = 0u;
+  __syncthreads();
+}
+
+// OR the block's word into *flags; every thread of the block must call it (it synchronises).
+__device__ __forceinline__ void loop_cap_end(uint32_t* flags) {
+  __syncthreads();
+  if (threadIdx.x == 0 && kg_loop_cap_word && flags) atomicOr(flags, kg_loop_cap_word);
+}
+#endif
+
 }  // namespace kg

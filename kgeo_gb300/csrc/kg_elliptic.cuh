@@ -23,7 +23,7 @@ namespace kg {
 // (3 r)^(-1/6) and (r/4)^(-1/6) for r = 1e-16 (Carlson 1995, eqs. 2.2 and 2.16).
 constexpr double RF_Q = 386.0;
 constexpr double RJ_Q = 585.0;
-constexpr int CARLSON_MAX_IT = 40;  // hard cap; convergence takes 4-12 steps in FP64
+constexpr int CARLSON_MAX_IT = KG_CARLSON_MAX_IT;  // hard cap; convergence takes 4-12 steps in FP64
 
 // R_C(1, 1 + e) for e > -1 (DLMF 19.2.18-19 in well-conditioned arctan / log form,
 // and the series sum_k (-e)^k / (2k + 1) near e = 0).
@@ -59,7 +59,8 @@ KG_HD double carlson_rf(double x, double y, double z) {
   const double A0 = (x + y + z) / 3.0;
   const double Q = RF_Q * fmax(fmax(fabs(A0 - x), fabs(A0 - y)), fabs(A0 - z));
   double A = A0, f = 1.0;
-  for (int it = 0; it < CARLSON_MAX_IT && f * Q >= fabs(A); ++it) {
+  int it = 0;
+  for (; it < CARLSON_MAX_IT && f * Q >= fabs(A); ++it) {
     double sx = sqrt(x), sy = sqrt(y), sz = sqrt(z);
     double lam = sx * sy + sx * sz + sy * sz;
     x = 0.25 * (x + lam);
@@ -68,6 +69,7 @@ KG_HD double carlson_rf(double x, double y, double z) {
     A = 0.25 * (A + lam);
     f *= 0.25;
   }
+  if (it == CARLSON_MAX_IT && f * Q >= fabs(A)) note_loop_cap();
   double X = (A0 - x0) * f / A;
   double Y = (A0 - y0) * f / A;
   double Z = -(X + Y);
@@ -95,12 +97,16 @@ KG_HD void rj_multi(double x, double y, double z, const double* p_in, double* rj
   }
   double f = 1.0;   // 4^-m
   double f3 = 1.0;  // 4^-3m
-  for (int it = 0; it < CARLSON_MAX_IT; ++it) {
+  for (int it = 0;; ++it) {
     // Carlson's stopping rule 4^-m Q < |A_m|, required of every integral in the set
     bool done = f * Qf < fabs(Af);
 #pragma unroll
     for (int i = 0; i < NP; ++i) done = done && (f * Q[i] < fabs(A[i]));
     if (done) break;
+    if (it == CARLSON_MAX_IT) {
+      note_loop_cap();
+      break;
+    }
     double sx = sqrt(x), sy = sqrt(y), sz = sqrt(z);
     double lam = sx * sy + sx * sz + sy * sz;
 #pragma unroll
@@ -247,7 +253,7 @@ KG_HD double ellip_pi_ref(double n, double phi, double m) {
 // Jacobi elliptic functions
 // ---------------------------------------------------------------------------
 
-constexpr int LANDEN_MAX = 12;
+constexpr int LANDEN_MAX = KG_LANDEN_MAX;
 
 struct Jacobi {
   double sn, cn, dn;
@@ -270,6 +276,7 @@ KG_HD Jacobi jacobi_landen(double u, double m) {
     w = w / (1.0 + k1);
     mm = k1 * k1;
   }
+  if (mm > 1.0e-9) note_loop_cap();
   // DLMF 22.10.4-6 to first order in m
   double s = sin(w), c = cos(w);
   double t = 0.25 * mm * (w - s * c);

@@ -5,6 +5,8 @@ kgeo/kerr_raytracing_ana.py:46-193; the work runs in the sm_103a kernels behind 
 C ABI (include/kgeo_gb300.h). Plotting and HDF5 saving of the reference are not
 part of this package: `plotdata` and `savedata` are accepted and ignored.
 """
+import warnings
+
 import numpy as np
 import torch
 
@@ -48,12 +50,23 @@ def _pixels(alpha, beta):
     return alpha, beta
 
 
+class ConvergenceWarning(RuntimeWarning):
+    """An iterative loop of the device's elliptic arithmetic stopped at its iteration cap."""
+
+
+def warn_loop_cap(f):
+    if f & _lib.FLAG_LOOP_CAP:
+        warnings.warn("kgeo_gb300: an elliptic-integral loop (Carlson duplication or Landen descent) stopped "
+                      "at its iteration cap; some samples may be inaccurate", ConvergenceWarning, stacklevel=3)
+
+
 def _flags_check(a, flags):
     f = flags if isinstance(flags, int) else int(flags.item())
     if f & _lib.FLAG_MINSPIN_VORTICAL:
         raise Exception("below MINSPIN but there are eta<0 points in th_integrate!")
     if np.abs(a) < MINSPIN and (f & _lib.FLAG_ANY_ETA_NONPOS):
         print("WARNING: there were eta<0 points for spin %f<MINSPIN!" % a)
+    warn_loop_cap(f)
 
 
 def raytrace_ana(a=SPIN, observer_coords=[0, ROUT, INC, 0], image_coords=[alpha_default, beta_default],

@@ -30,6 +30,12 @@ static EmissionModel make_model(const int* mi, const double* md) {
 
 extern "C" {
 int hm_num_fields() { return NUM_FIELDS; }
+// Loop-cap word of the host build (note_loop_cap), returned and cleared.
+unsigned hm_take_loop_cap() {
+  unsigned w = host_loop_cap();
+  host_loop_cap() = 0;
+  return w;
+}
 double hm_rf(double x, double y, double z) { return carlson_rf(x, y, z); }
 double hm_rj(double x, double y, double z, double p) { return carlson_rj(x, y, z, p); }
 double hm_rd(double x, double y, double z) { return carlson_rd(x, y, z); }

@@ -65,3 +65,19 @@ def test_argument_errors_return_codes_without_gpu(lib):
     assert lib.kgeo_raytrace(ctypes.byref(ob), None, None, -1, 5, 1.0, ctypes.byref(g), None, 0, None) == 4
     assert lib.kgeo_raytrace(ctypes.byref(ob), None, None, 10, -5, 1.0, ctypes.byref(g), None, 0, None) == 5
     assert lib.kgeo_raytrace(ctypes.byref(ob), None, None, 10, 5, 1.0, ctypes.byref(g), None, 0, None) == 8
+
+
+def test_kernel_stacks_within_default_limit(lib):
+    """Every kernel's per-thread stack (its whole call chain) stays under CUDA's default
+    1024-byte limit with the build's margin; the build refuses a unit otherwise, and this
+    re-reads the ptxas report it keeps (kgeo_gb300/_build/ptxas.log)."""
+    from kgeo_gb300 import build
+    path = os.path.join(build.BUILD, 'ptxas.log')
+    if not os.path.exists(path):
+        pytest.skip('library built without its ptxas report')
+    res = build.check_resources(open(path).read())
+    names = ' '.join(res)
+    for k in ('stepped_kernel', 'ray_setup_kernel', 'samples_kernel', 'batch_samples_kernel', 'image_kernel'):
+        assert k in names
+    over = {k: v for k, v in res.items() if v[1] > build.STACK_BUDGET}
+    assert not over, over
