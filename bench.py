@@ -402,8 +402,8 @@ def error_stats(got, ref, rclass, torch, rho=None):
                   'frac_above_1e-6': float((body > 1e-6).double().mean()),
                   'nonfinite_mismatch': int((torch.isfinite(x) != torch.isfinite(y)).sum())}
         if rho is not None:
-            # the parity rule near elliptic-Pi poles: bar max(1e-6, 1e-12 / rho) per sample
-            bar = torch.clamp(1e-12 / rho[:G - 1], min=1e-6)
+            # the FP64 parity rule near elliptic-Pi poles: bar max(1e-6, 10 eps / rho) per sample
+            bar = torch.clamp(10 * 2.220446049250313e-16 / rho[:G - 1], min=1e-6)
             res[k]['max_over_bar'] = float((body / bar).max())
     return res
 
@@ -488,7 +488,7 @@ def run_mixed(args):
         'speedup_vs_fp64_recurrence': t_fp64 / t_mixed, 'speedup_vs_fp64_plain': t_plain / t_mixed,
         'mixed_vs_fp64_error': errs, 'fp64_vs_oracle_error': orc, 'mixed_vs_oracle_error': orc_m,
         'error_scales': 'relative; floor 1 rad for theta, phi; r_o for t, sigma; max_over_bar = max of error / '
-                        'max(1e-6, 1e-12 / rho), rho = distance to the nearest elliptic-Pi pole',
+                        'max(1e-6, 10 eps / rho), rho = distance to the nearest elliptic-Pi pole',
         'clocks': ck,
         'gpu_launches': 4 * args.steps,
     }

@@ -325,6 +325,14 @@ KG_HD ff pi_inc_ff(const ff& nf, float c, const ff& S3, const ff& X, float rho_u
 // small enough that few lanes of a warp enter it at the same step.
 constexpr float RESEED_RHO = 1.0e-3f;
 
+// Within DEEP_RHO of a pole even the FP64 Pi from the float-float state is not enough: the
+// state's own ~1e-13 error reaches the sample as ~1e-13 / rho (1e-8 at the zone's edge). There
+// the whole theta or radial state is re-seeded from the FP64 direct evaluation at the sample
+// (Landen Jacobi functions, Carlson integrals), as the FP64 recurrence does next to a pole, so
+// the error falls to the FP64 path's ~eps / rho. 4e-5 of the samples of the 2048^2-plus-band
+// workload lie in the zone.
+constexpr float DEEP_RHO = 1.0e-5f;
+
 template <class FV>
 KG_HD ff radial_pi_direct(const FV& f, int i, const FFRadial& st, const FFState& w, const ff& Xw) {
   const double X = ff_to_double(Xw);
@@ -630,6 +638,12 @@ KG_HD void ray_chunk_ff(const Observer& ob, const FV& f, int code, int64_t g0, i
     } else {
       ff_theta_step(f, c, code, tau, &ts);
       ff_radial_step(f, c, code, &rs);
+      if (c.tn > 0.0f && fabsf(ts.rho) < DEEP_RHO)
+        ts = ff_theta_from(theta_state_direct(f, code, theta_snarg(f, tau)), c.tnf);
+      bool deep = false;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) deep = deep || (c.rn[i] > 0.0f && fabsf(rs.rho[i]) < DEEP_RHO);
+      if (deep) rs = ff_radial_from(radial_state_direct(f, code, radial_X(f, tau), true), c);
     }
     FFOut o;
     const ff tau_ff = ff_mul_f(c.step, (float)g);
