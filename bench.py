@@ -15,9 +15,16 @@ Metric: rays/s (whole job, all ranks). Also reported: geodesic points/s.
 --impl reference times the reference's own CPU algorithm for this path (the oracle port
 under oracle/, numpy + scipy.special) on all host cores over a bounded seeded sample of
 the same workload. --case small runs a 128 x 128 grid of the same draw (for ncu captures).
-Multi-GPU: launched by torch.distributed.run, one rank per GPU, each rank traces its own
-image (weak scaling, no data-path collective); a barrier + CUDA synchronize bracket the
-timed steps and the max time over ranks is reported.
+Multi-GPU: launched by torch.distributed.run, one rank per GPU; the seed-0 image's pixels
+are split into N contiguous ranges, one per rank (rays are independent: no data-path
+collective), so every N traces the same image (strong scaling); a barrier + CUDA synchronize
+bracket the timed steps and the max time over ranks is reported.
+
+On one GPU the default run also measures the other configurations of the target and adds
+them to the same JSON line under "north_star" (--no-extras skips them): the
+mixed-precision 2048^2-plus-band workload against the FP64 recurrence and the plain FP64
+kernel with the error statistics, the 64-image batch, the differentiable image
+(image + gradient per second) and the FP64 drop-in over the draws of seeds 0-7.
 """
 import argparse
 import json
@@ -38,8 +45,8 @@ ORDERS = (0, 1, 2)
 R_O = 1.0e4
 CPU_SAMPLE_RAYS = 16384      # rays of the bounded CPU sample (every 16th pixel of the grid)
 # FP64 floating-point work of the sample kernel (addition-theorem recurrence, chunks of 64)
-# per geodesic point on this workload, from the ncu capture summarised in
-# profiles/geo_samples_fp64_config2.md: (dadd + dmul + 2 dfma thread instructions) / points.
+# per geodesic point on this workload, from an ncu capture of one launch on the 128x128 case
+# (--case small): (dadd + dmul + 2 dfma thread instructions) / points.
 # Used for roofline.achieved. FP64_INST_PER_POINT: FP64 pipe instructions (dadd + dmul +
 # dfma) per point, against the pipe's rate (fp64_peak / 2 instructions per second).
 FP64_FLOP_PER_POINT = 748
@@ -48,6 +55,13 @@ FP64_INST_PER_POINT = 480
 DRAM_BYTES_PER_POINT = 53.6
 BYTES_PER_POINT = 48          # t, r, theta, phi, sigma, Mino tau written per point (8 B each)
 L2_FLUSH_BYTES = 256 << 20
+
+
+def shard(npix, rank, world):
+    """Contiguous pixel range [lo, hi) of rank out of world (sizes differ by at most one)."""
+    lo = npix * rank // world
+    hi = npix * (rank + 1) // world
+    return lo, hi
 
 
 def workload(seed, grid=GRID):
@@ -186,7 +200,9 @@ def run_ours(args):
     from kgeo_gb300 import kerr_raytracing_ana as kra
 
     grid = GRID if args.case == 'full' else 128
-    a, th_o, A, B = workload(rank, grid)
+    a, th_o, A_all, B_all = workload(0, grid)
+    lo, hi = shard(A_all.size, rank, world)
+    A, B = A_all[lo:hi], B_all[lo:hi]
     npix = A.size
     al, be = dev.as_device(A), dev.as_device(B)
     prep = dev.PreparedRays(a, R_O, th_o, al, be, ngeo=NGEO)
@@ -238,7 +254,7 @@ def run_ours(args):
     setup_ms = np.mean([r[0].elapsed_time(r[1]) for r in recs])
     samp_ms = np.mean([r[1].elapsed_time(r[2]) for r in recs])
     eq_ms = np.mean([r[2].elapsed_time(r[3]) for r in recs])
-    rays = npix * args.steps * world
+    rays = A_all.size * args.steps
     value = rays / elapsed
     points = npix * NGEO
     launches = 5 * args.steps  # setup + bucket scan + bucket scatter, samples, r_equatorial
@@ -265,9 +281,14 @@ def run_ours(args):
             del g, rq
             step_ms.append((time.perf_counter() - t_s) * 1e3)
         dt = (time.perf_counter() - t_e) / nsteps_e
-        h2d = 2 * npix * 8 * (1 + len(ORDERS))
-        d2h = 6 * points * 8 + len(ORDERS) * 4 * npix * 8
-        e2e = {'value': npix * world / dt, 'unit': 'rays/s', 'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
+        if world > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([dt], dtype=torch.float64, device=al.device)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            dt = float(tt.item())
+        h2d = 2 * A_all.size * 8 * (1 + len(ORDERS))
+        d2h = 6 * A_all.size * NGEO * 8 + len(ORDERS) * 4 * A_all.size * 8
+        e2e = {'value': A_all.size / dt, 'unit': 'rays/s', 'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
                'ms_per_step': dt * 1e3, 'step_ms': [round(x, 2) for x in step_ms],
                'path': 'kgeo_gb300.kerr_raytracing_ana.raytrace_ana + equatorial_lensing.r_equatorial (numpy in/out)'}
 
@@ -302,12 +323,18 @@ def run_ours(args):
                'sample': '%d rays (every %dth pixel of the same grid and draw), ngeo=%d, r_equatorial n=0..2; '
                          'oracle/kgeo_oracle.py (numpy+scipy restatement of the reference) on a %d-process pool, '
                          '%.1f s wall' % (n, npix // CPU_SAMPLE_RAYS, NGEO, cores, dt)}
+    extras = None
+    if world == 1 and args.case == 'full' and not args.no_extras:
+        del prep, out, flush
+        torch.cuda.empty_cache()
+        extras = north_star_extras(args)
     line = {
         'metric': 'Kerr rays/s: FP64 raytrace_ana (ngeo=400) + r_equatorial n=0..2, 512x512 image',
         'value': value, 'unit': 'rays/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': elapsed / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+        'ms_per_step': elapsed / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'strong',
         'vs_baseline': None, 'dtype': 'f64',
-        'data': 'synthetic: uniform image-plane grid, a and theta_o drawn from default_rng(rank)',
+        'data': 'synthetic: uniform image-plane grid, a and theta_o drawn from default_rng(0); with N ranks each '
+                'traces a contiguous 1/N of the pixels',
         'config': {'workload': 'FP64 drop-in at production size (512x512 over [-10,10] M, a~U[0,0.998), '
                                'theta_o~U[1,89] deg, r_o=1e4, ngeo=400, r_equatorial n=0,1,2)',
                    'npix': npix, 'ngeo': NGEO, 'a': a, 'th_o_deg': th_o * 180 / np.pi, 'orders': list(ORDERS),
@@ -316,8 +343,84 @@ def run_ours(args):
         'points_per_s': value * NGEO, 'kernel_ms': {'ray_setup': setup_ms, 'samples': samp_ms,
                                                     'r_equatorial': eq_ms},
         'roofline': roof, 'cpu_baseline': cpu, 'e2e': e2e, 'gpu_launches': launches, 'clocks': ck,
+        'north_star': extras,
     }
     print(json.dumps(line))
+
+
+def north_star_extras(args):
+    """The target's other configurations, measured in the same run (one GPU)."""
+    import copy
+    import torch
+    sub = copy.copy(args)
+    sub.no_cpu_baseline = True
+    out = {}
+
+    def free():
+        import gc
+        gc.collect()
+        torch.cuda.empty_cache()
+
+    def err_summary(e):
+        return {k: {'max': v['max'], 'rms': v['rms'], 'frac_above_1e-6': v.get('frac_above_1e-6')}
+                for k, v in e.items() if isinstance(v, dict)}
+    # configuration 3: mixed vs the FP64 recurrence and the plain FP64 kernel
+    sub.case, sub.steps, sub.warmup = 'mixed', 2, 3
+    m = run_mixed(sub, emit=False)
+    out['config3_mixed'] = {
+        'rays_per_s': m['value'], 'ms_per_step': m['ms_per_step'],
+        'fp64_recurrence_rays_per_s': m['fp64_recurrence']['value'], 'fp64_plain_rays_per_s': m['fp64_plain']['value'],
+        'speedup_vs_fp64_recurrence': m['speedup_vs_fp64_recurrence'], 'speedup_vs_fp64_plain': m['speedup_vs_fp64_plain'],
+        'mixed_vs_fp64_recurrence_error': err_summary(m['mixed_vs_fp64_error']), 'clocks': m['clocks'],
+        'workload': m['config']['workload']}
+    free()
+    # configuration 4: 64 images in one persistent launch / CUDA graph
+    sub.case, sub.steps, sub.warmup = 'batch', 2, 3
+    b = run_batch(sub, emit=False)
+    out['config4_batch'] = {
+        'rays_per_s': b['value'], 'ms_per_step': b['ms_per_step'],
+        'fp64_batched_recurrence_rays_per_s': b['fp64_batched_recurrence']['value'],
+        'fp64_plain_rays_per_s': b['fp64_plain']['value'], 'speedup_vs_fp64_plain': b['speedup_vs_fp64_plain'],
+        'speedup_vs_fp64_recurrence': b['speedup_vs_fp64_recurrence'],
+        'mixed_vs_fp64_error': b['mixed_vs_fp64_error'], 'tuned': b['config']['tuned'], 'clocks': b['clocks']}
+    free()
+    # configuration 5: image + adjoint gradient
+    sub.case, sub.steps, sub.warmup = 'image', 10, 3
+    im = run_image(sub, emit=False)
+    out['config5_image_grad'] = {
+        'image_grad_per_s': im['value'], 'ms_per_step': im['ms_per_step'], 'kernel_ms': im['kernel_ms'],
+        'e2e_image_grad_per_s': im['e2e']['value'], 'roofline_frac': im['roofline']['frac'], 'clocks': im['clocks']}
+    free()
+    # configuration 2 over the draws of seeds 0-7 (device rays/s of setup + samples + r_equatorial)
+    from kgeo_gb300 import device as dev
+    from kgeo_gb300 import equatorial_lensing as el
+    stream = torch.cuda.current_stream()
+    rates, draws = [], []
+    for seed in range(8):
+        a, th_o, A, B = workload(seed)
+        al, be = dev.as_device(A), dev.as_device(B)
+        prep = dev.PreparedRays(a, R_O, th_o, al, be, ngeo=NGEO)
+        o = prep.alloc()
+
+        def step():
+            prep.setup()
+            prep.samples(o)
+            el.r_equatorial_device(a, R_O, th_o, ORDERS, al, be)
+        step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(2):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        rates.append(2 * A.size / (e0.elapsed_time(e1) / 1e3))
+        draws.append((round(a, 4), round(th_o * 180 / np.pi, 2)))
+        del prep, o
+    free()
+    out['config2_seeds_0_7'] = {'rays_per_s': rates, 'min': min(rates), 'mean': float(np.mean(rates)),
+                                'draws_a_thdeg': draws}
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -408,7 +511,7 @@ def error_stats(got, ref, rclass, torch, rho=None):
     return res
 
 
-def run_mixed(args):
+def run_mixed(args, emit=True):
     small = args.case == 'mixed-small'
     pool = cores = None
     import torch
@@ -492,7 +595,9 @@ def run_mixed(args):
         'clocks': ck,
         'gpu_launches': 4 * args.steps,
     }
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -504,7 +609,7 @@ IMG_LIM = 8.0
 IMG_PHYS = (0.5, 60 * np.pi / 180, 2.0, 0.8, 0.5)   # a, theta_o, p, xi, beta_r
 IMG_MBAR = 2
 # FP64 FLOP per pixel of the adjoint kernel on this workload (all three orders), from the
-# ncu capture summarised in profiles/image_adjoint_config5.md: (dadd + dmul + 2 dfma
+# ncu capture of one launch on the 128x128 case (--case image-small): (dadd + dmul + 2 dfma
 # thread instructions) / pixels. Used for roofline.achieved.
 ADJ_FLOP_PER_PIXEL = 29170
 CPU_IMG_SAMPLE = 65536       # pixels of the bounded CPU sample (every 4th pixel)
@@ -552,7 +657,7 @@ def cpu_image_run(pool, cores):
                       'full image' % (idx.size, A.size // CPU_IMG_SAMPLE, cores, dt)}
 
 
-def run_image(args):
+def run_image(args, emit=True):
     small = args.case == 'image-small'
     pool = cores = None
     import torch
@@ -659,7 +764,9 @@ def run_image(args):
                 'path': 'kgeo_gb300.image_grad.equatorial_image (torch.autograd.Function) from pinned host arrays'},
         'gpu_launches': 3 * args.steps, 'clocks': ck,
     }
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -669,8 +776,8 @@ def run_image(args):
 POL_NX = 800
 POL_MBAR = 2
 POL_MODEL = dict(a=0.7, inc=45.0, fac_subkep=0.6, beta_phi=0.8, beta_r=0.7)
-# FP64 FLOP per pixel of the polarised image kernel (three orders), from the ncu capture in
-# profiles/image_pol_800.md: (dadd + dmul + 2 dfma thread instructions) / pixels, and the
+# FP64 FLOP per pixel of the polarised image kernel (three orders), from an ncu capture of one
+# launch (--case polimage-small): (dadd + dmul + 2 dfma thread instructions) / pixels, and the
 # FP64 pipe instructions (dadd + dmul + dfma) per pixel.
 POL_FLOP_PER_PIXEL = 10445
 POL_FP64_INST_PER_PIXEL = 6800
@@ -809,7 +916,7 @@ def run_polimage(args):
 # ---------------------------------------------------------------------------
 
 CPU_LIB_SAMPLE = 600     # (curve, angle) roots of the bounded CPU sample
-# FP64 work of curve_kernel per root on the library-small capture (profiles/curve_library_jet.md):
+# FP64 work of curve_kernel per root on an ncu capture of the library-small case:
 # (dadd + dmul + 2 dfma) thread instructions / roots, and FP64 pipe instructions / roots
 LIB_FLOP_PER_ROOT = 153960
 LIB_FP64_INST_PER_ROOT = 102000
@@ -936,8 +1043,8 @@ def run_library(args):
 JET_GRID = 256
 JET_CASE = dict(a=0.9, inc=17.0, model='para', psitarget=1.0, ngeo=200, neqmax=1)
 CPU_JET_SAMPLE = 2048     # pixels of the bounded CPU sample
-# FP64 work of jet_solve_kernel per converged solve on the jet-small capture
-# (profiles/curve_library_jet.md), as for the curve kernel
+# FP64 work of jet_solve_kernel per converged solve on an ncu capture of the jet-small case,
+# as for the curve kernel
 JET_FLOP_PER_SOLVE = 14310
 JET_FP64_INST_PER_SOLVE = 8973
 
@@ -1038,8 +1145,8 @@ def run_jet(args):
 STOKES_GRID = 256
 STOKES_CASE = dict(a=0.5, inc=60.0, model='mono', psitarget=0.4, ngeo=200, neqmax=1, nu_parallel=0.0, sigma=2.0)
 CPU_STOKES_SAMPLE = 2048
-# FP64 work of jet_stokes_kernel per crossing (r != 0) on the stokes-small capture
-# (profiles/jet_stokes.md): dadd + dmul + 2 dfma, and FP64 pipe instructions
+# FP64 work of jet_stokes_kernel per crossing (r != 0) on an ncu capture of the stokes-small
+# case: dadd + dmul + 2 dfma, and FP64 pipe instructions
 STOKES_FLOP_PER_CROSSING = 2940
 STOKES_FP64_INST_PER_CROSSING = 1901
 
@@ -1184,7 +1291,7 @@ def _oracle_batch_chunk(args):
     return len(A)
 
 
-def run_batch(args):
+def run_batch(args, emit=True):
     small = args.case == 'batch-small'
     pool = cores = None
     import torch
@@ -1299,7 +1406,9 @@ def run_batch(args):
         'cpu_baseline': cpu, 'clocks': ck, 'gpu_launches': 6 * args.steps,
     }
     plan.close()
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 def main():
@@ -1313,6 +1422,7 @@ def main():
                                       'jet-small', 'stokes', 'stokes-small'),
                    default='full')
     p.add_argument('--no-cpu-baseline', action='store_true')
+    p.add_argument('--no-extras', action='store_true', help='skip the other configurations of the north_star key')
     args = p.parse_args()
     if args.impl == 'reference':
         run_reference(args)

@@ -74,3 +74,61 @@ def test_reduce_without_process_group_is_identity():
     from kgeo_gb300.image_grad import reduce_loss_grad
     L, g = reduce_loss_grad(1.5, [1.0, -2.0])
     assert L == 1.5 and g == [1.0, -2.0]
+
+
+def _trace_worker(rank, world, port, q):
+    """One rank of the benchmark's multi-GPU split: its contiguous pixel range of the image
+    (bench.shard), traced with the kernel arithmetic built for the host; rank 0 gathers."""
+    os.environ['MASTER_ADDR'] = '127.0.0.1'
+    os.environ['MASTER_PORT'] = str(port)
+    dist.init_process_group('gloo', rank=rank, world_size=world)
+    try:
+        import sys
+        sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+        import bench
+        import test_hostmath_cpu as T
+        import ctypes
+        L = ctypes.CDLL(T.LIBPATH)
+        L.hm_setup.restype = ctypes.c_uint
+        a, th_o, A, B = bench.workload(0, grid=20)
+        lo, hi = bench.shard(A.size, rank, world)
+        part = T.host_trace_stepped(L, a, bench.R_O, th_o, A[lo:hi], B[lo:hi], 40, 16)
+        parts = [None] * world
+        dist.all_gather_object(parts, (lo, hi, part))
+        if rank == 0:
+            q.put(parts)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_pixel_shards_concatenate_to_single_trace():
+    """Rays are independent: the ranks' contiguous pixel ranges, concatenated, are the
+    single-process trace of the whole image, sample for sample."""
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    import test_hostmath_cpu as T
+    import ctypes
+    if not os.path.exists(T.LIBPATH):
+        import pytest
+        pytest.skip('host build of the kernel headers missing')
+    for world in (2, 3):
+        ctx = mp.get_context('spawn')
+        q = ctx.Queue()
+        port = _free_port()
+        procs = [ctx.Process(target=_trace_worker, args=(r, world, port, q)) for r in range(world)]
+        for p in procs:
+            p.start()
+        parts = q.get(timeout=120)
+        for p in procs:
+            p.join(timeout=60)
+            assert p.exitcode == 0
+        L = ctypes.CDLL(T.LIBPATH)
+        L.hm_setup.restype = ctypes.c_uint
+        a, th_o, A, B = bench.workload(0, grid=20)
+        whole = T.host_trace_stepped(L, a, bench.R_O, th_o, A, B, 40, 16)
+        assert [p[0] for p in parts] == sorted(p[0] for p in parts) and parts[-1][1] == A.size
+        assert all(parts[i][1] == parts[i + 1][0] for i in range(world - 1))
+        for k in ('t', 'r', 'th', 'ph', 'sig', 'mino'):
+            cat = np.concatenate([p[2][k] for p in parts], axis=1)
+            np.testing.assert_array_equal(cat, whole[k])
