@@ -432,11 +432,13 @@ int kgeo_batch_graph_launch(kgeo_batch_plan* plan, void* stream);
  * device memory under a fixed budget, a latency-critical loop that cannot afford an
  * allocator call, or a host that offers no allocator. Same arguments, outputs and status
  * codes as kgeo_raytrace minus the workspace: the per-ray scratch lives in a fixed array
- * inside the library (room for KGEO_NOALLOC_MAX_PIXELS rays, about 9.9 MB of device memory
+ * inside the library (room for KGEO_NOALLOC_MAX_PIXELS rays, about 13.2 MB of device memory
  * that every GPU loading the library keeps until the process exits). Larger npix is
  * refused with KGEO_ERR_NOALLOC_SIZE before any work. The call allocates and frees nothing.
  * The first call on a device looks up the array's device address (cudaGetSymbolAddress)
- * once for that device; make that first call before any stream capture. Every call on a
+ * once for that device and keeps it for the life of the process; make that first call before
+ * any stream capture, and do not call this entry point on a device after a cudaDeviceReset of
+ * it (the kept address would be stale). Every call on a
  * device shares the one array and it keeps the last call's contents, so calls whose work
  * overlaps on the GPU (different streams, or different host threads) race: order them on one
  * stream or serialise them. */

@@ -76,6 +76,9 @@ def _compile(args):
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError('nvcc failed for %s:\n%s\n%s' % (src, ' '.join(cmd), r.stderr))
+    if 'cannot be statically determined' in r.stderr:
+        raise RuntimeError('%s: a kernel whose stack is not known at compile time (recursion or an '
+                           'indirect call); the library keeps every stack static' % src)
     over = {k: v for k, v in check_resources(r.stderr).items() if v[1] > STACK_BUDGET}
     if over:
         raise RuntimeError('%s: per-thread stack above %d bytes (CUDA default limit 1024): %s'

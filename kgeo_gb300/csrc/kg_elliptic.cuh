@@ -40,18 +40,24 @@ KG_HD double rc_one(double e) {
 }
 
 // General R_C(x, y), x >= 0, y != 0 (Cauchy principal value for y < 0), DLMF 19.2.17-20.
+// The principal value is R_C(x, y) = sqrt(x / (x - y)) R_C(x - y, -y) (DLMF 19.2.20), written
+// without a recursive call so that every kernel's stack is known at compile time.
 KG_HD double carlson_rc(double x, double y) {
+  double scale = 1.0;
   if (y < 0.0) {
-    return sqrt(x / (x - y)) * carlson_rc(x - y, -y);
+    scale = sqrt(x / (x - y));
+    const double x1 = x - y;
+    y = -y;
+    x = x1;
   }
   double d = y - x;
-  if (fabs(d) < 2.0e-3 * x) return rc_one(d / x) / sqrt(x);
+  if (fabs(d) < 2.0e-3 * x) return scale * (rc_one(d / x) / sqrt(x));
   if (d > 0.0) {
-    if (x == 0.0) return HALFPI / sqrt(y);
-    return atan(sqrt(d / x)) / sqrt(d);
+    if (x == 0.0) return scale * (HALFPI / sqrt(y));
+    return scale * (atan(sqrt(d / x)) / sqrt(d));
   }
   double xd = -d;
-  return log((sqrt(x) + sqrt(xd)) / sqrt(y)) / sqrt(xd);
+  return scale * (log((sqrt(x) + sqrt(xd)) / sqrt(y)) / sqrt(xd));
 }
 
 KG_HD double carlson_rf(double x, double y, double z) {

@@ -8,7 +8,7 @@
 
 namespace kg {
 
-KG_HD float __frcp_rn_compat(float x) {
+KG_HD float rcp_rn_f(float x) {
 #if defined(__CUDA_ARCH__)
   return __frcp_rn(x);
 #else
@@ -19,7 +19,7 @@ KG_HD float __frcp_rn_compat(float x) {
 // Pi increment of one step in FP32 (see pi_add_term for the formula); X is formed in
 // float-float by the caller (it cancels near a pole) and handed over rounded.
 KG_HD float pi_add_term_f(float n, float c, float X, float S3) {
-  float iX = __frcp_rn_compat(X);
+  float iX = rcp_rn_f(X);
   float t = S3 * iX;
   float z2 = c * (t * t);
   if (X > 0.0f && fabsf(z2) < 2.0e-2f) return n * t * rc_one_f(-z2);

@@ -1,8 +1,10 @@
 // Mixed-precision recurrence on the FP32 pipe: the Jacobi states, the E / Pi accumulators,
 // r and the combination into t, phi, sigma are carried in float-float (kg_ff.cuh, ~48 bits),
-// the Pi and E increments of a step in FP32; FP64 is left to the chunk starts (FP64 Jacobi
-// functions by Landen, FP32 Carlson integrals: kg_mixed.cuh), the samples next to a Pi pole,
-// the increments the per-ray precision planner flags, and the final horizon-adjacent sample.
+// the Pi and E increments of a step as a float-float leading term plus an FP32 correction (or
+// the FP32 atan2 / log form of kg_mixed.cuh); FP64 is left to the chunk starts (the direct
+// evaluation by Landen Jacobi functions and Carlson integrals of kg_ray.cuh seeds the state),
+// the samples next to a Pi pole, the increments the per-ray precision planner flags, and the
+// final horizon-adjacent sample.
 //
 // Same sample order and outputs as ray_chunk (kg_ray.cuh); the formulas are those of
 // theta_step / radial_step / theta_assemble / radial_assemble / combine, regrouped so that

@@ -8,7 +8,7 @@
 // allocator. kgeo_raytrace needs per-ray scratch (the ray records the sample kernel reads)
 // and either takes it from the caller or allocates it; this entry point does neither.
 //
-// The cost: the array below (KGEO_NOALLOC_MAX_PIXELS rays' records and sort keys, about 9.9 MB) is part of
+// The cost: the array below (KGEO_NOALLOC_MAX_PIXELS rays' records and sort keys, about 13.2 MB) is part of
 // the library's device image, so every GPU that loads the library holds it until the
 // process exits, whether or not this entry point is called.
 #include <cstring>
@@ -28,8 +28,10 @@ constexpr size_t kScratchBytes = workspace_bytes_n((size_t)kMaxPixels);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Device address of g_noalloc_scratch, looked up once per device. In host code the array's
-// name only stands in for the symbol; the address a kernel can use comes from the runtime.
+// Device address of g_noalloc_scratch, looked up once per device and kept for the process. In
+// host code the array's name only stands in for the symbol; the address a kernel can use comes
+// from the runtime. A cudaDeviceReset unloads the module and would leave the kept address
+// stale: the entry point is documented as not to be called on a device after its reset.
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_addr[kMaxDevices] = {nullptr};

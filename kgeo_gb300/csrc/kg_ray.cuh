@@ -65,6 +65,17 @@ enum RecField : int {
   S_RSN, S_RCN, S_RDN, S_RE, S_RP0, S_RP1, S_RP2, S_RC0, S_RC1, S_RC2,
   // observer constants the gain estimate needs
   G_A, G_RP, G_RM, G_RO,
+  // constants of the Pi increments' atan2 / log forms: sqrt|c| and n / (2 sqrt c) (c > 0) or
+  // n / sqrt(-c) (c < 0), theta then r
+  S_TQ, S_TQN, S_RQ0, S_RQ1, S_RQ2, S_RQN0, S_RQN1, S_RQN2,
+  // reciprocals and quotients of ray constants that the radial assembly would divide by at
+  // every sample (case 3: 1/(1 - al_i^2), al0^2/jd, 1/(al0^2 - 1), (2k - n0)/jd, 1/C16,
+  // 1/C17; case 4: 1/(1 + g_i^2))
+  R_D0, R_D1, R_D2, R_D3, R_D4, R_D5, R_D6, R_D7,
+  // coefficients of I_phi and I_t in I_+ and I_- (kgeo/kerr_raytracing_ana.py:626-633)
+  F_CP, F_CM, F_TP, F_TM,
+  // theta assembly: G_t = T_GTC (E - F) (ordinary motion), cos(theta) = T_NSQUP sn
+  T_GTC, T_NSQUP,
   NUM_FIELDS
 };
 
@@ -391,6 +402,14 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
   f[G_RP] = o.rplus;
   f[G_RM] = o.rminus;
   f[G_RO] = o.r_o;
+  {
+    const double rp = o.rplus, rm = o.rminus;
+    const double c2 = 2 * a / (rp - rm), c4 = 4 / (rp - rm);
+    f[F_CP] = c2 * (rp - 0.5 * a * lam);
+    f[F_CM] = c2 * (rm - 0.5 * a * lam);
+    f[F_TP] = c4 * (rp * rp - 0.5 * a * lam * rp);
+    f[F_TM] = c4 * (rm * rm - 0.5 * a * lam * rm);
+  }
 
   // u_+, u_- with clamps, kgeo/kerr_raytracing_utils.py:290-326
   Turning U = u_turning(o, lam, eta);
@@ -452,6 +471,8 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     f[T_GT] = Gt_o;
     f[T_UP] = up;
     f[T_UM] = um;
+    f[T_GTC] = kk == 0 ? 0.0 : -(2 * up * pref) / (2 * kk);
+    f[T_NSQUP] = -s * sqrt(up);
   }
   if (eta < 0.) {
     th = TH_VORT;
@@ -555,6 +576,7 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     const double g02 = g0 * g0, g02p1 = 1 + g02, g02j = 1 - k4 + g02;
     f[R_C23] = -1.0 / (g02p1 * g02j);           // S2 = S2a f[R_C23] + S1_0 f[R_C24]
     f[R_C24] = 1. / g02p1 + (1 - k4) / g02j;
+    for (int i = 0; i < 3; ++i) f[R_D0 + i] = 1.0 / (1 + g4[i] * g4[i]);
   }
   if (c3) {
     rcase = RCASE_3;
@@ -617,6 +639,15 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     f[R_C18] = sqrt((a0s - 1) / (k3 + (1 - k3) * a0s));  // p1 of R1_R2 for al0, alp, alm
     f[R_C19] = sqrt((aps - 1) / (k3 + (1 - k3) * aps));
     f[R_C20] = sqrt((ams - 1) / (k3 + (1 - k3) * ams));
+    const double jd = k3 + (1 - k3) * a0s;
+    f[R_D0] = 1.0 / (1 - a0s);
+    f[R_D1] = 1.0 / (1 - aps);
+    f[R_D2] = 1.0 / (1 - ams);
+    f[R_D3] = a0s / jd;
+    f[R_D4] = 1.0 / (a0s - 1);
+    f[R_D5] = (2 * k3 - nn3[0]) / jd;
+    f[R_D6] = 1.0 / f[R_C16];
+    f[R_D7] = 1.0 / f[R_C17];
   }
   if (c2) {
     rcase = RCASE_2;
@@ -769,6 +800,23 @@ KG_HD double pi_add_term(double n, double c, double snu, double snv, const Jacob
   return n * S3 / X;
 }
 
+// pi_add_term with q = sqrt|c| and qn = n / (2 q) (c > 0) or n / q (c < 0) taken from the
+// per-ray record (the same quotients, formed once per ray).
+KG_HD double pi_add_term_q(double n, double c, double q, double qn, double snu, double snv, const JacobiW& w) {
+  double S3 = snu * snv * w.sn;
+  double X = 1.0 - n * (w.sn * w.sn) + n * snu * snv * w.cn * w.dn;
+  double iX = rcp_fast(X);
+  double t = S3 * iX;
+  double z2 = c * (t * t);
+  if (X > 0.0 && fabs(z2) < 2.0e-3) return n * t * rc_one(-z2);
+  if (c > 0.0) {
+    double qs = q * S3;
+    return qn * log(fabs((X + qs) / (X - qs)));
+  }
+  if (c < 0.0) return qn * atan2(q * S3, X);
+  return n * t;
+}
+
 // ---- theta -----------------------------------------------------------------
 
 struct ThetaState {
@@ -830,11 +878,10 @@ KG_HD ThetaOut theta_assemble(const FV& f, int code, const ThetaState& st) {
   const double s = f[F_S];
   out.Gph = f[T_PREF] * st.pi - s * f[T_GPH];
   if (code_th(code) == TH_ORD) {
-    const double up = f[T_UP];
-    out.th = acos(-s * sqrt(up) * st.sn);
+    out.th = acos(f[T_NSQUP] * st.sn);
     double gt;
-    if (code_kk0(code)) gt = -2 * up * f[T_PREF] * 0.125 * (-2 * st.Phi + sin(2 * st.Phi));
-    else gt = -(2 * up * f[T_PREF] * st.e) / (2 * f[T_KK]);
+    if (code_kk0(code)) gt = -2 * f[T_UP] * f[T_PREF] * 0.125 * (-2 * st.Phi + sin(2 * st.Phi));
+    else gt = f[T_GTC] * st.e;
     out.Gt = gt - s * f[T_GT];
   } else {
     const double up = f[T_UP], um = f[T_UM];
@@ -853,7 +900,7 @@ KG_HD bool theta_step(const FV& f, ThetaState* st) {
   JacobiW w = jacobi_add(st->sn, st->cn, st->dn, snv, cnv, dnv, kk);
   double S3 = st->sn * snv * w.sn;
   if (near_pi_pole(n, st->sn, POLE_RHO_PI) || near_pi_pole(n, w.sn, POLE_RHO_PI)) return false;
-  double pi = st->pi - f[S_TPI] + pi_add_term(n, f[S_TC], st->sn, snv, w);
+  double pi = st->pi - f[S_TPI] + pi_add_term_q(n, f[S_TC], f[S_TQ], f[S_TQN], st->sn, snv, w);
   st->e = st->e - f[S_TE] - kk * S3;
   st->pi = pi;
   st->sn = w.sn;
@@ -959,7 +1006,7 @@ KG_HD bool radial_step(const FV& f, RadialState* st, double Xnew) {
       const double pic = i == 0 ? f[R_PIC0] : (i == 1 ? f[R_PIC1] : f[R_PIC2]);
       pnew[i] = pi_assemble(nn[i], am, (double)nr, Jsn * rf + (nn[i] / 3.0) * (Jsn * Jsn * Jsn) * rj, pic, k);
     } else {
-      pnew[i] = st->P[i] - sp[i] + pi_add_term(nn[i], sc[i], st->sn, snv, w);
+      pnew[i] = st->P[i] - sp[i] + pi_add_term_q(nn[i], sc[i], f[S_RQ0 + i], f[S_RQN0 + i], st->sn, snv, w);
     }
   }
   double p0 = pnew[0], p1 = pnew[1], p2 = pnew[2];
@@ -1018,13 +1065,12 @@ KG_HD RadialOut radial_assemble(const FV& f, int code, double tau, const RadialS
       double al2 = a_ * a_;
       double p1 = f[R_C18 + i];
       double f1 = 0.5 * p1 * log(fabs((p1 * dnX + snX) / (p1 * dnX - snX)));
-      R1[i] = (st.P[i] - a_ * f1) / (1 - al2);
+      R1[i] = (st.P[i] - a_ * f1) * f[R_D0 + i];
       (void)nn;
+      (void)al2;
     }
-    double al2 = al[0] * al[0];
-    double jd = k + (1 - k) * al2;
-    double R2 = (st.X - (al2 / jd) * (st.E - al[0] * snX * dnX / (1 + al[0] * cnX))) / (al2 - 1);
-    R2 = R2 + (2 * k - nn[0]) * R1[0] / jd;
+    double R2 = (st.X - f[R_D3] * (st.E - al[0] * snX * dnX / (1 + al[0] * cnX))) * f[R_D4];
+    R2 = R2 + f[R_D5] * R1[0];
     const bool use_m = !code_minspin(code);
     double R1m = use_m ? R1[2] : 0.0;
     double R1bm = use_m ? f[R_C10] : 0.0;
@@ -1036,8 +1082,8 @@ KG_HD RadialOut radial_assemble(const FV& f, int code, double tau, const RadialS
     double pr = f[R_C14];
     o.I1 = pr * (-tau) + Pi_1;
     o.I2 = (pr * pr) * (-tau) + 2 * pr * Pi_1 + f[R_C15] * Pi_2;
-    o.Ip = -((BB + AA) * (-tau) + Pi_p) / f[R_C16];
-    o.Im = -((BB + AA) * (-tau) + Pi_m) / f[R_C17];
+    o.Ip = -((BB + AA) * (-tau) + Pi_p) * f[R_D6];
+    o.Im = -((BB + AA) * (-tau) + Pi_m) * f[R_D7];
     return o;
   }
   if (rc == RCASE_4) {
@@ -1054,7 +1100,8 @@ KG_HD RadialOut radial_assemble(const FV& f, int code, double tau, const RadialS
       double al2p1 = 1 + al2;
       double p2 = f[R_C20 + i];
       double f2 = 0.5 * p2 * log(fabs(((1 - p2) * (1 + p2 * dnX)) / ((1 + p2) * (1 - p2 * dnX))));
-      S1[i] = (st.X + al2 * st.P[i] - al * f2) / al2p1;
+      S1[i] = (st.X + al2 * st.P[i] - al * f2) * f[R_D0 + i];
+      (void)al2p1;
     }
     double al2 = g0 * g0;
     double S2a = (1 - k) * st.X + al2 * st.E + al2 * dnX * (g0 - sc) / (1 + g0 * sc) - al2 * g0;
@@ -1080,10 +1127,10 @@ KG_HD RadialOut radial_assemble(const FV& f, int code, double tau, const RadialS
 // t, phi, sigma from the theta and r parts (kgeo/kerr_raytracing_ana.py:186-188, 626-633).
 template <class FV>
 KG_HD Sample combine(const Observer& ob, const FV& f, double tau, const ThetaOut& T, const RadialOut& R) {
-  const double a = ob.a, rp = ob.rplus, rm = ob.rminus, lam = f[F_LAM];
+  const double lam = f[F_LAM];
   double I_0 = -tau;
-  double I_phi = (2 * a / (rp - rm)) * ((rp - 0.5 * a * lam) * R.Ip - (rm - 0.5 * a * lam) * R.Im);
-  double I_tA = (4 / (rp - rm)) * ((rp * rp - 0.5 * a * lam * rp) * R.Ip - (rm * rm - 0.5 * a * lam * rm) * R.Im);
+  double I_phi = f[F_CP] * R.Ip - f[F_CM] * R.Im;
+  double I_tA = f[F_TP] * R.Ip - f[F_TM] * R.Im;
   double I_t = I_tA + 4 * I_0 + 2 * R.I1 + R.I2;
   Sample S;
   S.sig = 0 + R.I2 + ob.a2 * T.Gt;
@@ -1319,6 +1366,22 @@ KG_HD void mixed_gains(const GainArgs& g, const FV& f, int code, double* gain) {
 // Per-ray constants of one step of the even Mino grid (Mino step dtau): the Jacobi
 // functions and the integrals at the step itself. Sets CODE_STEP when the ray can be
 // stepped (finite constants, no n = 1 theta characteristic, not the a < MINSPIN limit).
+// q, qn of pi_add_term_q for characteristic n and c = n (m - n)(1 - n).
+KG_HD void pi_add_consts(double n, double c, double* q, double* qn) {
+  if (c > 0.0) {
+    const double sc = sqrt(c);
+    *q = sc;
+    *qn = n / (2.0 * sc);
+  } else if (c < 0.0) {
+    const double sc = sqrt(-c);
+    *q = sc;
+    *qn = n / sc;
+  } else {
+    *q = 0.0;
+    *qn = n;
+  }
+}
+
 template <class FV>
 KG_HD int step_constants(FV f, int code, double dtau, double* out /* f itself, writable */) {
   bool ok = dtau > 0 && std::isfinite(dtau) && code_rcase(code) != RCASE_NONE && code_th(code) != TH_ZERO &&
@@ -1347,6 +1410,8 @@ KG_HD int step_constants(FV f, int code, double dtau, double* out /* f itself, w
     out[S_RC0] = nn[0] * (k - nn[0]) * (1 - nn[0]);
     out[S_RC1] = nn[1] * (k - nn[1]) * (1 - nn[1]);
     out[S_RC2] = nn[2] * (k - nn[2]) * (1 - nn[2]);
+    pi_add_consts(n, out[S_TC], out + S_TQ, out + S_TQN);
+    for (int i = 0; i < 3; ++i) pi_add_consts(nn[i], out[S_RC0 + i], out + S_RQ0 + i, out + S_RQN0 + i);
     ok = n != 1.0 && std::isfinite(f[T_PIC]);
     for (int i = S_TSN; i <= S_RC2; ++i) ok = ok && std::isfinite(out[i]);
   }

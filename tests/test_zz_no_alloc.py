@@ -77,3 +77,34 @@ def test_noalloc_refuses_oversize_before_any_work(env):
     code = lib.kgeo_raytrace_noalloc(ctypes.byref(ob), None, None, 16385, 10, 1 - 1e-10, ctypes.byref(g), None)
     assert code == 11
     assert 'KGEO_NOALLOC_MAX_PIXELS' in _lib.status_string(code)
+
+
+def _default_pool_used_high(reset):
+    """High-water mark of the device's default memory pool (the pool cudaMallocAsync draws
+    from), through the CUDA driver API; reset=True sets it back to the current use first."""
+    import ctypes
+    cu = ctypes.CDLL('libcuda.so.1')
+    dev = ctypes.c_int(0)
+    assert cu.cuCtxGetDevice(ctypes.byref(dev)) == 0
+    pool = ctypes.c_void_p(0)
+    assert cu.cuDeviceGetDefaultMemPool(ctypes.byref(pool), dev) == 0
+    used_mem_high = 8  # CU_MEMPOOL_ATTR_USED_MEM_HIGH
+    v = ctypes.c_uint64(0)
+    if reset:
+        assert cu.cuMemPoolSetAttribute(pool, used_mem_high, ctypes.byref(v)) == 0
+    assert cu.cuMemPoolGetAttribute(pool, used_mem_high, ctypes.byref(v)) == 0
+    return v.value
+
+
+def test_noalloc_allocates_nothing(env):
+    """The defining property: a call draws nothing from the device's memory pool, where
+    kgeo_raytrace without a workspace does (stream-ordered cudaMallocAsync)."""
+    torch = env[0]
+    x = np.linspace(-8, 8, 40)
+    A, B = (v.flatten() for v in np.meshgrid(x, x))
+    torch.cuda.synchronize()
+    base = _default_pool_used_high(reset=True)
+    _run(env, 'kgeo_raytrace_noalloc', 0.7, 1.e4, 0.6, A, B, 32)
+    assert _default_pool_used_high(reset=False) == base
+    _run(env, 'kgeo_raytrace', 0.7, 1.e4, 0.6, A, B, 32)
+    assert _default_pool_used_high(reset=False) > base
