@@ -368,3 +368,23 @@ def test_region2_r_equatorial_vs_oracle(kg, golden, name):
     got = kg.raytrace_ana(a=a, observer_coords=[0, r_o, th_o, 0], image_coords=[g['alpha'], g['beta']],
                           ngeo=int(g['ngeo']), plotdata=False)
     np.testing.assert_allclose(got.tautot, g['tau_tot'], rtol=1e-12, atol=0)
+
+
+def test_no_loop_cap_on_fixture_traces(kg, golden):
+    """No Carlson duplication or Landen descent stops at its iteration cap on any fixture's rays
+    (setup and FP64 recurrence, and the mixed kernel): KGEO_FLAG_LOOP_CAP stays clear."""
+    import torch
+    from kgeo_gb300 import _lib, device as dev
+    for name in TRACES + ['band_a094_i17']:
+        g = golden(name)
+        a, r_o, th_o = float(g['a']), float(g['r_o']), float(g['th_o'])
+        res = dev.trace(a, r_o, th_o, dev.as_device(g['alpha']), dev.as_device(g['beta']), ngeo=int(g['ngeo']))
+        torch.cuda.synchronize()
+        assert not (int(res['flags'].item()) & _lib.FLAG_LOOP_CAP), name
+        if not np.isfinite(r_o):
+            continue
+        prep = dev.PreparedRays(a, r_o, th_o, dev.as_device(g['alpha']), dev.as_device(g['beta']), ngeo=int(g['ngeo']))
+        fl = torch.zeros(1, dtype=torch.int32, device='cuda')
+        prep.samples(prep.alloc(), mixed=True, flags=fl)
+        torch.cuda.synchronize()
+        assert not (int(fl.item()) & _lib.FLAG_LOOP_CAP), name + '-mixed'
