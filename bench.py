@@ -468,7 +468,8 @@ def run_reference(args):
 def mixed_workload(small=False):
     from kgeo_gb300.equatorial_lensing import critical_band
     a, th_o = 0.94, 17 * np.pi / 180
-    n = 256 if small else 2048
+    # the small (ncu capture) case: 384^2 + 512 x 32 band rays, about four waves of the kernel
+    n = 384 if small else 2048
     x = np.linspace(-LIM, LIM, n)
     A, B = (v.flatten() for v in np.meshgrid(x, x))
     bA, bB = critical_band(a, th_o, n_angles=512 if small else 4096, n_radii=32 if small else 256)

@@ -109,12 +109,15 @@ int kgeo_raytrace_mixed(const kgeo_observer* obs, const double* alpha, const dou
 /* raytrace_ana with HOST buffers end to end (kgeo/kerr_raytracing_ana.py:46-122, the call a
  * numpy caller makes): alpha, beta (npix) and every non-NULL output of `out` (t, r, th, ph,
  * sig, mino (ngeo, npix) row-major; tau_tot, rclass, thclass (npix); flags, one word) are
- * host pointers. The samples are computed in windows of whole recurrence chunks into a ring of
- * device buffers, and each window is copied to the host on a second stream while the next one
- * computes, so the device-to-host traffic (48 B per sample) overlaps the kernels; results
- * equal kgeo_raytrace / kgeo_raytrace_mixed (precision = KGEO_PRECISION_FP64 / _MIXED).
- * Page-locked host outputs (cudaHostAlloc, cudaHostRegister) are needed for the copies to
- * overlap; pageable ones work but serialise. workspace: device scratch of
+ * host pointers. Results equal kgeo_raytrace / kgeo_raytrace_mixed (precision =
+ * KGEO_PRECISION_FP64 / _MIXED). When every sample output is page-locked host memory that the
+ * device can address (cudaHostAlloc, cudaHostRegister: cudaPointerGetAttributes reports a device
+ * pointer for it), the sample kernel stores into the host outputs directly (48 B per sample over
+ * the host link, no staging, no copy engine). Otherwise the samples are computed in windows of
+ * whole recurrence chunks into a ring of device buffers, and each window is copied to the host
+ * on a second stream while the next one computes; pageable outputs work but serialise. On GB300
+ * the direct stores keep the call at the kernels' own time, where the copy engine's rate varies
+ * several-fold while FP64 kernels run beside it. workspace: device scratch of
  * kgeo_raytrace_host_workspace_size(npix, ngeo, precision) bytes, or NULL (allocated and freed
  * stream-ordered). The call returns once the work is queued on `stream`; the host outputs are
  * complete when that stream has synchronised. */

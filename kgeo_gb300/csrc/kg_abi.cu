@@ -244,6 +244,23 @@ struct HostPipe {
   }
 };
 
+// Device address of host memory the device can write directly (page-locked and mapped into the
+// unified address space); false for pageable memory (or a pointer the runtime does not know).
+bool device_view(const void* host, void** dev) {
+  if (!host) {
+    *dev = nullptr;
+    return true;
+  }
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return false;
+  *dev = at.devicePointer;
+  return true;
+}
+
 int raytrace_host(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix, int64_t ngeo,
                   double maxtaufrac, int mixed, kgeo_geodesics* out, void* workspace, size_t workspace_bytes_,
                   cudaStream_t s) {
@@ -283,6 +300,32 @@ int raytrace_host(const kgeo_observer* obs, const double* alpha, const double* b
   per.thclass = thclass;
   int st = setup_common(obs, al, be, npix, ngeo, maxtaufrac, w, &per, s);
   if (st) return st;
+  // the sample outputs as device addresses, when the host buffers allow it
+  void* dv[6];
+  const double* const hv[6] = {out->t, out->r, out->th, out->ph, out->sig, out->mino};
+  bool direct = true;
+  for (int j = 0; j < 6; ++j) direct = direct && device_view(hv[j], &dv[j]);
+  if (direct) {
+    kgeo_geodesics dout{};
+    dout.t = static_cast<double*>(dv[0]);
+    dout.r = static_cast<double*>(dv[1]);
+    dout.th = static_cast<double*>(dv[2]);
+    dout.ph = static_cast<double*>(dv[3]);
+    dout.sig = static_cast<double*>(dv[4]);
+    dout.mino = static_cast<double*>(dv[5]);
+    st = samples_common(obs, w, npix, ngeo, nullptr, 1, -1, mixed, &dout, s);
+    if (st) return st;
+    bool fail = false;
+    if (npix > 0)
+      fail = (out->tau_tot && cudaMemcpyAsync(out->tau_tot, tau_tot, bytes_px, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+             (out->rclass && cudaMemcpyAsync(out->rclass, rclass, sizeof(int32_t) * (size_t)npix,
+                                             cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+             (out->thclass && cudaMemcpyAsync(out->thclass, thclass, sizeof(int32_t) * (size_t)npix,
+                                              cudaMemcpyDeviceToHost, s) != cudaSuccess);
+    if (!fail && out->flags)
+      fail = cudaMemcpyAsync(out->flags, w.flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess;
+    return fail ? KGEO_ERR_CUDA : KGEO_OK;
+  }
   HostPipe pipe;
   if (!pipe.ok) return KGEO_ERR_CUDA;
   double* const host_out[6] = {out->t, out->r, out->th, out->ph, out->sig, out->mino};

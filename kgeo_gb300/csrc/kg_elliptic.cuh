@@ -104,10 +104,11 @@ KG_HD void rj_multi(double x, double y, double z, const double* p_in, double* rj
   double f = 1.0;   // 4^-m
   double f3 = 1.0;  // 4^-3m
   for (int it = 0;; ++it) {
-    // Carlson's stopping rule 4^-m Q < |A_m|, required of every integral in the set
-    bool done = f * Qf < fabs(Af);
+    // Carlson's stopping rule 4^-m Q < |A_m|, required of every integral in the set (written
+    // as "not >=" so that NaN arguments stop at once: their result is NaN, not a capped loop)
+    bool done = !(f * Qf >= fabs(Af));
 #pragma unroll
-    for (int i = 0; i < NP; ++i) done = done && (f * Q[i] < fabs(A[i]));
+    for (int i = 0; i < NP; ++i) done = done && !(f * Q[i] >= fabs(A[i]));
     if (done) break;
     if (it == CARLSON_MAX_IT) {
       note_loop_cap();

@@ -36,7 +36,27 @@ KG_HD ff ff_from(double x) {
   return ff{hi, (float)(x - (double)hi)};
 }
 
-KG_HD double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
+// float -> double without a conversion instruction for normal floats and zeros: the IEEE
+// fields moved by integer operations (exponent rebiased by 1023 - 127, mantissa shifted by
+// 52 - 23); denormals, infinities and NaNs take the conversion instruction. GB300 executes
+// float / double conversions on its FP64 pipe, at 1/64 of the FP32 rate. Exact either way.
+KG_HD double f2d_exact(float x) {
+#if defined(__CUDA_ARCH__)
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) {
+    if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)x;
+  }
+  const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hi, (int)(u << 29));
+#else
+  return (double)x;
+#endif
+}
+
+// hi + lo in double: exact (the two FP32 words together carry at most ~49 significant bits).
+KG_HD double ff_to_double(ff a) { return f2d_exact(a.hi) + f2d_exact(a.lo); }
 
 // s + e = a + b exactly, |b| <= |a| or a == 0
 KG_HD ff quick_two_sum(float a, float b) {

@@ -303,7 +303,7 @@ KG_HD float rc_one_m1_f(float e) {
 // increment); otherwise the FP32 atan2 / log form, or FP64 within MIXED_RHO of a pole or where
 // the planner flags the integral.
 KG_HD ff pi_inc_ff(const ff& nf, float c, const ff& S3, const ff& X, float rho_u, float rho_w, bool flagged,
-                   double nd, double cd, double snu, double snv, const FFState& w) {
+                   double nd, double cd, const ff& snu_f, double snv_neg, const FFState& w) {
   const float n = nf.hi;
   // n S3 sgn(X) R_C(X^2, X^2 - c S3^2) = n t R_C(1, 1 - z2) for either sign of X when c > 0
   // (the principal-value log form); for c < 0 and X < 0 the atan2 branch decides.
@@ -316,7 +316,7 @@ KG_HD ff pi_inc_ff(const ff& nf, float c, const ff& S3, const ff& X, float rho_u
     }
   }
   if (flagged || fabsf(rho_u) < (float)MIXED_RHO || fabsf(rho_w) < (float)MIXED_RHO)
-    return ff_from(pi_add_term(nd, cd, snu, snv, to_w(w)));
+    return ff_from(pi_add_term(nd, cd, ff_to_double(snu_f), -snv_neg, to_w(w)));
   return ff_c(pi_add_term_f(n, c, X.hi, S3.hi));
 }
 
@@ -388,7 +388,7 @@ KG_HD void ff_theta_step(const FV& f, const FFRay& c, int code, double tau, FFTh
     st->pi = theta_pi_direct(f, tau, w);
   } else {
     const ff inc = pi_inc_ff(c.tnf, c.tc, S3, X, st->rho, rho_w.hi, code_f64(code, 0), f[T_N], f[S_TC],
-                             ff_to_double(st->j.sn), -f[S_TSN], w);
+                             st->j.sn, f[S_TSN], w);
     st->pi = ff_add(ff_sub(st->pi, c.t_pi), inc);
   }
   st->j = w;
@@ -405,7 +405,6 @@ KG_HD void ff_radial_step(const FV& f, const FFRay& c, int code, FFRadial* st) {
   const ff uv = ff_mul(st->j.sn, c.rj.snv);
   const ff S3 = ff_mul(uv, w.sn);
   const ff q = ff_mul(uv, ff_mul(w.cn, w.dn));
-  const double snu_d = ff_to_double(st->j.sn);
   const double cd[3] = {f[S_RC0], f[S_RC1], f[S_RC2]};
   const double nd[3] = {f[R_N0], f[R_N1], f[R_N2]};
   const ff Xw = ff_sub(st->X, c.dX);
@@ -416,7 +415,7 @@ KG_HD void ff_radial_step(const FV& f, const FFRay& c, int code, FFRadial* st) {
     } else {
       const ff X = ff_add(rho_w[i], ff_mul(q, c.rnf[i]));
       const ff inc = pi_inc_ff(c.rnf[i], c.rc[i], S3, X, st->rho[i], rho_w[i].hi, code_f64(code, 1 + i), nd[i],
-                               cd[i], snu_d, -f[S_RSN], w);
+                               cd[i], st->j.sn, f[S_RSN], w);
       st->P[i] = ff_add(ff_sub(st->P[i], c.r_p[i]), inc);
     }
     st->rho[i] = rho_w[i].hi;
@@ -485,9 +484,9 @@ KG_HD ff ff_logratio(const ff& a) {
 template <class FV>
 KG_HD ff ff_logterm(const FV& f, const FFRay& c, int code, int rc, int i, const FFRadial& st) {
   const bool f64 = code_f64(code, 1 + i) || fabsf(st.rho[i]) < (float)MIXED_RHO;
-  const double ald = ff_to_double(c.alf[i]), pd = ff_to_double(c.ppf[i]);
   if (rc == RCASE_3) {
     if (f64) {
+      const double ald = ff_to_double(c.alf[i]), pd = ff_to_double(c.ppf[i]);
       const double sn = ff_to_double(st.j.sn), dn = ff_to_double(st.j.dn);
       return ff_from(ald * (0.5 * pd * log(fabs((pd * dn + sn) / (pd * dn - sn)))));
     }
@@ -495,6 +494,7 @@ KG_HD ff ff_logterm(const FV& f, const FFRay& c, int code, int rc, int i, const 
     return ff_mul(c.alf[i], ff_mul_f(ff_mul(L, c.ppf[i]), 0.5f));
   }
   if (f64) {
+    const double ald = ff_to_double(c.alf[i]), pd = ff_to_double(c.ppf[i]);
     const double dn = ff_to_double(st.j.dn);
     return ff_from(ald * (0.5 * pd * log(fabs(((1 - pd) * (1 + pd * dn)) / ((1 + pd) * (1 - pd * dn))))));
   }
@@ -589,7 +589,7 @@ KG_HD Sample ff_combine(const FFRay& c, const ff& tau, const FFOut& o) {
   S.t = ff_to_double(ff_add(I_t, a2Gt));
   S.ph = ff_to_double(ff_add(I_phi, ff_mul(c.lam, o.Gph)));
   S.r = ff_to_double(o.r);
-  S.th = (double)o.th;
+  S.th = f2d_exact(o.th);
   return S;
 }
 

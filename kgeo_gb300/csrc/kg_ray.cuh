@@ -113,7 +113,9 @@ KG_HD bool code_f64(int code, int i) { return (code >> (CODE_F64_SHIFT + i)) & 1
 
 // One Carlson evaluation at (x, y, z) for up to three Pi's plus R_D; rho[i] = the (scaled)
 // 1 - n_i sin^2. For rho_i < 0 the DLMF 19.20.14 transform is used; rho == 0 gives +inf
-// like the reference.
+// like the reference. A non-finite rho_i (an infinite characteristic, whose Pi the callers set
+// to the reference adapter's 0) gives NaN without entering the shared duplication, which a NaN
+// parameter would keep from converging.
 template <int NP>
 KG_HD void carlson_set(double x, double y, double z, const double* rho, double* rj, double* rd, double* rf) {
   double p[NP + 1];
@@ -124,7 +126,7 @@ KG_HD void carlson_set(double x, double y, double z, const double* rho, double* 
     neg[i] = !(rho[i] > 0.0);
     q[i] = -rho[i];
     p[i] = neg[i] ? (z * (x + y + q[i]) - x * y) / (z + q[i]) : rho[i];
-    if (rho[i] == 0.0) p[i] = z;  // placeholder, result replaced below
+    if (rho[i] == 0.0 || !std::isfinite(rho[i])) p[i] = z;  // placeholder, result replaced below
   }
   p[NP] = z;  // R_D(x,y,z) = R_J(x,y,z,z)
   double out[NP + 1];
@@ -134,6 +136,8 @@ KG_HD void carlson_set(double x, double y, double z, const double* rho, double* 
   for (int i = 0; i < NP; ++i) {
     if (rho[i] == 0.0) {
       rj[i] = kg_inf();
+    } else if (!std::isfinite(rho[i])) {
+      rj[i] = kg_nan();
     } else if (neg[i]) {
       double pq = p[i] * q[i];
       double xy = x * y;

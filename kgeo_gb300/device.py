@@ -94,8 +94,8 @@ _HOST_WS = {}
 def trace_host(a, r_o, th_o, alpha, beta, ngeo, maxtaufrac=1.0 - 1.0e-10, mixed=False, device=None):
     """kgeo_raytrace_host: numpy alpha, beta (npix) in, numpy outputs out.
 
-    The outputs live in page-locked host tensors (torch's pinned allocator caches them), so
-    each window's device-to-host copy overlaps the next window's kernel. Returns a dict of
+    The outputs live in page-locked host tensors (torch's pinned allocator caches them), which
+    the sample kernel stores into directly (no staging, no copies). Returns a dict of
     numpy arrays t, r, th, ph, sig, mino (ngeo, npix), tau_tot, rclass, thclass (npix) and
     the flags word (int).
     """

@@ -50,8 +50,8 @@ CHILD = textwrap.dedent('''
 
 
 def test_loop_cap_flag_clear_on_regular_inputs(tmp_path):
-    """The regular build: a trace of ordinary, vortical and horizon-bound rays and the
-    reference's elliptic-Pi points reach no cap."""
+    """The regular build: traces of ordinary, vortical and horizon-bound rays (a = 0 included)
+    and the reference's elliptic-Pi points reach no cap."""
     sys.path.insert(0, os.path.join(ROOT, 'tests'))
     import test_hostmath_cpu as T
     lib = str(tmp_path / 'libhm.so')
@@ -65,6 +65,9 @@ def test_loop_cap_flag_clear_on_regular_inputs(tmp_path):
     A, B = (g.flatten() for g in np.meshgrid(x, x))
     T.host_trace(L, 0.94, 1e4, 17 * np.pi / 180, A, B, 32)
     T.host_trace_stepped(L, 0.5, 1e4, 80 * np.pi / 180, A, B, 32, 16)
+    # a = 0: r_- = r_1 = 0 makes one radial characteristic infinite (its Pi is the adapter's 0)
+    T.host_trace(L, 0.0, 1e4, 45 * np.pi / 180, A, B, 16)
+    T.host_trace_stepped(L, 0.0, 1e4, 45 * np.pi / 180, A, B, 16, 8)
     g = np.load(os.path.join(ROOT, 'tests', 'golden', 'ellip_pi.npz'))
     for n, phi, m in zip(g['n'], g['phi'], g['m']):
         L.hm_ellippi(n, phi, m)

@@ -1,7 +1,8 @@
-"""kgeo_raytrace_host (host buffers in and out, windows of samples copied while the next
-window computes) gives exactly the outputs of kgeo_raytrace / kgeo_raytrace_mixed on device
-buffers: FP64 and mixed precision, more windows than ring buffers, a partial last window,
-fewer samples than one chunk, page-locked and pageable host outputs, empty inputs."""
+"""kgeo_raytrace_host (host buffers in and out) gives exactly the outputs of kgeo_raytrace /
+kgeo_raytrace_mixed on device buffers, on both of its paths: page-locked outputs the kernel
+stores into directly, and the window pipeline (samples computed into device buffers, each window
+copied while the next computes) that pageable outputs take: FP64 and mixed precision, more
+windows than ring buffers, a partial last window, fewer samples than one chunk, empty inputs."""
 import ctypes
 
 import numpy as np
@@ -87,3 +88,29 @@ def test_host_pipeline_raytrace_ana_and_edges():
     assert e['r'].shape == (50, 0)
     z = dev.trace_host(0.5, 1.e4, 1.0, A[:10], B[:10], 0)
     assert z['r'].shape == (0, 10)
+
+
+@pytest.mark.parametrize('mixed', [False, True])
+def test_host_pipeline_windows_with_one_pageable_output(mixed):
+    """One pageable sample output sends the call through the window pipeline (the other five
+    page-locked); the results are the device path's."""
+    from kgeo_gb300 import _lib
+    lib = _lib.load()
+    A, B = _pixels(12000, 5)
+    a, r_o, th_o, ngeo = 0.71, 1.e4, 0.9, 333
+    ref = _device_reference(a, r_o, th_o, A, B, ngeo, mixed)
+    out = {k: torch.empty((ngeo, A.size), dtype=torch.float64, pin_memory=True).numpy() for k in KEYS[:5]}
+    out['mino'] = np.empty((ngeo, A.size))
+    out['tau_tot'] = np.empty(A.size)
+    out['rclass'] = np.empty(A.size, np.int32)
+    out['thclass'] = np.empty(A.size, np.int32)
+    out['flags'] = np.zeros(1, np.int32)
+    g = _lib.GeodesicsOut(*[ctypes.c_void_p(out[k].ctypes.data) for k in KEYS + ('flags',)])
+    ob = _lib.Observer(a, r_o, th_o)
+    prec = _lib.PRECISION_MIXED if mixed else _lib.PRECISION_FP64
+    _lib.check(lib.kgeo_raytrace_host(ctypes.byref(ob), ctypes.c_void_p(A.ctypes.data), ctypes.c_void_p(B.ctypes.data),
+                                      A.size, ngeo, 1.0 - 1e-10, prec, ctypes.byref(g), None, 0, None))
+    torch.cuda.synchronize()
+    for k in KEYS:
+        assert np.array_equal(out[k], ref[k], equal_nan=True), k
+    assert int(out['flags'][0]) == int(ref['flags'][0])
