@@ -1352,6 +1352,8 @@ def run_batch(args, emit=True):
         torch.cuda.synchronize()
         a0, a1 = ev(), ev()
         a0.record(stream)
+        # the same pipeline as the batch's: per-ray setup, then the samples
+        prep.setup()
         prep.samples(out, chunk=0)
         a1.record(stream)
         torch.cuda.synchronize()
@@ -1401,7 +1403,8 @@ def run_batch(args, emit=True):
         'points_per_s': n_points / t_mixed,
         'fp64_batched_recurrence': {'value': n_rays / t_fp64, 'ms_per_step': t_fp64 * 1e3},
         'fp64_plain': {'value': plain_pts_per_s / pts_per_ray, 'points_per_s': plain_pts_per_s,
-                       'sample': 'images %s, independent evaluation per sample, scaled by points' % sub},
+                       'sample': 'images %s, per-ray setup + independent evaluation per sample (the batch '
+                                 'pipeline\'s stages), scaled by points' % sub},
         'speedup_vs_fp64_plain': (n_rays / t_mixed) / (plain_pts_per_s / pts_per_ray),
         'speedup_vs_fp64_recurrence': t_fp64 / t_mixed,
         'mixed_vs_fp64_error': mixed_err,

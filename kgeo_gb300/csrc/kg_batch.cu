@@ -309,12 +309,17 @@ int kgeo_batch_autotune(kgeo_batch_plan* p, int32_t budget_ms, void* stream, kge
   // candidates: block size x CTAs per SM x tile length x chunk length
   std::vector<kgeo_batch_config> cands;
   const bool mixed = p->precision == KGEO_PRECISION_MIXED;
-  const int chunks_m[] = {64, 128, 256};
+  // mixed chunks of at least 128 samples: every chunk starts with an FP64 direct evaluation
+  // (GB300 runs FP64 at 1/64 of the FP32 rate), which shorter chunks repeat; on the whole
+  // 64-image batch 64-sample chunks measured 6 % slower than 128, while the tuner's sparse
+  // subset of tiles could not tell them apart
+  const int chunks_m[] = {128, 256};
   const int chunks_d[] = {32, 50, 64};
+  const int nchunk = mixed ? 2 : 3;
   for (int block : {128, 256})
     for (int cps : {1, 2})
       for (int tmul : {1, 8})
-        for (int k = 0; k < 3; ++k) {
+        for (int k = 0; k < nchunk; ++k) {
           kgeo_batch_config c;
           c.block = block;
           c.ctas_per_sm = block == 256 ? cps : 2 * cps;

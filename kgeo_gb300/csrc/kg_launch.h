@@ -217,6 +217,21 @@ KG_HD int batch_find(const int64_t* off, int nimg, int64_t x) {
 }
 
 cudaError_t launch_batch_setup(const BatchArgs& a, cudaStream_t s);
+cudaError_t launch_batch_step(const BatchArgs& a, cudaStream_t s);
+
+#if defined(__CUDACC__)
+// End of a batch setup block: a capped loop in it is charged to the images of the block's first
+// and last rays (every thread of the block calls it; it synchronises).
+__device__ __forceinline__ void batch_loop_cap_end(const BatchArgs& a) {
+  __syncthreads();
+  if (threadIdx.x == 0 && kg_loop_cap_word && a.ntot > 0) {
+    const int64_t r0 = (int64_t)blockIdx.x * blockDim.x;
+    const int64_t r1 = r0 + blockDim.x - 1 < a.ntot ? r0 + blockDim.x - 1 : a.ntot - 1;
+    const int i0 = batch_find(a.pix_off, a.nimg, r0), i1 = batch_find(a.pix_off, a.nimg, r1);
+    for (int j = i0; j <= i1; ++j) atomicOr(a.flags + j, kg_loop_cap_word);
+  }
+}
+#endif
 cudaError_t launch_batch_samples(const BatchArgs& a, int block, int grid, cudaStream_t s);
 cudaError_t prepare_batch_kernels();
 
@@ -224,6 +239,7 @@ constexpr int IMAGE_BLOCK = 128;
 KG_HD constexpr int64_t image_adjoint_blocks(int64_t npix) { return (npix + IMAGE_BLOCK - 1) / IMAGE_BLOCK; }
 
 cudaError_t launch_ray_setup(const SetupArgs& a, cudaStream_t s);
+cudaError_t launch_ray_step(const SetupArgs& a, cudaStream_t s);
 // curve library (kg_curves.cu)
 struct CurveArgs {
   const CurveSpec* curves;  // (ncurves) device table

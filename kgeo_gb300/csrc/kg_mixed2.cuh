@@ -60,6 +60,26 @@ KG_HD float ff_rho(float n, const ff& sn2) { return ff_one_minus(ff_mul_f(sn2, n
 
 KG_HD bool rho_near_pole(float n, float rho) { return n > 0.0f && fabsf(rho) < (float)POLE_RHO; }
 
+#if defined(__CUDA_ARCH__)
+#define KG_COLD __device__ __noinline__
+#else
+#define KG_COLD inline
+#endif
+
+// The FP64 direct evaluations and FP64 fallbacks of the mixed recurrence run once per chunk or
+// at rare samples; out of line they keep the per-step loop's code compact.
+template <class FV>
+KG_COLD ThetaState theta_direct_cold(FV f, int code, double snarg) { return theta_state_direct(f, code, snarg); }
+template <class FV>
+KG_COLD RadialState radial_direct_cold(FV f, int code, double X) { return radial_state_direct(f, code, X, true); }
+KG_COLD double pi_add_term_cold(double n, double c, double snu, double snv, JacobiW w) {
+  return pi_add_term(n, c, snu, snv, w);
+}
+KG_COLD double log_term_cold(double ald, double pd, double sn, double dn, int rc3) {
+  if (rc3) return ald * (0.5 * pd * log(fabs((pd * dn + sn) / (pd * dn - sn))));
+  return ald * (0.5 * pd * log(fabs(((1 - pd) * (1 + pd * dn)) / ((1 + pd) * (1 - pd * dn)))));
+}
+
 // Constants of the radial assembly, by case (indices into FFRay::K).
 enum : int {
   // case 2
@@ -316,7 +336,7 @@ KG_HD ff pi_inc_ff(const ff& nf, float c, const ff& S3, const ff& X, float rho_u
     }
   }
   if (flagged || fabsf(rho_u) < (float)MIXED_RHO || fabsf(rho_w) < (float)MIXED_RHO)
-    return ff_from(pi_add_term(nd, cd, ff_to_double(snu_f), -snv_neg, to_w(w)));
+    return ff_from(pi_add_term_cold(nd, cd, ff_to_double(snu_f), -snv_neg, to_w(w)));
   return ff_c(pi_add_term_f(n, c, X.hi, S3.hi));
 }
 
@@ -336,7 +356,7 @@ constexpr float RESEED_RHO = 1.0e-3f;
 constexpr float DEEP_RHO = 1.0e-5f;
 
 template <class FV>
-KG_HD ff radial_pi_direct(const FV& f, int i, const FFRadial& st, const FFState& w, const ff& Xw) {
+KG_COLD ff radial_pi_direct(FV f, int i, FFState w, ff Xw) {
   const double X = ff_to_double(Xw);
   double v;
   const double nr = reduce_half_period(X, f[R_K2], &v);
@@ -348,7 +368,6 @@ KG_HD ff radial_pi_direct(const FV& f, int i, const FFRadial& st, const FFState&
   const double rf = carlson_rf(x, y, 1.0);
   const double rj = rj_any(x, y, 1.0, 1.0 - n * s2, rf);
   const double am = nr * PI + atan2(sn, cn);
-  (void)st;
   return ff_from(pi_assemble(n, am, nr, sn * rf + (n / 3.0) * (s2 * sn) * rj, pic, f[R_M]));
 }
 
@@ -356,7 +375,7 @@ KG_HD ff radial_pi_direct(const FV& f, int i, const FFRadial& st, const FFState&
 // values at parameter m follow from sn, cn, dn at parameter kk (J.dn = 1 / dn, J.cn = odd cn / dn,
 // sin(phi0) dn(v|m) = odd sn / dn), the half-period count from the sample's snarg.
 template <class FV>
-KG_HD ff theta_pi_direct(const FV& f, double tau, const FFState& w) {
+KG_COLD ff theta_pi_direct(FV f, double tau, FFState w) {
   const double x = theta_snarg(f, tau) / f[T_S1M];
   double v;
   const double nr = reduce_half_period(x, f[T_K2], &v);
@@ -411,7 +430,7 @@ KG_HD void ff_radial_step(const FV& f, const FFRay& c, int code, FFRadial* st) {
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     if (c.rn[i] > 0.0f && (fabsf(st->rho[i]) < RESEED_RHO || fabsf(rho_w[i].hi) < RESEED_RHO)) {
-      st->P[i] = radial_pi_direct(f, i, *st, w, Xw);
+      st->P[i] = radial_pi_direct(f, i, w, Xw);
     } else {
       const ff X = ff_add(rho_w[i], ff_mul(q, c.rnf[i]));
       const ff inc = pi_inc_ff(c.rnf[i], c.rc[i], S3, X, st->rho[i], rho_w[i].hi, code_f64(code, 1 + i), nd[i],
@@ -485,19 +504,14 @@ template <class FV>
 KG_HD ff ff_logterm(const FV& f, const FFRay& c, int code, int rc, int i, const FFRadial& st) {
   const bool f64 = code_f64(code, 1 + i) || fabsf(st.rho[i]) < (float)MIXED_RHO;
   if (rc == RCASE_3) {
-    if (f64) {
-      const double ald = ff_to_double(c.alf[i]), pd = ff_to_double(c.ppf[i]);
-      const double sn = ff_to_double(st.j.sn), dn = ff_to_double(st.j.dn);
-      return ff_from(ald * (0.5 * pd * log(fabs((pd * dn + sn) / (pd * dn - sn)))));
-    }
+    if (f64)
+      return ff_from(log_term_cold(ff_to_double(c.alf[i]), ff_to_double(c.ppf[i]), ff_to_double(st.j.sn),
+                                   ff_to_double(st.j.dn), 1));
     const ff L = ff_logratio(ff_div(st.j.sn, ff_mul(st.j.dn, c.ppf[i])));
     return ff_mul(c.alf[i], ff_mul_f(ff_mul(L, c.ppf[i]), 0.5f));
   }
-  if (f64) {
-    const double ald = ff_to_double(c.alf[i]), pd = ff_to_double(c.ppf[i]);
-    const double dn = ff_to_double(st.j.dn);
-    return ff_from(ald * (0.5 * pd * log(fabs(((1 - pd) * (1 + pd * dn)) / ((1 + pd) * (1 - pd * dn))))));
-  }
+  if (f64)
+    return ff_from(log_term_cold(ff_to_double(c.alf[i]), ff_to_double(c.ppf[i]), 0.0, ff_to_double(st.j.dn), 0));
   // ((1 - p2)(1 + p2 dn)) / ((1 + p2)(1 - p2 dn)) = (1 + y) / (1 - y) with
   // y = p2 (dn - 1) / (1 - p2^2 dn) and dn - 1 = -k sn^2 / (1 + dn): no cancellation as dn -> 1
   const ff om = ff_div(ff_mul(c.rkf, ff_sqr(st.j.sn)), ff_add_f(st.j.dn, 1.0f));
@@ -622,15 +636,15 @@ KG_HD void ray_chunk_ff(const Observer& ob, const FV& f, int code, int64_t g0, i
       FFOut o;
       ff_theta_assemble(c, ts, &o);
       const ThetaOut T{(double)o.th, ff_to_double(o.Gph), ff_to_double(o.Gt)};
-      const RadialState r0 = radial_state_direct(f, code, radial_X(f, tau), true);
+      const RadialState r0 = radial_direct_cold(f, code, radial_X(f, tau));
       emit(g, tau, combine(ob, f, tau, T, radial_assemble(f, code, tau, r0, true)));
       continue;
     }
     if (g == g0 || g == G - 1) {
       // chunk start (and a last sample that starts its chunk): FP64 direct evaluation (the start
       // seeds the float-float state)
-      const ThetaState t0 = theta_state_direct(f, code, theta_snarg(f, tau));
-      const RadialState r0 = radial_state_direct(f, code, radial_X(f, tau), true);
+      const ThetaState t0 = theta_direct_cold(f, code, theta_snarg(f, tau));
+      const RadialState r0 = radial_direct_cold(f, code, radial_X(f, tau));
       if (g == G - 1) {
         emit(g, tau, combine(ob, f, tau, theta_assemble(f, code, t0), radial_assemble(f, code, tau, r0, true)));
         continue;
@@ -641,11 +655,11 @@ KG_HD void ray_chunk_ff(const Observer& ob, const FV& f, int code, int64_t g0, i
       ff_theta_step(f, c, code, tau, &ts);
       ff_radial_step(f, c, code, &rs);
       if (c.tn > 0.0f && fabsf(ts.rho) < DEEP_RHO)
-        ts = ff_theta_from(theta_state_direct(f, code, theta_snarg(f, tau)), c.tnf);
+        ts = ff_theta_from(theta_direct_cold(f, code, theta_snarg(f, tau)), c.tnf);
       bool deep = false;
 #pragma unroll
       for (int i = 0; i < 3; ++i) deep = deep || (c.rn[i] > 0.0f && fabsf(rs.rho[i]) < DEEP_RHO);
-      if (deep) rs = ff_radial_from(radial_state_direct(f, code, radial_X(f, tau), true), c);
+      if (deep) rs = ff_radial_from(radial_direct_cold(f, code, radial_X(f, tau)), c);
     }
     FFOut o;
     const ff tau_ff = ff_mul_f(c.step, (float)g);

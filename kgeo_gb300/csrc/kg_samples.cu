@@ -97,6 +97,73 @@ __global__ void __launch_bounds__(256) stepped_kernel(SampleArgs a) {
   loop_cap_end(a.flags);
 }
 
+// Step constants of the even Mino grid (step_constants: the Jacobi values and integral
+// increments of one step, the recurrence and precision bits of the code word), after
+// ray_setup_kernel wrote the record; in this translation unit FMA contraction is allowed. Counts
+// the class buckets of the final code words.
+__global__ void __launch_bounds__(128) ray_step_kernel(SetupArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int key = -1;
+  loop_cap_begin();
+  if (i < a.npix) {
+    int code = a.code[i];
+    if (a.ngeo > 1) {
+      double f[NUM_FIELDS];
+#pragma unroll
+      for (int k = 0; k < NUM_FIELDS; ++k) f[k] = a.rec[(int64_t)k * a.npix + i];
+      code = step_constants<const double*>(f, code, f[F_TAUMAX] / (double)(a.ngeo - 1), f);
+#pragma unroll
+      for (int k = 0; k < NUM_FIELDS; ++k) a.rec[(int64_t)k * a.npix + i] = f[k];
+      a.code[i] = code;
+    }
+    key = ray_bucket(code);
+  }
+  // class-bucket counts, one atomic per distinct bucket of the warp
+  const unsigned grp = __match_any_sync(0xffffffffu, key);
+  if (key >= 0 && (threadIdx.x & 31) == (unsigned)(__ffs(grp) - 1)) atomicAdd(a.counts + key, (uint32_t)__popc(grp));
+  loop_cap_end(a.flags);
+}
+
+cudaError_t launch_ray_step(const SetupArgs& a, cudaStream_t s) {
+  if (a.npix <= 0) return cudaSuccess;
+  const int block = 128;
+  ray_step_kernel<<<(unsigned)((a.npix + block - 1) / block), block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// The same for every image of a batch.
+__global__ void __launch_bounds__(128) batch_step_kernel(BatchArgs a) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int key = -1;
+  loop_cap_begin();
+  if (r < a.ntot) {
+    const int im = batch_find(a.pix_off, a.nimg, r);
+    const BatchImage& B = a.img[im];
+    int code = a.code[r];
+    if (B.ngeo > 1) {
+      double f[NUM_FIELDS];
+#pragma unroll
+      for (int k = 0; k < NUM_FIELDS; ++k) f[k] = a.rec[(int64_t)k * a.ntot + r];
+      code = step_constants<const double*>(f, code, f[F_TAUMAX] / (double)(B.ngeo - 1), f);
+#pragma unroll
+      for (int k = 0; k < NUM_FIELDS; ++k) a.rec[(int64_t)k * a.ntot + r] = f[k];
+      a.code[r] = code;
+    }
+    key = im * NBUCKET + ray_bucket(code);
+  }
+  // bucket counts: one atomic per distinct (image, bucket) key of the warp
+  const unsigned grp = __match_any_sync(0xffffffffu, key);
+  if (key >= 0 && (int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(a.counts + key, (uint32_t)__popc(grp));
+  batch_loop_cap_end(a);
+}
+
+cudaError_t launch_batch_step(const BatchArgs& a, cudaStream_t s) {
+  if (a.ntot <= 0) return cudaSuccess;
+  const int block = 128;
+  batch_step_kernel<<<(unsigned)((a.ntot + block - 1) / block), block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 // Pi(n; phi | m) as the sample kernels' translation unit compiles it (FMA contraction on):
 // form 1 = ellip_set_at (the direct sample evaluators' path), form 2 = ellip_pi_ref.
 __global__ void __launch_bounds__(256) ellip_pi_samples_kernel(const double* n, const double* phi, const double* m,

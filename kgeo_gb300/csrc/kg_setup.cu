@@ -4,6 +4,11 @@
 
 namespace kg {
 
+// The per-ray setup in numpy's one-operation-at-a-time rounding (the classification decides
+// integer outputs, and several ray constants are ill-conditioned functions of the observer's
+// position that the reference evaluates in that rounding). The step constants of the even
+// Mino grid and the class-bucket counts follow in ray_step_kernel (kg_samples.cu), where FMA
+// contraction is allowed.
 __global__ void __launch_bounds__(128) ray_setup_kernel(SetupArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned fl = 0;
@@ -12,22 +17,17 @@ __global__ void __launch_bounds__(128) ray_setup_kernel(SetupArgs a) {
     RayRec R;
     int rc = 0, tc = 0;
     fl = ray_setup(a.obs, a.alpha[i], a.beta[i], a.maxtaufrac, &R, &rc, &tc);
-    if (a.ngeo > 1)
-      R.code = step_constants<const double*>(R.f, R.code, R.f[F_TAUMAX] / (double)(a.ngeo - 1), R.f);
+    const double* f = R.f;
 #pragma unroll
-    for (int k = 0; k < NUM_FIELDS; ++k) a.rec[(int64_t)k * a.npix + i] = R.f[k];
+    for (int k = 0; k < NUM_FIELDS; ++k) a.rec[(int64_t)k * a.npix + i] = f[k];
     a.code[i] = R.code;
     if (a.rclass) a.rclass[i] = rc;
     if (a.thclass) a.thclass[i] = tc;
-    if (a.tau_tot) a.tau_tot[i] = R.f[F_TAUTOT];
-    if (a.ngeo > 1 && R.f[F_TAUMAX] / (double)(a.ngeo - 1) == 0.0) fl |= FLAG_ANY_STEP_ZERO;
+    if (a.tau_tot) a.tau_tot[i] = f[F_TAUTOT];
+    if (a.ngeo > 1 && f[F_TAUMAX] / (double)(a.ngeo - 1) == 0.0) fl |= FLAG_ANY_STEP_ZERO;
   }
   fl = __reduce_or_sync(0xffffffffu, fl);
   if ((threadIdx.x & 31) == 0 && fl) atomicOr(a.flags, fl);
-  // class-bucket counts, one atomic per distinct bucket of the warp
-  const int key = i < a.npix ? ray_bucket(a.code[i]) : -1;
-  const unsigned grp = __match_any_sync(0xffffffffu, key);
-  if (key >= 0 && (threadIdx.x & 31) == (unsigned)(__ffs(grp) - 1)) atomicAdd(a.counts + key, (uint32_t)__popc(grp));
   loop_cap_end(a.flags);
 }
 
@@ -62,6 +62,7 @@ cudaError_t launch_ray_setup(const SetupArgs& a, cudaStream_t s) {
   const int block = 128;
   const int64_t grid = (a.npix + block - 1) / block;
   ray_setup_kernel<<<(unsigned)grid, block, 0, s>>>(a);
+  if (launch_ray_step(a, s) != cudaSuccess) return cudaGetLastError();
   bucket_scan_kernel<<<1, 32, 0, s>>>(a.counts);
   bucket_scatter_kernel<<<(unsigned)grid, block, 0, s>>>(a.code, a.npix, a.counts, a.perm);
   return cudaGetLastError();
@@ -127,9 +128,10 @@ __global__ void batch_item_offsets_kernel(BatchArgs a) {
   a.item_off[a.nimg] = acc;
 }
 
+// The per-ray setup of every image's rays (as ray_setup_kernel); batch_step_kernel
+// (kg_samples.cu) follows with the step constants and the bucket counts.
 __global__ void __launch_bounds__(128) batch_setup_kernel(BatchArgs a) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int key = -1;
   unsigned fl = 0;
   int im = 0;
   loop_cap_begin();
@@ -139,18 +141,14 @@ __global__ void __launch_bounds__(128) batch_setup_kernel(BatchArgs a) {
     RayRec R;
     int rc = 0, tc = 0;
     fl = ray_setup(B.obs, a.alpha[r], a.beta[r], B.maxtaufrac, &R, &rc, &tc);
-    if (B.ngeo > 1) {
-      const double step = R.f[F_TAUMAX] / (double)(B.ngeo - 1);
-      R.code = step_constants<const double*>(R.f, R.code, step, R.f);
-      if (step == 0.0) fl |= FLAG_ANY_STEP_ZERO;
-    }
+    const double* f = R.f;
+    if (B.ngeo > 1 && f[F_TAUMAX] / (double)(B.ngeo - 1) == 0.0) fl |= FLAG_ANY_STEP_ZERO;
 #pragma unroll
-    for (int k = 0; k < NUM_FIELDS; ++k) a.rec[(int64_t)k * a.ntot + r] = R.f[k];
+    for (int k = 0; k < NUM_FIELDS; ++k) a.rec[(int64_t)k * a.ntot + r] = f[k];
     a.code[r] = R.code;
     if (a.rclass) a.rclass[r] = rc;
     if (a.thclass) a.thclass[r] = tc;
-    if (a.tau_tot) a.tau_tot[r] = R.f[F_TAUTOT];
-    key = im * NBUCKET + ray_bucket(R.code);
+    if (a.tau_tot) a.tau_tot[r] = f[F_TAUTOT];
   }
   // flags: one atomic per image present in the warp (warp-uniform loop, full-mask reductions)
   const int lane = threadIdx.x & 31;
@@ -164,17 +162,7 @@ __global__ void __launch_bounds__(128) batch_setup_kernel(BatchArgs a) {
     if (lane == leader && v) atomicOr(a.flags + lim, v);
     pending &= ~in;
   }
-  // bucket counts: one atomic per distinct (image, bucket) key of the warp
-  const unsigned grp = __match_any_sync(0xffffffffu, key);
-  if (key >= 0 && lane == __ffs(grp) - 1) atomicAdd(a.counts + key, (uint32_t)__popc(grp));
-  // a capped loop in this block is charged to the images of the block's first and last rays
-  __syncthreads();
-  if (threadIdx.x == 0 && kg_loop_cap_word) {
-    const int64_t r0 = (int64_t)blockIdx.x * blockDim.x;
-    const int64_t r1 = r0 + blockDim.x - 1 < a.ntot ? r0 + blockDim.x - 1 : a.ntot - 1;
-    const int i0 = batch_find(a.pix_off, a.nimg, r0), i1 = batch_find(a.pix_off, a.nimg, r1);
-    for (int j = i0; j <= i1; ++j) atomicOr(a.flags + j, kg_loop_cap_word);
-  }
+  batch_loop_cap_end(a);
 }
 
 // Per image: exclusive scan of its NBUCKET counts into cursors that start at its first ray.
@@ -207,6 +195,7 @@ cudaError_t launch_batch_setup(const BatchArgs& a, cudaStream_t s) {
     const int block = 128;
     const unsigned grid = (unsigned)((a.ntot + block - 1) / block);
     batch_setup_kernel<<<grid, block, 0, s>>>(a);
+    if (launch_batch_step(a, s) != cudaSuccess) return cudaGetLastError();
     batch_scan_kernel<<<a.nimg, 32, 0, s>>>(a);
     batch_scatter_kernel<<<grid, block, 0, s>>>(a);
   }
