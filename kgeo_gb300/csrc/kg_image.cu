@@ -9,7 +9,7 @@ namespace kg {
 // OPTS: polarisation and / or path length requested (kg_polar.cuh); the plain image keeps
 // the shorter kernel.
 template <bool OPTS>
-__global__ void __launch_bounds__(IMAGE_BLOCK) image_kernel(ImageArgs a) {
+__global__ void __launch_bounds__(IMAGE_BLOCK, 1) image_kernel(ImageArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.npix) return;
   const Observer& o = a.obs;

@@ -25,7 +25,7 @@ __device__ void block_sum_nq(double* v, double* out) {
   }
 }
 
-__global__ void __launch_bounds__(IMAGE_BLOCK) image_adjoint_kernel(ImageAdjointArgs a) {
+__global__ void __launch_bounds__(IMAGE_BLOCK, 1) image_adjoint_kernel(ImageAdjointArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double acc[NQ];
 #pragma unroll
