@@ -112,14 +112,14 @@ struct FFRay {
   float al[3], pp[3];       // case 3: alpha_i, p1_i; case 4: g_i, p2_i
   ff alf[3];                // alpha_i / g_i in float-float (the log terms multiply them exactly)
   ff ppf[3];                // p1_i / p2_i in float-float
-  float drsc, dxs;          // case 2: rr31 rr43 rr41, -R_XS
-  ff drscf, dxsf;           // the same in float-float (dsn2 carries the factor 2)
+  ff dxsf;                  // case 2: -2 R_XS in float-float (dsn2 carries the factor 2)
   // combination
   ff cp, cm, tp, tm, a2, lam;
   ff step;                  // Mino step
   float pad;                // makes the size an odd number of 4-byte words (conflict-free
                             // shared-memory slots, one per thread)
 };
+static_assert(sizeof(FFRay) % 8 == 4, "FFRay slots must be an odd number of 4-byte words");
 
 template <class FV>
 KG_HD void ff_ray_consts(const Observer& ob, const FV& f, int code, double step, FFRay* c) {
@@ -167,8 +167,7 @@ KG_HD void ff_ray_consts(const Observer& ob, const FV& f, int code, double step,
   c->al[0] = c->al[1] = c->al[2] = c->pp[0] = c->pp[1] = c->pp[2] = 0.0f;
   c->alf[0] = c->alf[1] = c->alf[2] = ff_c(0.0f);
   c->ppf[0] = c->ppf[1] = c->ppf[2] = ff_c(0.0f);
-  c->drsc = c->dxs = 0.0f;
-  c->drscf = c->dxsf = ff_c(0.0f);
+  c->dxsf = ff_c(0.0f);
   if (rc == RCASE_2) {
     const double rr3 = f[R_C2], rr4 = f[R_C3], rr31 = f[R_C16], rr41 = f[R_C17], rr43 = f[R_C18];
     c->K[K2_N0] = ff_from(rr4 * rr31);
@@ -189,9 +188,6 @@ KG_HD void ff_ray_consts(const Observer& ob, const FV& f, int code, double step,
     c->K[K2_C15] = ff_from(f[R_C15]);
     c->K[K2_IC13] = ff_from(1.0 / f[R_C13]);
     c->K[K2_IC14] = ff_from(1.0 / f[R_C14]);
-    c->drsc = (float)(rr31 * rr43 * rr41);
-    c->dxs = (float)(-f[R_XS]);
-    c->drscf = ff_from(rr31 * rr43 * rr41);
     c->dxsf = ff_from(-2.0 * f[R_XS]);
   } else if (rc == RCASE_3) {
     const double AA = f[R_C0], BB = f[R_C1], rr1 = f[R_C2], rr2 = f[R_C3];
@@ -530,10 +526,10 @@ KG_HD void ff_radial_assemble(const FV& f, const FFRay& c, int code, const ff& t
     const ff den = ff_sub(K[K2_D0], ff_mul(K[K2_D1], sn2));
     const ff num = ff_sub(K[K2_N0], ff_mul(K[K2_N1], sn2));
     o->r = ff_div(num, den);
-    // H = dr/dX / (r - r3) - C8 in float-float (near the observer dr/dX ~ r^2 is large)
+    // H = dr/dX / (r - r3) - C8 = -rr41 dsn2 / den - C8 in float-float (r - r3 = rr31 rr43 / den
+    // and dr/dX = -rr31 rr43 rr41 dsn2 / den^2; near the observer dr/dX ~ r^2 is large)
     const ff dsn2 = ff_mul(ff_mul(st.j.sn, st.j.cn), ff_mul(st.j.dn, c.dxsf));
-    const ff drs = ff_neg(ff_div(ff_mul(c.drscf, dsn2), ff_sqr(den)));
-    const ff H = ff_sub(ff_div(drs, ff_sub(o->r, K[K2_RR3])), K[K2_C8]);
+    const ff H = ff_sub(ff_neg(ff_div(ff_mul(K[K2_D1], dsn2), den)), K[K2_C8]);
     const ff Eterm = ff_mul(K[K2_C12], ff_sub(st.E, K[K2_C4]));
     const ff Pi_1 = ff_mul(K[K2_C9], ff_sub(st.P[0], K[K2_C5]));
     const ff Pi_p = ff_mul(K[K2_C10], ff_sub(st.P[1], K[K2_C6]));

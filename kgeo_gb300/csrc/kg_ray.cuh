@@ -76,6 +76,9 @@ enum RecField : int {
   F_CP, F_CM, F_TP, F_TM,
   // theta assembly: G_t = T_GTC (E - F) (ordinary motion), cos(theta) = T_NSQUP sn
   T_GTC, T_NSQUP,
+  // products of the step's Jacobi values for the addition theorem (jacobi_add_q), theta then r:
+  // m sn_v^2, cn_v dn_v, sn_v dn_v, m sn_v cn_v with sn_v = -S_TSN (-S_RSN), the step's sign
+  S_TJ0, S_TJ1, S_TJ2, S_TJ3, S_RJ0, S_RJ1, S_RJ2, S_RJ3,
   NUM_FIELDS
 };
 
@@ -759,6 +762,25 @@ KG_HD JacobiW jacobi_add(double snu, double cnu, double dnu, double snv, double 
   return w;
 }
 
+// jacobi_add with the step's products q = (m sn_v^2, cn_v dn_v, sn_v dn_v, m sn_v cn_v) formed
+// once per ray.
+KG_HD JacobiW jacobi_add_q(double snu, double cnu, double dnu, double snv, double cnv, double dnv,
+                           const double q[4]) {
+  const double inv = rcp_fast(fma(-q[0], snu * snu, 1.0));
+  JacobiW w;
+  w.sn = fma(snu, q[1], snv * (cnu * dnu)) * inv;
+  w.cn = fma(-(snu * dnu), q[2], cnu * cnv) * inv;
+  w.dn = fma(-(snu * cnu), q[3], dnu * dnv) * inv;
+  return w;
+}
+
+KG_HD void jacobi_step_products(double snv, double cnv, double dnv, double m, double* q) {
+  q[0] = m * (snv * snv);
+  q[1] = cnv * dnv;
+  q[2] = snv * dnv;
+  q[3] = m * snv * cnv;
+}
+
 // Distance rho = 1 - n sn^2 to a pole (n > 1) or near-pole (n slightly below 1, at a
 // turning point close to the polar axis) of a Pi integrand. Within rho < POLE_RHO_PI of any
 // characteristic, at the previous or the new sample, the recurrence state's rounding is
@@ -784,14 +806,16 @@ KG_HD bool near_pi_pole(double n, double sn, double rho_max = POLE_RHO) {
 // written in branch-continuous form: (n / sqrt(-c)) atan2(sqrt(-c) S3, X) for c < 0 and
 // (n / 2 sqrt(c)) ln|(X + sqrt(c) S3) / (X - sqrt(c) S3)| for c > 0 (the principal value when
 // the step crosses a pole of the integrand, as the reference's Pi takes it there); the
-// R_C series when the ratio c S3^2 / X^2 is small.
+// R_C series n t R_C(1, 1 - c t^2), t = S3 / X, when z2 = c t^2 is small. For c > 0 the log
+// form is (n / sqrt c) atanh(sqrt(c) t) = n t R_C(1, 1 - z2) at either sign of X (past a pole,
+// X < 0); for c < 0 the series is the atan2 form only at X > 0 (at X < 0 atan2 adds +-pi).
 KG_HD double pi_add_term(double n, double c, double snu, double snv, const JacobiW& w) {
   double S3 = snu * snv * w.sn;
   double X = 1.0 - n * (w.sn * w.sn) + n * snu * snv * w.cn * w.dn;
   double iX = rcp_fast(X);
   double t = S3 * iX;
   double z2 = c * (t * t);
-  if (X > 0.0 && fabs(z2) < 2.0e-3) return n * t * rc_one(-z2);
+  if ((X > 0.0 || c > 0.0) && fabs(z2) < 2.0e-3) return n * t * rc_one(-z2);
   if (c > 0.0) {
     double sc = sqrt(c);
     double q = sc * S3;
@@ -812,7 +836,7 @@ KG_HD double pi_add_term_q(double n, double c, double q, double qn, double snu, 
   double iX = rcp_fast(X);
   double t = S3 * iX;
   double z2 = c * (t * t);
-  if (X > 0.0 && fabs(z2) < 2.0e-3) return n * t * rc_one(-z2);
+  if ((X > 0.0 || c > 0.0) && fabs(z2) < 2.0e-3) return n * t * rc_one(-z2);
   if (c > 0.0) {
     double qs = q * S3;
     return qn * log(fabs((X + qs) / (X - qs)));
@@ -901,7 +925,8 @@ template <class FV>
 KG_HD bool theta_step(const FV& f, ThetaState* st) {
   const double kk = f[T_KK], n = f[T_N];
   const double snv = -f[S_TSN], cnv = f[S_TCN], dnv = f[S_TDN];
-  JacobiW w = jacobi_add(st->sn, st->cn, st->dn, snv, cnv, dnv, kk);
+  const double q[4] = {f[S_TJ0], f[S_TJ1], f[S_TJ2], f[S_TJ3]};
+  JacobiW w = jacobi_add_q(st->sn, st->cn, st->dn, snv, cnv, dnv, q);
   double S3 = st->sn * snv * w.sn;
   if (near_pi_pole(n, st->sn, POLE_RHO_PI) || near_pi_pole(n, w.sn, POLE_RHO_PI)) return false;
   double pi = st->pi - f[S_TPI] + pi_add_term_q(n, f[S_TC], f[S_TQ], f[S_TQN], st->sn, snv, w);
@@ -971,7 +996,8 @@ template <class FV>
 KG_HD bool radial_step(const FV& f, RadialState* st, double Xnew) {
   const double k = f[R_M];
   const double snv = -f[S_RSN], cnv = f[S_RCN], dnv = f[S_RDN];
-  JacobiW w = jacobi_add(st->sn, st->cn, st->dn, snv, cnv, dnv, k);
+  const double q[4] = {f[S_RJ0], f[S_RJ1], f[S_RJ2], f[S_RJ3]};
+  JacobiW w = jacobi_add_q(st->sn, st->cn, st->dn, snv, cnv, dnv, q);
   const double nn[3] = {f[R_N0], f[R_N1], f[R_N2]};
   // characteristics whose pole is within POLE_RHO_PI of the previous sample or this one
   bool pole[3];
@@ -1044,8 +1070,9 @@ KG_HD RadialOut radial_assemble(const FV& f, int code, double tau, const RadialS
     double dX = -f[R_XS];
     double dsn2 = 2 * snX * cnX * dnX * dX;
     double den = rr31 - rr41 * sn2;
-    double drs = -(rr31 * rr43 * rr41 * dsn2 / (den * den));
-    double H = drs / (rs - rr3) - f[R_C8];
+    // H = (dr/dX) / (r - r3) - C8 with dr/dX = -rr31 rr43 rr41 dsn2 / den^2 and
+    // r - r3 = rr31 rr43 / den: the quotient is -rr41 dsn2 / den (no cancellation in r - r3)
+    double H = -(rr41 * dsn2) / den - f[R_C8];
     double Eterm = f[R_C12] * (st.E - f[R_C4]);
     double Pi_1 = f[R_C9] * (st.P[0] - f[R_C5]);
     double Pi_p = f[R_C10] * (st.P[1] - f[R_C6]);
@@ -1264,7 +1291,8 @@ KG_HD double theta_of_sn(const FV& f, int code, double sn) {
 template <class FV>
 KG_HD void radial_sncd_step(const FV& f, RadialState* st, double Xnew) {
   const double k = f[R_M];
-  JacobiW w = jacobi_add(st->sn, st->cn, st->dn, -f[S_RSN], f[S_RCN], f[S_RDN], k);
+  const double q[4] = {f[S_RJ0], f[S_RJ1], f[S_RJ2], f[S_RJ3]};
+  JacobiW w = jacobi_add_q(st->sn, st->cn, st->dn, -f[S_RSN], f[S_RCN], f[S_RDN], q);
   if (near_pi_pole(f[R_N0], st->sn, POLE_RHO_R) || near_pi_pole(f[R_N0], w.sn, POLE_RHO_R)) {
     double v;
     const int nr = (int)reduce_half_period(Xnew, f[R_K2], &v);
@@ -1303,7 +1331,8 @@ KG_HD void ray_chunk_rth(const FV& f, int code, int64_t g0, int64_t g1, int64_t 
       if (rdo) rs = radial_state_direct(f, code, X, false);
     } else {
       if (thact) {
-        const JacobiW w = jacobi_add(ts.sn, ts.cn, ts.dn, -f[S_TSN], f[S_TCN], f[S_TDN], f[T_KK]);
+        const double q[4] = {f[S_TJ0], f[S_TJ1], f[S_TJ2], f[S_TJ3]};
+        const JacobiW w = jacobi_add_q(ts.sn, ts.cn, ts.dn, -f[S_TSN], f[S_TCN], f[S_TDN], q);
         ts.sn = w.sn;
         ts.cn = w.cn;
         ts.dn = w.dn;
@@ -1414,10 +1443,13 @@ KG_HD int step_constants(FV f, int code, double dtau, double* out /* f itself, w
     out[S_RC0] = nn[0] * (k - nn[0]) * (1 - nn[0]);
     out[S_RC1] = nn[1] * (k - nn[1]) * (1 - nn[1]);
     out[S_RC2] = nn[2] * (k - nn[2]) * (1 - nn[2]);
+    jacobi_step_products(-ts.sn, ts.cn, ts.dn, kk, out + S_TJ0);
     pi_add_consts(n, out[S_TC], out + S_TQ, out + S_TQN);
     for (int i = 0; i < 3; ++i) pi_add_consts(nn[i], out[S_RC0 + i], out + S_RQ0 + i, out + S_RQN0 + i);
+    jacobi_step_products(-rs.sn, rs.cn, rs.dn, k, out + S_RJ0);
     ok = n != 1.0 && std::isfinite(f[T_PIC]);
     for (int i = S_TSN; i <= S_RC2; ++i) ok = ok && std::isfinite(out[i]);
+    for (int i = S_TJ0; i <= S_RJ3; ++i) ok = ok && std::isfinite(out[i]);
   }
   code = ok ? (code | CODE_STEP) : (code & ~CODE_STEP);
   // gains by which an error in each integral's increments reaches phi (scale 1) or t (scale r_o)

@@ -103,31 +103,31 @@ def _trace_worker(rank, world, port, q):
 
 def test_pixel_shards_concatenate_to_single_trace():
     """Rays are independent: the ranks' contiguous pixel ranges, concatenated, are the
-    single-process trace of the whole image, sample for sample."""
+    single-process trace of the whole image, sample for sample. Every trace runs in a spawned
+    process (world size 1 for the whole image), so all of them load the same host build."""
     import sys
     sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
-    import bench
     import test_hostmath_cpu as T
-    import ctypes
     if not os.path.exists(T.LIBPATH):
         import pytest
         pytest.skip('host build of the kernel headers missing')
-    for world in (2, 3):
+    results = {}
+    for world in (1, 2, 3):
         ctx = mp.get_context('spawn')
         q = ctx.Queue()
         port = _free_port()
         procs = [ctx.Process(target=_trace_worker, args=(r, world, port, q)) for r in range(world)]
         for p in procs:
             p.start()
-        parts = q.get(timeout=120)
+        results[world] = q.get(timeout=120)
         for p in procs:
             p.join(timeout=60)
             assert p.exitcode == 0
-        L = ctypes.CDLL(T.LIBPATH)
-        L.hm_setup.restype = ctypes.c_uint
-        a, th_o, A, B = bench.workload(0, grid=20)
-        whole = T.host_trace_stepped(L, a, bench.R_O, th_o, A, B, 40, 16)
-        assert [p[0] for p in parts] == sorted(p[0] for p in parts) and parts[-1][1] == A.size
+    whole = results[1][0][2]
+    npix = results[1][0][1]
+    for world in (2, 3):
+        parts = results[world]
+        assert [p[0] for p in parts] == sorted(p[0] for p in parts) and parts[-1][1] == npix
         assert all(parts[i][1] == parts[i + 1][0] for i in range(world - 1))
         for k in ('t', 'r', 'th', 'ph', 'sig', 'mino'):
             cat = np.concatenate([p[2][k] for p in parts], axis=1)
