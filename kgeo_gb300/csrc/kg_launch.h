@@ -48,8 +48,14 @@ inline Workspace carve_workspace(void* base, int64_t npix) {
   return w;
 }
 
-// Class bucket of a ray: radial case, theta branch, recurrence flag.
-KG_HD int ray_bucket(int code) { return code_rcase(code) * 6 + code_th(code) * 2 + (code_step(code) ? 1 : 0); }
+// Class bucket of a ray: recurrence flag, radial case, theta branch, ordered so that the
+// costliest work comes first in the sorted order (rays without the recurrence, evaluated
+// directly at every sample; then radial cases 4, 3, 2): the kernels take items in that order,
+// so the last blocks of a launch hold the cheapest rays and the launch ends without a long
+// tail (5 % on 512x512 x 400 samples, 5 % on the 5.2 M-ray mixed launch, measured on GB300).
+KG_HD int ray_bucket(int code) {
+  return (code_step(code) ? 16 : 0) + (4 - code_rcase(code)) * 3 + code_th(code);
+}
 
 struct SetupArgs {
   Observer obs;

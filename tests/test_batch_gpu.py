@@ -85,6 +85,51 @@ def test_batch_equals_single_images(precision):
     plan.close()
 
 
+def test_batch_configuration4_sizes():
+    """Three images of the 64-image batch workload (default_rng(0): sides 128-768, ngeo 64-256,
+    grids over [-12, 12] M), the smallest, a middle and the largest side, traced as one batch.
+    FP64: each image equals its single-image trace within 1e-9 of the parity scales. Mixed
+    precision: within the 1e-6 relative target of that FP64 trace (r 1e-7, theta 5e-7, phi 1e-6,
+    t and sigma 1e-7 of r_o; r reaches 2.6e-8 on the 749^2 image at theta_o = 2.3 deg, where a
+    single 256-sample chunk runs from the observer to the horizon), the same non-finite samples."""
+    import bench
+    from kgeo_gb300.batch import BatchPlan
+    ims_all, A_all, B_all = bench.batch_workload()
+    offs = np.cumsum([0] + [im['npix'] for im in ims_all])
+    order = np.argsort([im['side'] for im in ims_all], kind='stable')
+    pick = [int(order[0]), int(order[len(order) // 2]), int(order[-1])]
+    ims = [{k: ims_all[i][k] for k in ('a', 'th_o', 'npix', 'ngeo')} for i in pick]
+    A = np.concatenate([A_all[offs[i]:offs[i + 1]] for i in pick])
+    B = np.concatenate([B_all[offs[i]:offs[i + 1]] for i in pick])
+    keys = ('t', 'r', 'th', 'ph', 'sig', 'mino')
+    outs, chunk = {}, None
+    for prec in ('fp64', 'mixed'):
+        plan = BatchPlan(ims, precision=prec)
+        plan.bind(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda())
+        plan.run()
+        torch.cuda.synchronize()
+        outs[prec] = [{k: plan.image(i)[k].clone() for k in keys} for i in range(len(ims))]
+        if prec == 'fp64':
+            chunk = plan.config['chunk']
+        plan.close()
+    off = 0
+    for i, im in enumerate(ims):
+        n = im['npix']
+        ref, _ = single(im, A[off:off + n], B[off:off + n], chunk, False)
+        got, mix = outs['fp64'][i], outs['mixed'][i]
+        for k in keys:
+            assert same(got[k], ref[k], 0.0 if k == 'mino' else 1e-9, SCALE[k]), (i, k)
+        for k, bar, floor in (('r', 1e-7, 0.0), ('th', 5e-7, 1.0), ('ph', 1e-6, 1.0), ('t', 1e-7, 1.e4),
+                              ('sig', 1e-7, 1.e4)):
+            x, y = mix[k], ref[k]
+            assert torch.equal(torch.isfinite(x), torch.isfinite(y)), (i, k)
+            fin = torch.isfinite(y)
+            e = (x[fin] - y[fin]).abs() / torch.clamp(y[fin].abs(), min=floor)
+            assert float(e.max()) <= bar, (i, k, float(e.max()))
+        del ref, got, mix
+        off += n
+
+
 def test_batch_autotune_and_graph_replay():
     from kgeo_gb300.batch import BatchPlan
     ims, A, B = batch_images(seed=5)
