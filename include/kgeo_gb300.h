@@ -395,9 +395,9 @@ int kgeo_jet_stokes(const kgeo_observer* obs, const double* alpha, const double*
  * same chunk length to rounding (the kernels may contract different multiply-adds; Mino times and
  * classes are identical). A plan and its bound buffers are used by one stream at a time.
  *
- * kgeo_batch_autotune times the sample kernel's launch shapes (block size, CTAs per SM, tile
- * length, samples per work item) on a subset of the bound batch's tiles within about budget_ms
- * and keeps the fastest; results are cached per device, precision and image sizes (the cache
+ * kgeo_batch_autotune times the sample kernel's launch shapes (block size, CTAs per SM, samples
+ * per work item; tiles of one item per thread) on a subset of the bound batch's tiles within
+ * about budget_ms and keeps the fastest; results are cached per device, precision and image sizes (the cache
  * and the BZ f(r) tables of kgeo_jet_stokes are the library's only global state, both
  * mutex-guarded), so a new plan for the same batch shape
  * starts tuned. kgeo_batch_graph_launch captures the whole run into a CUDA graph on first use

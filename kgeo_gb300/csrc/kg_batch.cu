@@ -90,12 +90,16 @@ BatchLayout layout(int64_t ntot, int nimg) {
   return L;
 }
 
+// Default launch shape: tiles of one item per thread (on the 64-image batch, full runs on GB300:
+// mixed 2112 ms with tiles of 256 items against 2452 ms with 1024 and 2614 ms with 2048;
+// FP64 2821 ms with two 256-thread blocks per SM against 3028 ms with one and tiles of 1024).
 kgeo_batch_config default_config(const kgeo_batch_plan* p) {
+  const bool mixed = p->precision == KGEO_PRECISION_MIXED;
   kgeo_batch_config c;
   c.block = 256;
-  c.ctas_per_sm = 1;
-  c.tile = 4 * 256;
-  c.chunk = p->precision == KGEO_PRECISION_MIXED ? DEFAULT_CHUNK_MIXED : DEFAULT_CHUNK;
+  c.ctas_per_sm = mixed ? 1 : 2;
+  c.tile = 256;
+  c.chunk = mixed ? DEFAULT_CHUNK_MIXED : DEFAULT_CHUNK;
   return c;
 }
 
@@ -306,27 +310,26 @@ int kgeo_batch_autotune(kgeo_batch_plan* p, int32_t budget_ms, void* stream, kge
     if (best) *best = p->cfg;
     return KGEO_OK;
   }
-  // candidates: block size x CTAs per SM x tile length x chunk length
+  // candidates: block size x CTAs per SM x chunk length, tiles of one item per thread. Full
+  // runs of the 64-image batch on GB300 set the list: tiles longer than a block were 16-24 %
+  // slower; mixed chunks of 64 samples 6 % slower than 128 (every chunk starts with an FP64
+  // direct evaluation, which GB300 runs at 1/64 of the FP32 rate), 128 within 2 % of 256; FP64
+  // chunks of 50 4 % slower than 64. The tuner's sparse subset of tiles cannot resolve a few per
+  // cent, so the list holds only shapes within a few per cent of the best full run.
   std::vector<kgeo_batch_config> cands;
   const bool mixed = p->precision == KGEO_PRECISION_MIXED;
-  // mixed chunks of at least 128 samples: every chunk starts with an FP64 direct evaluation
-  // (GB300 runs FP64 at 1/64 of the FP32 rate), which shorter chunks repeat; on the whole
-  // 64-image batch 64-sample chunks measured 6 % slower than 128, while the tuner's sparse
-  // subset of tiles could not tell them apart
-  const int chunks_m[] = {128, 256};
-  const int chunks_d[] = {32, 50, 64};
-  const int nchunk = mixed ? 2 : 3;
-  for (int block : {128, 256})
-    for (int cps : {1, 2})
-      for (int tmul : {1, 8})
-        for (int k = 0; k < nchunk; ++k) {
-          kgeo_batch_config c;
-          c.block = block;
-          c.ctas_per_sm = block == 256 ? cps : 2 * cps;
-          c.tile = tmul * block;
-          c.chunk = mixed ? chunks_m[k] : chunks_d[k];
-          if (valid_config(p, c)) cands.push_back(c);
-        }
+  const int shapes_m[][3] = {{256, 1, 256}, {256, 1, 128}, {128, 2, 256}};
+  const int shapes_d[][3] = {{256, 2, 64}, {128, 2, 64}, {128, 4, 64}, {256, 1, 64}};
+  const int nshape = mixed ? 3 : 4;
+  for (int k = 0; k < nshape; ++k) {
+    const int* sh = mixed ? shapes_m[k] : shapes_d[k];
+    kgeo_batch_config c;
+    c.block = sh[0];
+    c.ctas_per_sm = sh[1];
+    c.tile = sh[0];
+    c.chunk = sh[2];
+    if (valid_config(p, c)) cands.push_back(c);
+  }
   // setup once; each candidate then times its sample kernel on every S-th tile, S chosen so
   // that a candidate costs about budget / (number of candidates)
   int st = run_pipeline(p, p->cfg, 1 << 20, s);
