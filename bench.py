@@ -363,17 +363,31 @@ def north_star_extras(args):
         torch.cuda.empty_cache()
 
     def err_summary(e):
-        return {k: {'max': v['max'], 'rms': v['rms'], 'frac_above_1e-6': v.get('frac_above_1e-6')}
-                for k, v in e.items() if isinstance(v, dict)}
-    # configuration 3: mixed vs the FP64 recurrence and the plain FP64 kernel
+        if e is None:
+            return None
+        keep = ('max', 'rms', 'frac_above_1e-6', 'max_over_bar', 'horizon_sample_max')
+        res = {k: {q: v[q] for q in keep if q in v} for k, v in e.items()
+               if isinstance(v, dict) and k != 'max_over_parity_bar'}
+        for k in ('max_over_parity_bar', 'parity_bar'):
+            if k in e:
+                res[k] = e[k]
+        return res
+    # configuration 3: mixed vs the FP64 recurrence and the plain FP64 kernel; both GPU paths
+    # against the oracle on a seeded 1/64 subsample of the rays (band included), on the host
+    # cores after the GPU timings
     sub.case, sub.steps, sub.warmup = 'mixed', 2, 3
+    sub.no_cpu_baseline = False
     m = run_mixed(sub, emit=False)
+    sub.no_cpu_baseline = True
     out['config3_mixed'] = {
         'rays_per_s': m['value'], 'ms_per_step': m['ms_per_step'],
         'fp64_recurrence_rays_per_s': m['fp64_recurrence']['value'], 'fp64_plain_rays_per_s': m['fp64_plain']['value'],
         'speedup_vs_fp64_recurrence': m['speedup_vs_fp64_recurrence'], 'speedup_vs_fp64_plain': m['speedup_vs_fp64_plain'],
-        'mixed_vs_fp64_recurrence_error': err_summary(m['mixed_vs_fp64_error']), 'clocks': m['clocks'],
-        'workload': m['config']['workload']}
+        'mixed_vs_fp64_recurrence_error': err_summary(m['mixed_vs_fp64_error']),
+        'fp64_vs_oracle_error': err_summary(m['fp64_vs_oracle_error']),
+        'mixed_vs_oracle_error': err_summary(m['mixed_vs_oracle_error']),
+        'oracle_rays': (m['fp64_vs_oracle_error'] or {}).get('rays'),
+        'error_scales': m['error_scales'], 'clocks': m['clocks'], 'workload': m['config']['workload']}
     free()
     # configuration 4: 64 images in one persistent launch / CUDA graph
     sub.case, sub.steps, sub.warmup = 'batch', 2, 3
@@ -578,6 +592,18 @@ def run_mixed(args, emit=True):
         orc['rays'] = int(sub.size)
         orc_m = error_stats({k: out_m[k][:, idx] for k in refd}, refd, rct, torch, rho)
         orc_m['rays'] = int(sub.size)
+        # the parity bars themselves: FP64 max(1e-10, 10 eps / rho, 10 S) and mixed
+        # max(1e-6, 10 eps / rho, 10 S), S = the oracle's change under a one-ulp change of
+        # lambda or eta (evaluated for the rays above the other bars); max of error / bar
+        from oracle.parity import lambda_eta_sensitivity, parity_ratios
+        refn = {k: ref[i] for i, k in enumerate(('r', 'th', 'ph', 't', 'sig'))}
+        rho_np = rho.cpu().numpy()
+        sens = lambda_eta_sensitivity(a, R_O, th_o, A[sub], B[sub], ngeo=G)
+        for err, outp, tol in ((orc, out_d, 1e-10), (orc_m, out_m, 1e-6)):
+            ratio = parity_ratios({k: outp[k][:, idx].cpu().numpy() for k in refn}, refn, R_O, tol, rho_np, sens)
+            err['max_over_parity_bar'] = {k: float(v.max()) / tol for k, v in ratio.items()}
+            err['parity_bar'] = 'max(%g, 10 eps / rho, 10 S)' % tol
+            del ratio
     points = npix * G
     line = {
         'metric': 'Kerr rays/s: mixed-precision raytrace (ngeo=256), 2048^2 grid + 256x4096 critical-curve band',
