@@ -790,12 +790,23 @@ KG_HD void jacobi_step_products(double snv, double cnv, double dnv, double m, do
 // The radial characteristic n0 is also the pole of the r
 // formula (r ~ 1 / (1 - n0 sn^2)), so r carries the recurrence's drift of sn amplified by
 // 1 / rho over the wider zone rho < POLE_RHO_R: there the step keeps its integrals but takes
-// sn, cn, dn from a direct Jacobi evaluation. (FP64 parity within the conditioning bar
-// max(1e-10, 10 eps / rho), measured over seeded 512x512-range draws.) POLE_RHO is the
-// float-float path's zone (kg_mixed.cuh, kg_mixed2.cuh).
+// sn, cn, dn from a direct Jacobi evaluation. The radial state's drift grows with the steps
+// taken since its sn, cn, dn were last evaluated directly (k), and with it the error the pole
+// amplifies: the radial Pi zone is POLE_RHO_PI up to k = PI_ZONE_K0 and widens in proportion to
+// k beyond (2.6e-3 at the 63rd step of a 64-sample chunk). On a seeded 1/64 of the
+// 2048^2-plus-band rays a flat 1e-3 zone left phi up to 1.2x the 1e-10 bar at k = 56-63 and rho
+// just above 1e-3 (0.6x at k < 32), from the radial Pi; with the widening zone 0.74x. The theta
+// zone stays at POLE_RHO_PI (widening it too cost 2 % more and moved phi's maximum to 0.73x).
+// (FP64 parity within the conditioning bar max(1e-10, 10 eps / rho), measured over seeded
+// 512x512-range draws and that workload.) POLE_RHO is the float-float path's zone (kg_mixed.cuh,
+// kg_mixed2.cuh).
 constexpr double POLE_RHO = 2.0e-2;
 constexpr double POLE_RHO_R = 5.0e-3;
 constexpr double POLE_RHO_PI = 1.0e-3;
+constexpr int PI_ZONE_K0 = 24;
+
+// The radial Pi zone after k steps of the recurrence since the last direct Jacobi evaluation.
+KG_HD double pi_zone(int k) { return k > PI_ZONE_K0 ? POLE_RHO_PI * ((double)k / PI_ZONE_K0) : POLE_RHO_PI; }
 
 KG_HD bool near_pi_pole(double n, double sn, double rho_max = POLE_RHO) {
   return n > 0.0 && fabs(1.0 - n * (sn * sn)) < rho_max;
@@ -946,6 +957,7 @@ struct RadialState {
   double E;           // E(am X | k)
   double P[3];        // Pi(n_i; am X | k)
   double am;          // amplitude (direct evaluations only)
+  int k = 0;          // recurrence steps since sn, cn, dn were last evaluated directly
 };
 
 struct RadialOut {
@@ -999,19 +1011,22 @@ KG_HD bool radial_step(const FV& f, RadialState* st, double Xnew) {
   const double q[4] = {f[S_RJ0], f[S_RJ1], f[S_RJ2], f[S_RJ3]};
   JacobiW w = jacobi_add_q(st->sn, st->cn, st->dn, snv, cnv, dnv, q);
   const double nn[3] = {f[R_N0], f[R_N1], f[R_N2]};
-  // characteristics whose pole is within POLE_RHO_PI of the previous sample or this one
+  // characteristics whose pole is within the Pi zone of the previous sample or this one
+  const double zone = pi_zone(st->k + 1);
   bool pole[3];
   int npole = 0;
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    pole[i] = near_pi_pole(nn[i], st->sn, POLE_RHO_PI) || near_pi_pole(nn[i], w.sn, POLE_RHO_PI);
+    pole[i] = near_pi_pole(nn[i], st->sn, zone) || near_pi_pole(nn[i], w.sn, zone);
     npole += pole[i] ? 1 : 0;
   }
   if (npole > 1) return false;
   // next to the pole of the r formula or of a Pi: fresh sn, cn, dn at the new argument
   int nr = 0;
   double Jsn = 0.0, am = 0.0;
+  bool fresh = false;
   if (npole == 1 || near_pi_pole(nn[0], st->sn, POLE_RHO_R) || near_pi_pole(nn[0], w.sn, POLE_RHO_R)) {
+    fresh = true;
     double v;
     nr = (int)reduce_half_period(Xnew, f[R_K2], &v);
     const Jacobi J = jacobi_landen(v, k);
@@ -1048,6 +1063,7 @@ KG_HD bool radial_step(const FV& f, RadialState* st, double Xnew) {
   st->cn = w.cn;
   st->dn = w.dn;
   st->X = Xnew;
+  st->k = fresh ? 0 : st->k + 1;
   return true;
 }
 
