@@ -172,3 +172,20 @@ def test_host_trace_vs_reference_fixture(hm, golden, name):
         check_trace(dict(r=rth['r'], th=rth['th'], t=g['t'], ph=g['ph'], sig=g['sig']),
                     dict(t=g['t'], r=g['r'], th=g['th'], ph=g['ph'], sig=g['sig']), r_o, g['rclass'],
                     name + '-rth', rho=rho)
+
+
+def test_recurrence_late_in_chunk_next_to_radial_pi_pole(hm):
+    """conftest.PI_ZONE_RAYS through the host build of the FP64 recurrence (chunks of 64)
+    against the oracle."""
+    from conftest import PI_ZONE_RAYS
+    from oracle import kgeo_oracle as ko
+    a, r_o, th_o, ngeo = 0.94, 1.e4, 17 * np.pi / 180, 256
+    x = np.linspace(-10, 10, 2048)
+    alpha = np.array([x[j] for i, j in PI_ZONE_RAYS])
+    beta = np.array([x[i] for i, j in PI_ZONE_RAYS])
+    ref = ko.raytrace(a, r_o, th_o, alpha, beta, ngeo)
+    rho = ko.pole_distance(a, r_o, th_o, alpha, beta, ref['mino_times'])
+    assert rho[:, 0].min() < 1.5e-3
+    st = host_trace_stepped(hm, a, r_o, th_o, alpha, beta, ngeo, 64)
+    check_trace(st, dict(t=ref['t'], r=ref['r'], th=ref['th'], ph=ref['ph'], sig=ref['affine_times']), r_o,
+                ref['rclass'], 'pi-zone-recurrence', rho=rho)

@@ -388,3 +388,23 @@ def test_no_loop_cap_on_fixture_traces(kg, golden):
         prep.samples(prep.alloc(), mixed=True, flags=fl)
         torch.cuda.synchronize()
         assert not (int(fl.item()) & _lib.FLAG_LOOP_CAP), name + '-mixed'
+
+
+def test_recurrence_late_in_chunk_next_to_radial_pi_pole(kg):
+    """Rays of the 2048^2 grid at a = 0.94, theta_o = 17 deg (ngeo = 256) whose radial Pi passes
+    within rho ~ 1.0e-3 of its pole late in a 64-sample recurrence chunk, where the re-seed zone
+    widens with the steps since the last direct Jacobi evaluation (phi was 1.21x the 1e-10 bar
+    with a flat zone), FP64 path against the oracle."""
+    import torch
+    from oracle import kgeo_oracle as ko
+    from conftest import PI_ZONE_RAYS
+    a, r_o, th_o, ngeo = 0.94, 1.e4, 17 * np.pi / 180, 256
+    x = np.linspace(-10, 10, 2048)
+    A = np.array([x[j] for i, j in PI_ZONE_RAYS])
+    B = np.array([x[i] for i, j in PI_ZONE_RAYS])
+    ref = ko.raytrace(a, r_o, th_o, A, B, ngeo)
+    got = _run(kg, a, r_o, th_o, A, B, ngeo)
+    torch.cuda.synchronize()
+    refd = dict(t=ref['t'], r=ref['r'], th=ref['th'], ph=ref['ph'], sig=ref['affine_times'])
+    rho = ko.pole_distance(a, r_o, th_o, A, B, ref['mino_times'])
+    check_trace(got, refd, r_o, ref['rclass'], 'pi-zone', rho=rho)
