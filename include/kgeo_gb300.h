@@ -231,7 +231,9 @@ typedef struct {
  * (kgeo/equatorial_images.py:23-122; per order Iobs, :124-264) on the caller's pixels
  * (alpha, beta), for the orders mbar = mbar_lo .. mbar_lo + n_orders - 1 in one pass over the
  * pixels (make_image: mbar_lo = 0, n_orders = mbar_max + 1; Iobs: one order). Q and U of the
- * reference are zero in this mode and are not produced. */
+ * reference are zero in this mode and are not produced. The threads take the pixels in
+ * radial-class order (a deterministic counting sort into about 8 B per pixel of stream-ordered
+ * scratch, cudaMallocAsync / cudaFreeAsync on the stream); every output stays at its pixel. */
 int kgeo_image(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha, const double* beta,
                int64_t npix, const kgeo_emission* model, kgeo_image_out* out, void* stream);
 
@@ -274,8 +276,10 @@ int kgeo_image_ex(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, c
  * (npix, n_orders) for the orders mbar_lo .. mbar_lo + n_orders - 1, writes grad[7] = dL/dq for q = (a, th_o, emis_p[0], emis_p[1],
  * vel_p[0], vel_p[1], vel_p[2]) to device memory. Masks, the momentum signs and Nmax are
  * held fixed (they are piecewise constant); the geodesic is recomputed, not stored.
- * workspace: device scratch of kgeo_image_adjoint_workspace_size(npix) bytes. Deterministic:
- * per-block partial sums are added in a fixed order. */
+ * workspace: device scratch of kgeo_image_adjoint_workspace_size(npix) bytes (per-block partial
+ * sums, then the radial-class pixel order of kgeo_image). Deterministic: the pixel order comes
+ * from a counting sort without atomics in its ranks, and the per-block partial sums are added
+ * in a fixed order. */
 size_t kgeo_image_adjoint_workspace_size(int64_t npix);
 int kgeo_image_adjoint(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha,
                        const double* beta, int64_t npix, const kgeo_emission* model, const double* grad_I, double* grad,

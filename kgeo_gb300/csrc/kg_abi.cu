@@ -699,11 +699,22 @@ int kgeo_image_ex(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, c
   ia.U = (ex && ia.opts.polarization) ? out->U : nullptr;
   ia.lp = (ex && ia.opts.pathlength) ? out->lp : nullptr;
   ia.Ie = (ex && ia.opts.pathlength) ? out->Ie : nullptr;
-  return launch_image(ia, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
+  ia.perm = nullptr;
+  if (npix == 0) return KGEO_OK;
+  // pixels in radial-class order (stream-ordered scratch, freed after the launch)
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  void* scratch = nullptr;
+  if (cudaMallocAsync(&scratch, pixel_sort_bytes(npix), s) != cudaSuccess) return KGEO_ERR_CUDA;
+  const bool ok = launch_pixel_sort(ia.obs, alpha, beta, npix, scratch, &ia.perm, s) == cudaSuccess &&
+                  launch_image(ia, s) == cudaSuccess;
+  const bool freed = cudaFreeAsync(scratch, s) == cudaSuccess;
+  return ok && freed ? KGEO_OK : KGEO_ERR_CUDA;
 }
 
+// per-block partial sums, then the pixel-order scratch
 size_t kgeo_image_adjoint_workspace_size(int64_t npix) {
-  return (size_t)(npix > 0 ? image_adjoint_blocks(npix) : 0) * NQ * sizeof(double);
+  if (npix <= 0) return 0;
+  return align_up((size_t)image_adjoint_blocks(npix) * NQ * sizeof(double), 256) + pixel_sort_bytes(npix);
 }
 
 int kgeo_image_adjoint(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orders, const double* alpha,
@@ -728,7 +739,13 @@ int kgeo_image_adjoint(const kgeo_observer* obs, int32_t mbar_lo, int32_t n_orde
   aa.grad_I = grad_I;
   aa.partial = static_cast<double*>(workspace);
   aa.grad = grad;
-  return launch_image_adjoint(aa, static_cast<cudaStream_t>(stream)) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
+  aa.perm = nullptr;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (npix > 0) {
+    char* sort_scratch = static_cast<char*>(workspace) + align_up((size_t)image_adjoint_blocks(npix) * NQ * sizeof(double), 256);
+    if (launch_pixel_sort(aa.obs, alpha, beta, npix, sort_scratch, &aa.perm, s) != cudaSuccess) return KGEO_ERR_CUDA;
+  }
+  return launch_image_adjoint(aa, s) == cudaSuccess ? KGEO_OK : KGEO_ERR_CUDA;
 }
 
 int kgeo_equatorial_crossings(const kgeo_observer* obs, const double* alpha, const double* beta, int64_t npix,

@@ -26,11 +26,12 @@ __device__ void block_sum_nq(double* v, double* out) {
 }
 
 __global__ void __launch_bounds__(IMAGE_BLOCK, 1) image_adjoint_kernel(ImageAdjointArgs a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double acc[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) acc[q] = 0.0;
-  if (i < a.npix) {
+  if (t < a.npix) {
+    const int64_t i = a.perm ? (int64_t)a.perm[t] : t;
     const Observer& o = a.obs;
     const double alpha = a.alpha[i], beta = a.beta[i];
     PixelGeo p;

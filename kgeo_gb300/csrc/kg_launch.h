@@ -157,6 +157,7 @@ struct ImageArgs {
   double* U;      // polarised: sin(2 chi) I
   double* lp;     // path length (pathlength)
   double* Ie;     // emission before g^3 (pathlength)
+  const int* perm;  // (npix) pixel order of the threads (launch_pixel_sort), or NULL for 0..npix-1
 };
 
 // Adjoint of the image: sum over pixels and orders of grad_I * dI/dq for the NQ parameters.
@@ -171,6 +172,7 @@ struct ImageAdjointArgs {
   const double* grad_I;  // (npix, nord)
   double* partial;       // (blocks, NQ) per-block sums
   double* grad;          // (NQ)
+  const int* perm;       // (npix) pixel order of the threads, or NULL
 };
 
 // ---------------------------------------------------------------------------
@@ -243,6 +245,23 @@ cudaError_t prepare_batch_kernels();
 
 constexpr int IMAGE_BLOCK = 128;
 KG_HD constexpr int64_t image_adjoint_blocks(int64_t npix) { return (npix + IMAGE_BLOCK - 1) / IMAGE_BLOCK; }
+
+// Pixel order of the image kernels (kg_image.cu): pixels sorted by radial class (eta <= 0
+// first, then rclass 1..4) with a deterministic counting sort, so that the lanes of a warp take
+// the same radial case; each pixel's values do not depend on the order, and the adjoint's block
+// sums stay in a fixed order. Scratch: key and permutation (int32 per pixel) and the
+// per-(class, block) counts.
+constexpr int PIX_SORT_BLOCK = 256;
+constexpr int PIX_BUCKETS = 8;
+KG_HD constexpr int64_t pixel_sort_blocks(int64_t npix) { return (npix + PIX_SORT_BLOCK - 1) / PIX_SORT_BLOCK; }
+KG_HD constexpr size_t pixel_sort_bytes(int64_t npix) {
+  return npix > 0 ? 2 * align_up(sizeof(int) * (size_t)npix, 256) +
+                        align_up(sizeof(uint32_t) * PIX_BUCKETS * (size_t)pixel_sort_blocks(npix), 256)
+                  : 0;
+}
+// Sorts the pixels into scratch (pixel_sort_bytes(npix) bytes); *perm points into it.
+cudaError_t launch_pixel_sort(const Observer& o, const double* alpha, const double* beta, int64_t npix, void* scratch,
+                              const int** perm, cudaStream_t s);
 
 cudaError_t launch_ray_setup(const SetupArgs& a, cudaStream_t s);
 cudaError_t launch_ray_step(const SetupArgs& a, cudaStream_t s);
