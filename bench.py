@@ -639,7 +639,7 @@ IMG_MBAR = 2
 # FP64 FLOP per pixel of the adjoint kernel on this workload (all three orders), from the
 # ncu capture of one launch on the 128x128 case (--case image-small): (dadd + dmul + 2 dfma
 # thread instructions) / pixels. Used for roofline.achieved.
-ADJ_FLOP_PER_PIXEL = 29170
+ADJ_FLOP_PER_PIXEL = 30083
 CPU_IMG_SAMPLE = 65536       # pixels of the bounded CPU sample (every 4th pixel)
 
 
