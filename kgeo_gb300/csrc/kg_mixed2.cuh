@@ -639,8 +639,9 @@ KG_HD void ray_chunk_ff(const Observer& ob, const FV& f, int code, int64_t g0, i
     if (g == g0 || g == G - 1) {
       // chunk start (and a last sample that starts its chunk): FP64 direct evaluation (the start
       // seeds the float-float state)
-      const ThetaState t0 = theta_direct_cold(f, code, theta_snarg(f, tau));
-      const RadialState r0 = radial_direct_cold(f, code, radial_X(f, tau));
+      const bool observer = g == 0 && G > 1 && tau == 0.0;
+      const ThetaState t0 = observer ? theta_state_seed(f) : theta_direct_cold(f, code, theta_snarg(f, tau));
+      const RadialState r0 = observer ? radial_state_seed(f, radial_X(f, tau)) : radial_direct_cold(f, code, radial_X(f, tau));
       if (g == G - 1) {
         emit(g, tau, combine(ob, f, tau, theta_assemble(f, code, t0), radial_assemble(f, code, tau, r0, true)));
         continue;

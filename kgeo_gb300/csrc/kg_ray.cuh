@@ -79,6 +79,9 @@ enum RecField : int {
   // products of the step's Jacobi values for the addition theorem (jacobi_add_q), theta then r:
   // m sn_v^2, cn_v dn_v, sn_v dn_v, m sn_v cn_v with sn_v = -S_TSN (-S_RSN), the step's sign
   S_TJ0, S_TJ1, S_TJ2, S_TJ3, S_RJ0, S_RJ1, S_RJ2, S_RJ3,
+  // the recurrence states at tau = 0 (the observer), from the setup's integrals at the
+  // observer's amplitudes: theta sn, cn, dn, e, pi; r sn, cn, dn, E, Pi_0..2
+  T_SN0, T_CN0, T_DN0, T_E0, T_PI0, R_SN0, R_CN0, R_DN0, R_E0, R_PA0, R_PA1, R_PA2,
   NUM_FIELDS
 };
 
@@ -459,6 +462,15 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     double F = ath.F;
     double Gth_o = -pref * F;
     double Gph_o = -pref * ath.P[0];
+    {
+      // state at tau = 0: snarg = -s F(arg | kk), so the amplitude is -s arg
+      const double sa = o.cos_th / sqrt(up);
+      f[T_SN0] = -s * sa;
+      f[T_CN0] = sqrt(1.0 - sa * sa);
+      f[T_DN0] = sqrt(1.0 - kk * (sa * sa));
+      f[T_E0] = -s * (ath.E - F);
+      f[T_PI0] = -s * ath.P[0];
+    }
     double Gt_o;
     if (kk == 0) Gt_o = 2 * up * pref * 0.125 * (-2 * arg + sin(2 * arg));
     else Gt_o = 2 * up * pref * (ath.E - F) / (2 * kk);
@@ -498,6 +510,15 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     double Gth_o = -h * prefA * ath.F;
     double Gph_o = -h * prefB * ath.P[0];
     double Gt_o = -h * prefC * ath.E;
+    {
+      // state at tau = 0: snarg = -s h F(nu_o | kk), amplitude -s h nu_o
+      const double sn = sqrt((o.cos2 - um) / (up - um));
+      f[T_SN0] = -s * h * sn;
+      f[T_CN0] = sqrt(1.0 - sn * sn);
+      f[T_DN0] = sqrt(1.0 - kk * (sn * sn));
+      f[T_E0] = -s * h * ath.E;
+      f[T_PI0] = -s * h * ath.P[0];
+    }
     double m = kk / (kk - 1);
     f[T_SCALE] = sqrt(a2um);
     f[T_GTH] = Gth_o;
@@ -540,6 +561,17 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     const double nn4[3] = {1 + g0 * g0, 1 + gp * gp, 1 + gm * gm};
     const EllipSet<3> comp = ellip_set_at<3>(HALFPI, k4, nn4, nullptr);
     const EllipSet<3> at = ellip_set_at<3>(aux, k4, nn4, &comp);
+    {
+      // state at tau = 0: X = F(aux | k), so sn = sin(aux), cn = cos(aux)
+      const double sn = sin(aux), cn = cos(aux);
+      f[R_SN0] = sn;
+      f[R_CN0] = cn;
+      f[R_DN0] = sqrt(1.0 - k4 * (sn * sn));
+      f[R_E0] = at.E;
+      f[R_PA0] = at.P[0];
+      f[R_PA1] = at.P[1];
+      f[R_PA2] = at.P[2];
+    }
     double Ir_o = pref * at.F;
     double S1b0, S2b0, S1bp, S1bm, dummy;
     s1s2_at(g0, aux, k4, at.F, at.E, at.P[0], true, &S1b0, &S2b0);
@@ -607,6 +639,17 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     const double nn3[3] = {a0s / (a0s - 1), aps / (aps - 1), ams / (ams - 1)};
     const EllipSet<3> comp = ellip_set_at<3>(HALFPI, k3, nn3, nullptr);
     const EllipSet<3> at = ellip_set_at<3>(aux, k3, nn3, &comp);
+    {
+      // state at tau = 0: X = F(aux | k), so sn = sin(aux), cn = cos(aux)
+      const double sn = sqrt(1.0 - x3ro * x3ro), cn = x3ro;
+      f[R_SN0] = sn;
+      f[R_CN0] = cn;
+      f[R_DN0] = sqrt(1.0 - k3 * (sn * sn));
+      f[R_E0] = at.E;
+      f[R_PA0] = at.P[0];
+      f[R_PA1] = at.P[1];
+      f[R_PA2] = at.P[2];
+    }
     double Ir_o = pref * at.F;
     double R1b0, R2b0, R1bp, R1bm = 0.0, dummy;
     r1r2_at(al0, aux, k3, at.F, at.E, at.P[0], true, &R1b0, &R2b0);
@@ -670,6 +713,17 @@ KG_HD unsigned ray_setup(const Observer& o, double alpha, double beta, double ma
     const double nn2[3] = {n1, np, nm};
     const EllipSet<3> comp = ellip_set_at<3>(HALFPI, k2, nn2, nullptr);
     const EllipSet<3> at = ellip_set_at<3>(aux, k2, nn2, &comp);
+    {
+      // state at tau = 0: X = F(aux | k), so sn = sin(aux), cn = cos(aux)
+      const double sn = x2ro, cn = sqrt(1.0 - x2ro * x2ro);
+      f[R_SN0] = sn;
+      f[R_CN0] = cn;
+      f[R_DN0] = sqrt(1.0 - k2 * (sn * sn));
+      f[R_E0] = at.E;
+      f[R_PA0] = at.P[0];
+      f[R_PA1] = at.P[1];
+      f[R_PA2] = at.P[2];
+    }
     double Ir_o = 2 * at.F / sqrt(rr31 * rr42);
     double Rpot_o = (r_o - rr1) * (r_o - rr2) * (r_o - rr3) * (r_o - rr4);
     double drs_o = sqrt(Rpot_o);
@@ -910,6 +964,20 @@ KG_HD double theta_snarg(const FV& f, double tau) {
   return f[T_SCALE] * (-tau + f[F_S] * f[T_GTH]);
 }
 
+// The theta state at tau = 0 (the observer) from the record: what theta_state_direct gives at
+// theta_snarg(f, 0), from the setup's integrals at the observer's amplitude.
+template <class FV>
+KG_HD ThetaState theta_state_seed(const FV& f) {
+  ThetaState st;
+  st.sn = f[T_SN0];
+  st.cn = f[T_CN0];
+  st.dn = f[T_DN0];
+  st.e = f[T_E0];
+  st.pi = f[T_PI0];
+  st.Phi = atan2(st.sn, st.cn);
+  return st;
+}
+
 // theta, G_phi, G_t from the state (kgeo/kerr_raytracing_ana.py:280-296, 355-363).
 template <class FV>
 KG_HD ThetaOut theta_assemble(const FV& f, int code, const ThetaState& st) {
@@ -967,6 +1035,22 @@ struct RadialOut {
 template <class FV>
 KG_HD double radial_X(const FV& f, double tau) {
   return f[R_XS] * (-tau + f[R_IRO]);
+}
+
+// The radial state at tau = 0 (X = radial_X(f, 0)) from the record, as theta_state_seed.
+template <class FV>
+KG_HD RadialState radial_state_seed(const FV& f, double X) {
+  RadialState st;
+  st.X = X;
+  st.sn = f[R_SN0];
+  st.cn = f[R_CN0];
+  st.dn = f[R_DN0];
+  st.E = f[R_E0];
+  st.P[0] = f[R_PA0];
+  st.P[1] = f[R_PA1];
+  st.P[2] = f[R_PA2];
+  st.am = atan2(st.sn, st.cn);
+  return st;
 }
 
 // Direct evaluation at X (kgeo/kerr_raytracing_ana.py:434-440, 510-515, 584-591 and the
@@ -1262,7 +1346,11 @@ KG_HD void ray_chunk(const Observer& ob, const FV& f, int code, int64_t g0, int6
   for (int64_t g = g0; g < g1; ++g) {
     const double tau = grid.at(g);
     const double X = radial_X(f, tau);
-    if (g == g0 || g == G - 1 || !stepping) {
+    if (g == 0 && G > 1 && stepping && tau == 0.0) {
+      // the observer: the setup's states
+      if (thact) ts = theta_state_seed(f);
+      if (rdo) rs = radial_state_seed(f, X);
+    } else if (g == g0 || g == G - 1 || !stepping) {
       if (thact) ts = theta_state_direct(f, code, theta_snarg(f, tau));
       if (rdo) rs = radial_state_direct(f, code, X, true);
     } else {
@@ -1342,7 +1430,10 @@ KG_HD void ray_chunk_rth(const FV& f, int code, int64_t g0, int64_t g1, int64_t 
   for (int64_t g = g0; g < g1; ++g) {
     const double tau = grid.at(g);
     const double X = radial_X(f, tau);
-    if (g == g0 || g == G - 1 || !stepping) {
+    if (g == 0 && G > 1 && stepping && tau == 0.0) {
+      if (thact) ts = theta_state_seed(f);
+      if (rdo) rs = radial_state_seed(f, X);
+    } else if (g == g0 || g == G - 1 || !stepping) {
       if (thact) ts = theta_sncd_direct(f, theta_snarg(f, tau));
       if (rdo) rs = radial_state_direct(f, code, X, false);
     } else {
