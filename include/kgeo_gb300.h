@@ -439,7 +439,7 @@ int kgeo_batch_graph_launch(kgeo_batch_plan* plan, void* stream);
  * device memory under a fixed budget, a latency-critical loop that cannot afford an
  * allocator call, or a host that offers no allocator. Same arguments, outputs and status
  * codes as kgeo_raytrace minus the workspace: the per-ray scratch lives in a fixed array
- * inside the library (room for KGEO_NOALLOC_MAX_PIXELS rays, about 14.3 MB of device memory
+ * inside the library (room for KGEO_NOALLOC_MAX_PIXELS rays, about 15.9 MB of device memory
  * that every GPU loading the library keeps until the process exits). Larger npix is
  * refused with KGEO_ERR_NOALLOC_SIZE before any work. The call allocates and frees nothing.
  * The first call on a device looks up the array's device address (cudaGetSymbolAddress)

@@ -8,7 +8,7 @@
 // allocator. kgeo_raytrace needs per-ray scratch (the ray records the sample kernel reads)
 // and either takes it from the caller or allocates it; this entry point does neither.
 //
-// The cost: the array below (KGEO_NOALLOC_MAX_PIXELS rays' records and sort keys, about 14.3 MB) is part of
+// The cost: the array below (KGEO_NOALLOC_MAX_PIXELS rays' records and sort keys, about 15.9 MB) is part of
 // the library's device image, so every GPU that loads the library holds it until the
 // process exits, whether or not this entry point is called.
 #include <cstring>
