@@ -494,24 +494,37 @@ KG_HD ff ff_logratio(const ff& a) {
 }
 
 // alpha_i times the log term of R1 (case 3, f1 = p1 / 2 L(sn / (p1 dn))) or S1 (case 4,
-// f2 = p2 / 2 (L(p2 dn) - L(p2))), in FP64 where the planner flags the integral or within
-// MIXED_RHO of the pole that the term cancels.
+// f2 = p2 / 2 (L(p2 dn) - L(p2))), in float-float, and in FP64 where the planner flags the
+// integral, within MIXED_LOG_RHO of the pole of the Pi it cancels, or next to the log's own pole
+// (0.99 < |x| < 1 / 0.99, where ff_logratio would fall back to FP32). The zone: host-build runs
+// of the mixed recurrence against the oracle on six 30x30 grids (a 0.2-0.94, theta_o 17-85 deg)
+// kept every output at the same fraction of its bar (phi 0.15) with a zone of 0.1, 0.05, 0.03,
+// 0.02 or 0.01, and missed the phi bar by up to 4.8x with none; with 0.1 (the increments' zone,
+// MIXED_RHO) 37-64 % of the log terms of case-3 and case-4 rays ran in FP64.
+KG_HD bool ff_log_near_pole(const ff& x) {
+  const float ax = fabsf(x.hi);
+  return ax > 0.99f && ax < 1.0f / 0.99f;
+}
+
+constexpr float MIXED_LOG_RHO = 0.03f;  // 3x the smallest zone measured to keep the bars
+
 template <class FV>
 KG_HD ff ff_logterm(const FV& f, const FFRay& c, int code, int rc, int i, const FFRadial& st) {
-  const bool f64 = code_f64(code, 1 + i) || fabsf(st.rho[i]) < (float)MIXED_RHO;
+  const bool flagged = code_f64(code, 1 + i) || fabsf(st.rho[i]) < MIXED_LOG_RHO;
   if (rc == RCASE_3) {
-    if (f64)
+    const ff x = ff_div(st.j.sn, ff_mul(st.j.dn, c.ppf[i]));
+    if (flagged || ff_log_near_pole(x))
       return ff_from(log_term_cold(ff_to_double(c.alf[i]), ff_to_double(c.ppf[i]), ff_to_double(st.j.sn),
                                    ff_to_double(st.j.dn), 1));
-    const ff L = ff_logratio(ff_div(st.j.sn, ff_mul(st.j.dn, c.ppf[i])));
+    const ff L = ff_logratio(x);
     return ff_mul(c.alf[i], ff_mul_f(ff_mul(L, c.ppf[i]), 0.5f));
   }
-  if (f64)
-    return ff_from(log_term_cold(ff_to_double(c.alf[i]), ff_to_double(c.ppf[i]), 0.0, ff_to_double(st.j.dn), 0));
   // ((1 - p2)(1 + p2 dn)) / ((1 + p2)(1 - p2 dn)) = (1 + y) / (1 - y) with
   // y = p2 (dn - 1) / (1 - p2^2 dn) and dn - 1 = -k sn^2 / (1 + dn): no cancellation as dn -> 1
   const ff om = ff_div(ff_mul(c.rkf, ff_sqr(st.j.sn)), ff_add_f(st.j.dn, 1.0f));
   const ff y = ff_neg(ff_div(ff_mul(c.ppf[i], om), ff_one_minus(ff_mul(ff_sqr(c.ppf[i]), st.j.dn))));
+  if (flagged || ff_log_near_pole(y))
+    return ff_from(log_term_cold(ff_to_double(c.alf[i]), ff_to_double(c.ppf[i]), 0.0, ff_to_double(st.j.dn), 0));
   const ff L = ff_logratio(y);
   return ff_mul(c.alf[i], ff_mul_f(ff_mul(L, c.ppf[i]), 0.5f));
 }
