@@ -35,8 +35,9 @@ KG_HD float pi_add_term_f(float n, float c, float X, float S3) {
   return n * t;
 }
 
-// Below this distance rho = |1 - n sn^2| to a Pi pole a characteristic's increment and the log
-// term that cancels its pole in R1 / S1 are kept in FP64 (FP32 would lose ~eps32 / rho).
+// Below this distance rho = |1 - n sn^2| to a Pi pole a characteristic's increment, where the
+// float-float R_C series does not apply, is kept in FP64 (the FP32 atan2 / log form would lose
+// ~eps32 / rho). The R1 / S1 log terms have their own, narrower zone (MIXED_LOG_RHO).
 constexpr double MIXED_RHO = 0.1;
 
 template <class FV>
