@@ -308,3 +308,40 @@ void hm_ff_ops(double a, double b, double* out) {
 double hm_ff_logratio(double a) { return ff_to_double(ff_logratio(ff_from(a))); }
 double hm_rc_one_m1(double e) { return (double)rc_one_m1_f((float)e); }
 }
+
+// The recurrence's observer states from the record (theta_state_seed, radial_state_seed) minus
+// the direct evaluations at tau = 0, per stepping ray: out[i * 10 + k] for theta sn, cn, dn, e,
+// pi and r sn, cn, dn, E, and the largest Pi difference over the three; the Pi differences are
+// relative to max(1, |Pi|) and scaled by min(1, rho), rho = |1 - n sn^2| the distance to the
+// pole that amplifies either evaluation's rounding (NaN where the ray does not step or has no
+// such part).
+extern "C" void hm_seed_check(const double* rec, const int* code, long n, double* out) {
+  for (long i = 0; i < n; ++i) {
+    double f[NUM_FIELDS];
+    for (int k = 0; k < NUM_FIELDS; ++k) f[k] = rec[k * n + i];
+    const double* fp = f;
+    double* q = out + i * 10;
+    for (int k = 0; k < 10; ++k) q[k] = NAN;
+    if (!code_step(code[i])) continue;
+    if (code_th(code[i]) != TH_ZERO) {
+      const ThetaState d = theta_state_direct<const double*>(fp, code[i], theta_snarg<const double*>(fp, 0.0));
+      const ThetaState s = theta_state_seed<const double*>(fp);
+      const double rho = fmin(1.0, fabs(1.0 - fp[T_N] * d.sn * d.sn));
+      q[0] = s.sn - d.sn; q[1] = s.cn - d.cn; q[2] = s.dn - d.dn; q[3] = s.e - d.e;
+      q[4] = (s.pi - d.pi) / fmax(1.0, fabs(d.pi)) * rho;
+    }
+    if (code_rcase(code[i]) != RCASE_NONE) {
+      const double X = radial_X<const double*>(fp, 0.0);
+      const RadialState d = radial_state_direct<const double*>(fp, code[i], X, true);
+      const RadialState s = radial_state_seed<const double*>(fp, X);
+      q[5] = s.sn - d.sn; q[6] = s.cn - d.cn; q[7] = s.dn - d.dn; q[8] = s.E - d.E;
+      double m = 0.0;
+      const double nn[3] = {fp[R_N0], fp[R_N1], fp[R_N2]};
+      for (int k = 0; k < 3; ++k) {
+        const double rho = fmin(1.0, fabs(1.0 - nn[k] * d.sn * d.sn));
+        m = fmax(m, fabs(s.P[k] - d.P[k]) / fmax(1.0, fabs(d.P[k])) * rho);
+      }
+      q[9] = m;
+    }
+  }
+}

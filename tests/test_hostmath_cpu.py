@@ -189,3 +189,40 @@ def test_recurrence_late_in_chunk_next_to_radial_pi_pole(hm):
     st = host_trace_stepped(hm, a, r_o, th_o, alpha, beta, ngeo, 64)
     check_trace(st, dict(t=ref['t'], r=ref['r'], th=ref['th'], ph=ref['ph'], sig=ref['affine_times']), r_o,
                 ref['rclass'], 'pi-zone-recurrence', rho=rho)
+
+
+@pytest.mark.parametrize('case', ['config2', 'vortical', 'south', 'region2'])
+def test_observer_states_match_direct_evaluation(hm, case):
+    """The recurrence starts its first chunk from the observer's states that the setup stores
+    (theta sn, cn, dn, e, pi at the amplitude -s arg or -s h nu_o; r sn, cn, dn, E, Pi at aux):
+    they equal the direct evaluation at tau = 0 to rounding."""
+    import bench
+    if case == 'config2':
+        a, th_o, A, B = bench.workload(0)
+        A, B = A[::41], B[::41]
+    else:
+        a, th_o = {'vortical': (0.99, 2.0), 'south': (0.7, 150.0), 'region2': (0.81, 99.0)}[case]
+        th_o *= np.pi / 180
+        x = np.linspace(-12, 12, 61)
+        A, B = (v.ravel() for v in np.meshgrid(x, x))
+    A = np.ascontiguousarray(A, float)
+    B = np.ascontiguousarray(B, float)
+    n = A.size
+    nf = hm.hm_num_fields()
+    ob = observer(a, 1.e4, th_o)
+    rec = np.zeros(nf * n)
+    code, rc, tc = (np.zeros(n, np.int32) for _ in range(3))
+    hm.hm_setup(dp(ob), dp(A), dp(B), ctypes.c_long(n), D(1 - 1e-10), dp(rec), ip(code), ip(rc), ip(tc),
+                ctypes.c_long(200))
+    out = np.full(n * 10, np.nan)
+    hm.hm_seed_check(dp(rec), ip(code), ctypes.c_long(n), dp(out))
+    out = out.reshape(n, 10)
+    stepping = ((code >> 10) & 1).astype(bool)
+    assert stepping.sum() > n // 2
+    d = np.abs(out[stepping])
+    assert np.isfinite(d[:, :9]).all()
+    # sn, cn, dn, E and theta's e to a few ulps; the Pi (relative to max(1, |Pi|)) to a few ulps
+    # over the pole distance, the bar of either evaluation near a pole
+    assert d[:, [0, 1, 2, 3, 5, 6, 7, 8]].max() <= 2e-13, d[:, [0, 1, 2, 3, 5, 6, 7, 8]].max(axis=0)
+    assert d[:, 4].max() <= 2e-14, d[:, 4].max()
+    assert np.nanmax(d[:, 9]) <= 2e-14, np.nanmax(d[:, 9])
