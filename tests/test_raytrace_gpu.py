@@ -408,3 +408,40 @@ def test_recurrence_late_in_chunk_next_to_radial_pi_pole(kg):
     refd = dict(t=ref['t'], r=ref['r'], th=ref['th'], ph=ref['ph'], sig=ref['affine_times'])
     rho = ko.pole_distance(a, r_o, th_o, A, B, ref['mino_times'])
     check_trace(got, refd, r_o, ref['rclass'], 'pi-zone', rho=rho)
+
+
+@pytest.mark.parametrize('part', ['grid', 'band'])
+def test_config3_random_rays_vs_oracle(kg, part):
+    """A seeded random 3,000 rays of the 2048^2-plus-band workload (a = 0.94, theta_o = 17 deg,
+    ngeo = 256), grid or band, through the FP64 recurrence (chunks of 64) and the mixed kernel
+    (chunks of 256) against the oracle, with the parity bars of oracle/parity.py: FP64 1e-10,
+    mixed 1e-6, both widened by the pole rule and the input-conditioning allowance."""
+    import torch
+    from oracle import kgeo_oracle as ko
+    from oracle.parity import parity_ratios
+    from kgeo_gb300 import device as dev
+    from kgeo_gb300.equatorial_lensing import critical_band
+    a, th = 0.94, 17 * np.pi / 180
+    rng = np.random.default_rng(17)
+    if part == 'grid':
+        x = np.linspace(-10, 10, 2048)
+        i, j = rng.integers(0, 2048, 3000), rng.integers(0, 2048, 3000)
+        A, B = x[j], x[i]
+    else:
+        bA, bB = critical_band(a, th, n_angles=4096, n_radii=256)
+        k = rng.choice(bA.size, 3000, replace=False)
+        A, B = bA[k], bB[k]
+    ref = ko.raytrace(a, 1.e4, th, A, B, 256)
+    refd = dict(t=ref['t'], r=ref['r'], th=ref['th'], ph=ref['ph'], sig=ref['affine_times'])
+    rho = ko.pole_distance(a, 1.e4, th, A, B, ref['mino_times'])
+    sens = lambda_eta_sensitivity(a, 1.e4, th, A, B, ngeo=256)
+    prep = dev.PreparedRays(a, 1.e4, th, dev.as_device(A), dev.as_device(B), ngeo=256)
+    for mixed, tol in ((False, 1e-10), (True, 1e-6)):
+        out = prep.samples(prep.alloc(fill=float('nan')), mixed=mixed)
+        torch.cuda.synchronize()
+        got = {k: v.cpu().numpy() for k, v in out.items()}
+        for k in refd:
+            assert np.array_equal(np.isfinite(got[k]), np.isfinite(refd[k])), (mixed, k)
+        ratio = parity_ratios(got, refd, 1.e4, tol, rho, sens)
+        worst = {k: float(v.max()) / tol for k, v in ratio.items()}
+        assert max(worst.values()) <= 1.0, (mixed, worst)
