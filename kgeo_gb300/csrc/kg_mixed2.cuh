@@ -72,6 +72,8 @@ template <class FV>
 KG_COLD ThetaState theta_direct_cold(FV f, int code, double snarg) { return theta_state_direct(f, code, snarg); }
 template <class FV>
 KG_COLD RadialState radial_direct_cold(FV f, int code, double X) { return radial_state_direct(f, code, X, true); }
+template <class FV>
+KG_COLD RadialState radial_sncd_cold(FV f, int code, double X) { return radial_state_direct(f, code, X, false); }
 KG_COLD double pi_add_term_cold(double n, double c, double snu, double snv, JacobiW w) {
   return pi_add_term(n, c, snu, snv, w);
 }
@@ -635,9 +637,12 @@ KG_HD void ray_chunk_ff(const Observer& ob, const FV& f, int code, int64_t g0, i
   const FFRay& c = *cp;
   FFTheta ts;
   FFRadial rs;
+  // a ray that ends at the horizon (radial cases 3 and 4, case 2 with r3 inside the horizon);
+  // an escaping ray's last sample is back at r_o, as conditioned as the others
+  const bool captured = code_rcase(code) != RCASE_2 || f[R_C2] < ob.rplus;
   for (int64_t g = g0; g < g1; ++g) {
     const double tau = grid.at(g);
-    if (g == G - 1 && g != g0) {
+    if (g == G - 1 && g != g0 && captured) {
       // the horizon-adjacent last sample: r, I_+-, I_1, I_2 diverge there (condition ~1e10), so
       // the radial part is the FP64 direct evaluation; theta stays well conditioned and takes
       // its float-float step
@@ -649,7 +654,7 @@ KG_HD void ray_chunk_ff(const Observer& ob, const FV& f, int code, int64_t g0, i
       emit(g, tau, combine(ob, f, tau, T, radial_assemble(f, code, tau, r0, true)));
       continue;
     }
-    if (g == g0 || g == G - 1) {
+    if (g == g0 || (g == G - 1 && captured)) {
       // chunk start (and a last sample that starts its chunk): FP64 direct evaluation (the start
       // seeds the float-float state)
       const bool observer = g == 0 && G > 1 && tau == 0.0;
@@ -664,6 +669,15 @@ KG_HD void ray_chunk_ff(const Observer& ob, const FV& f, int code, int64_t g0, i
     } else {
       ff_theta_step(f, c, code, tau, &ts);
       ff_radial_step(f, c, code, &rs);
+      if (g == G - 1) {
+        // an escaping ray's last sample, back at r_o next to the pole of the r formula: sn, cn,
+        // dn from the FP64 Jacobi evaluation (the integrals keep their steps)
+        const RadialState rj = radial_sncd_cold(f, code, radial_X(f, tau));
+        rs.j = ff_state(rj.sn, rj.cn, rj.dn);
+        const ff s2 = ff_sqr(rs.j.sn);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) rs.rho[i] = ff_one_minus(ff_mul(s2, c.rnf[i])).hi;
+      }
       if (c.tn > 0.0f && fabsf(ts.rho) < DEEP_RHO)
         ts = ff_theta_from(theta_direct_cold(f, code, theta_snarg(f, tau)), c.tnf);
       bool deep = false;
