@@ -1343,6 +1343,11 @@ KG_HD void ray_chunk(const Observer& ob, const FV& f, int code, int64_t g0, int6
   ts.sn = ts.cn = ts.dn = ts.e = ts.pi = ts.Phi = 0.0;
   rs.X = rs.sn = rs.cn = rs.dn = rs.E = rs.am = 0.0;
   rs.P[0] = rs.P[1] = rs.P[2] = 0.0;
+  // a ray that ends at the horizon (radial cases 3 and 4, case 2 with r3 inside the horizon):
+  // its last sample, 1e-10 tau_tot before the horizon, is evaluated directly; an escaping ray's
+  // last sample is back at r_o and takes its step (the zone of the r formula's pole refreshes
+  // sn, cn, dn there)
+  const bool captured = code_rcase(code) != RCASE_2 || f[R_C2] < ob.rplus;
   for (int64_t g = g0; g < g1; ++g) {
     const double tau = grid.at(g);
     const double X = radial_X(f, tau);
@@ -1350,7 +1355,7 @@ KG_HD void ray_chunk(const Observer& ob, const FV& f, int code, int64_t g0, int6
       // the observer: the setup's states
       if (thact) ts = theta_state_seed(f);
       if (rdo) rs = radial_state_seed(f, X);
-    } else if (g == g0 || g == G - 1 || !stepping) {
+    } else if (g == g0 || (g == G - 1 && captured) || !stepping) {
       if (thact) ts = theta_state_direct(f, code, theta_snarg(f, tau));
       if (rdo) rs = radial_state_direct(f, code, X, true);
     } else {
