@@ -49,11 +49,11 @@ CPU_SAMPLE_RAYS = 16384      # rays of the bounded CPU sample (every 16th pixel 
 # (--case small): (dadd + dmul + 2 dfma thread instructions) / points.
 # Used for roofline.achieved. FP64_INST_PER_POINT: FP64 pipe instructions (dadd + dmul +
 # dfma) per point, against the pipe's rate (fp64_peak / 2 instructions per second).
-FP64_FLOP_PER_POINT = 552.2
-FP64_INST_PER_POINT = 356.8
+FP64_FLOP_PER_POINT = 545.1
+FP64_INST_PER_POINT = 352.3
 # DRAM bytes per point of the same capture (dram__bytes_read + dram__bytes_write) / points; the
 # capture's 315 MB of output is 2.4x L2, so ~14 % of its writes are still in L2 when it ends
-DRAM_BYTES_PER_POINT = 45.74
+DRAM_BYTES_PER_POINT = 46.19
 BYTES_PER_POINT = 48          # t, r, theta, phi, sigma, Mino tau written per point (8 B each)
 L2_FLUSH_BYTES = 256 << 20
 
