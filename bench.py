@@ -21,7 +21,7 @@ collective), so every N traces the same image (strong scaling); a barrier + CUDA
 bracket the timed steps and the max time over ranks is reported.
 
 On one GPU the default run also measures the other configurations of the target and adds
-them to the same JSON line under "north_star" (--no-extras skips them): the
+them to the same JSON line under "configurations" (--no-extras skips them): the
 mixed-precision 2048^2-plus-band workload against the FP64 recurrence and the plain FP64
 kernel with the error statistics, the 64-image batch, the differentiable image
 (image + gradient per second) and the FP64 drop-in over the draws of seeds 0-7.
@@ -328,7 +328,7 @@ def run_ours(args):
     if world == 1 and args.case == 'full' and not args.no_extras:
         del prep, out, flush
         torch.cuda.empty_cache()
-        extras = north_star_extras(args)
+        extras = configuration_extras(args)
     line = {
         'metric': 'Kerr rays/s: FP64 raytrace_ana (ngeo=400) + r_equatorial n=0..2, 512x512 image',
         'value': value, 'unit': 'rays/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
@@ -344,12 +344,12 @@ def run_ours(args):
         'points_per_s': value * NGEO, 'kernel_ms': {'ray_setup': setup_ms, 'samples': samp_ms,
                                                     'r_equatorial': eq_ms},
         'roofline': roof, 'cpu_baseline': cpu, 'e2e': e2e, 'gpu_launches': launches, 'clocks': ck,
-        'north_star': extras,
+        'configurations': extras,
     }
     print(json.dumps(line))
 
 
-def north_star_extras(args):
+def configuration_extras(args):
     """The target's other configurations, measured in the same run (one GPU)."""
     import copy
     import torch
@@ -1453,7 +1453,7 @@ def main():
                                       'jet-small', 'stokes', 'stokes-small'),
                    default='full')
     p.add_argument('--no-cpu-baseline', action='store_true')
-    p.add_argument('--no-extras', action='store_true', help='skip the other configurations of the north_star key')
+    p.add_argument('--no-extras', action='store_true', help='skip the other configurations (the configurations key)')
     args = p.parse_args()
     if args.impl == 'reference':
         run_reference(args)
